@@ -1,0 +1,173 @@
+/*
+ * spectrax_gb300 — C ABI of the GB300 (sm_103a) Hermite-Fourier Vlasov-Maxwell
+ * right-hand side and its device time steppers.
+ *
+ * State layout (identical to SPECTRAX): a flat complex128 vector
+ *   y = concat(Ck.ravel(), Fk.ravel()),
+ *   Ck[(s, p, m, n), ky, kx, kz]  shape (Ns*Np*Nm*Nn, Ny, Nx, Nz),
+ *   Fk[(Ex, Ey, Ez, Bx, By, Bz), ky, kx, kz],
+ * Fourier axes in fftshift order (index c <-> wavenumber c - N//2), axis order (y, x, z).
+ * Complex values are interleaved (re, im) doubles; all device pointers must be
+ * 16-byte aligned.  Every function returns 0 (SPX_OK) or a negative SPX_E* code.
+ * Streams are passed as `void*` (a cudaStream_t; NULL = legacy default stream).
+ */
+#ifndef SPECTRAX_GB300_H
+#define SPECTRAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPX_MAX_SPECIES 8
+#define SPX_MAX_AXIS 256        /* largest Nx, Ny or Nz */
+
+enum {
+  SPX_OK = 0,
+  SPX_E_ARG = -1,        /* null pointer, bad size, unsupported shape */
+  SPX_E_CUDA = -2,       /* a CUDA call failed (see spx_last_error) */
+  SPX_E_WORKSPACE = -3,  /* workspace too small or misaligned */
+  SPX_E_UNSUPPORTED = -4 /* valid input that this build does not handle */
+};
+
+/* Stepper status words (per solve / per batch instance). */
+enum {
+  SPX_ST_RUNNING = 0,
+  SPX_ST_DONE = 1,
+  SPX_ST_MAX_STEPS = 2,
+  SPX_ST_DT_UNDERFLOW = 3,
+  SPX_ST_NONFINITE = 4
+};
+
+/*
+ * Problem description: the entries of the reference's 28-tuple `args`
+ * (spectrax/_simulation.py:154-161) that are not derivable, plus the 2/3-mask
+ * cutoffs.  The k-grids, nabla, k2, collision and ladder tables are rebuilt from
+ * these with the formulas of spectrax/_initialization.py:114-146.
+ */
+typedef struct spx_problem {
+  int32_t Nx, Ny, Nz;          /* Fourier modes per axis */
+  int32_t Nn, Nm, Np;          /* Hermite modes per velocity axis */
+  int32_t Ns;                  /* species, <= SPX_MAX_SPECIES */
+  int32_t cut_x, cut_y, cut_z; /* 2/3 mask: largest |k| kept per axis (-1 keeps none) */
+  double Lx, Ly, Lz;           /* box lengths */
+  double nu, D;                /* hypercollision and hyperdiffusion coefficients */
+  double qs[SPX_MAX_SPECIES];
+  double Omega_cs[SPX_MAX_SPECIES];
+  double alpha_s[3 * SPX_MAX_SPECIES];
+  double u_s[3 * SPX_MAX_SPECIES];
+} spx_problem;
+
+typedef struct spx_plan spx_plan;  /* opaque: device tables for one problem */
+
+/* Text of the last error recorded by this thread (never NULL). */
+const char* spx_last_error(void);
+
+/* Library build info ("sm_103a ..."). */
+const char* spx_version(void);
+
+/*
+ * Build the device tables (FFT twiddles, k-grids, ladder and collision
+ * coefficients) of one problem.  Allocates a small device buffer on the
+ * current device.  Replaces the host-side table set-up of
+ * spectrax/_initialization.py:114-154.
+ */
+int spx_plan_create(const spx_problem* pb, spx_plan** out);
+int spx_plan_destroy(spx_plan* plan);
+
+/* Number of complex128 entries of the flat state (N_C + N_F). */
+int64_t spx_state_len(const spx_problem* pb);
+
+/* Device scratch spx_rhs / spx_jvp need for this plan (bytes; may be 0). */
+size_t spx_rhs_workspace_bytes(const spx_plan* plan);
+
+/*
+ * dy = f(t, y): the Hermite-Fourier right-hand side.  Replaces
+ * spectrax/_simulation.py:55-111 `ode_system` (with spectrax/_model.py:15-212).
+ * y and dy are device arrays of spx_state_len() complex128 (must not overlap).
+ * Allocates nothing; `ws` must hold spx_rhs_workspace_bytes().
+ */
+int spx_rhs(const spx_plan* plan, const void* y, void* dy, void* ws, size_t ws_bytes,
+            void* stream);
+
+/*
+ * Jv = J(y) v: the linearised right-hand side (the JVP that
+ * spectrax/midpoint_solver.py:75 obtains with jax.linearize).
+ */
+int spx_jvp(const spx_plan* plan, const void* y, const void* v, void* Jv, void* ws,
+            size_t ws_bytes, void* stream);
+
+/*
+ * g = J(y)^T w (plain transpose, no conjugation): the vector-Jacobian product of
+ * the holomorphic right-hand side.  conj(J^T conj(w)) = J^H w is what
+ * torch autograd needs; the Python layer applies the conjugations.
+ */
+int spx_vjp(const spx_plan* plan, const void* y, const void* w, void* g, void* ws,
+            size_t ws_bytes, void* stream);
+
+/* ------------------------------------------------------------------ Dopri8 */
+typedef struct spx_dopri8_opts {
+  double t0, t1;     /* integration interval */
+  double dt0;        /* first step (adaptive) or the constant step */
+  double rtol, atol; /* PID controller tolerances (adaptive only) */
+  int32_t adaptive;  /* 1: Diffrax PIDController defaults; 0: ConstantStepSize */
+  int32_t nsave;     /* number of save times (may be 0) */
+  const double* save_ts; /* host array of nsave increasing times in [t0, t1] */
+  int64_t max_steps; /* accepted + rejected steps before SPX_ST_MAX_STEPS */
+  int32_t save_states; /* 1: keep every saved state (nsave * state_len complex128) */
+  const double* masses; /* host array of Ns species masses for the kinetic energy (NULL: ones);
+                           spectrax/_diagnostics.py:44-68 uses (1, mi_me) for two species */
+} spx_dopri8_opts;
+
+typedef struct spx_dopri8 spx_dopri8;   /* opaque: stage buffers + CUDA graph */
+
+/* Device-side counters of a solve, copied out by spx_dopri8_stats. */
+typedef struct spx_dopri8_stats {
+  double t, dt;
+  int64_t accepted, rejected, rhs_evals;
+  int32_t status, saved;
+} spx_dopri8_stats;
+
+/*
+ * Adaptive / constant-step Prince-Dormand 8(7) solve of y' = f(t, y) on the
+ * device, replacing the diffeqsolve call of spectrax/_simulation.py:164-180.
+ * create() allocates the stage buffers and captures one step attempt as a CUDA
+ * graph; run() replays it until the solve ends.
+ */
+int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* opts, spx_dopri8** out);
+int spx_dopri8_destroy(spx_dopri8* s);
+/* Copy y0 (device) in and reset the clock/controller. */
+int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream);
+/* Replay up to `max_attempts` step attempts (accepted or rejected); returns
+ * after the solve ends or the attempts are used.  *status_out gets the status. */
+int spx_dopri8_advance(spx_dopri8* s, int64_t max_attempts, void* stream, int32_t* status_out);
+/* Run to the end (advance in chunks until status != RUNNING). */
+int spx_dopri8_run(spx_dopri8* s, void* stream, int32_t* status_out);
+int spx_dopri8_stats_get(spx_dopri8* s, spx_dopri8_stats* out, void* stream);
+/* Device pointers owned by the solver: current state, saved states
+ * (nsave x state_len, or NULL), per-save energies (nsave x (2 + Ns) doubles:
+ * EM_energy, kinetic_energy, kinetic_energy_species[0..Ns-1]). */
+const void* spx_dopri8_state(spx_dopri8* s);
+const void* spx_dopri8_saved_states(spx_dopri8* s);
+const double* spx_dopri8_saved_energies(spx_dopri8* s);
+/* Copy solver data to `dst` (host or device; cudaMemcpyDefault) on `stream`:
+ * what = 0: current state (state_len complex128), 1: saved states
+ * (nsave*state_len complex128), 2: saved energies (nsave*(2+Ns) doubles).
+ * `bytes` must equal the size of that item. */
+int spx_dopri8_copy(spx_dopri8* s, int32_t what, void* dst, size_t bytes, void* stream);
+
+/* ------------------------------------------------------------ measurement */
+/*
+ * FP64 issue-rate probe (no counterpart in the reference): `blocks` CTAs of 256
+ * threads each run 8 independent FMA chains of `iters` steps and write one
+ * double per thread to `out` (device, blocks*256 doubles).  Timed by the caller;
+ * FLOP/s = 16 * iters * blocks * 256 / seconds.  Used as the compute roofline.
+ */
+int spx_probe_fp64(void* out, int blocks, int iters, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPECTRAX_GB300_H */

@@ -1,0 +1,278 @@
+// spx_core.cuh — device-side core of the GB300 Hermite-Fourier right-hand side.
+//
+// FP64 everywhere.  On GB300 the FP64 pipe (about 2 lane-ops per clock per SM) is
+// the binding resource, far below HBM bandwidth, so the code is organised to
+// spend as few FP64 instructions as possible and to keep whole warps busy:
+//  * FFTs are mixed-radix Stockham transforms in shared memory.  Radix 2/4/8
+//    butterflies run in registers; odd radices use a two-phase symmetric direct
+//    DFT (pair x_q, x_{R-q} -> a_q = sum, b_q = difference, then
+//    X_k = x_0 + sum a_q cos - i sum b_q sin) that needs ~R^2 FP64 ops instead
+//    of 4 R^2.
+//  * The 1/N of norm="forward", q*Omega_c and the Hermite ladder factors are
+//    folded into the final fused multiply-adds of each mode.
+//  * Per-plane coefficients are uniform per CTA, so Hermite-boundary cases are
+//    uniform branches (no lane divergence).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/spectrax_gb300.h"
+
+namespace spx {
+
+constexpr int MAXST = 12;      // FFT stages per axis
+constexpr int NTHREADS = 256;  // threads per CTA for every kernel of this library
+
+struct AxisPlan {
+  int n;                 // length along the axis (1 = nothing to transform)
+  int nst;               // number of Stockham stages
+  int cut;               // 2/3 mask: largest |k| kept (-1 = nothing kept)
+  int koff;              // k-grid: k_c = 2*pi*(c + koff)   (spectrax/_initialization.py:114-116)
+  int radix[MAXST];
+  int span[MAXST];       // product of the radices of the earlier stages
+  int tw[MAXST];         // offset of the stage twiddles (span*(R-1) entries), -1 when span == 1
+  int cs[MAXST];         // offset of the odd-radix table (cos, sin)(2 pi j / R), j < R; -1 if even
+  int kofs;              // offset of the per-axis k table: (k_c / L, k_c) pairs, n entries
+};
+
+// Everything a kernel needs about one problem; lives in device memory next to
+// the double2 table it indexes.
+struct DevPlan {
+  spx_problem pb;
+  AxisPlan ax[3];        // 0: y, 1: x, 2: z (the axis order of the data)
+  int plane;             // Ny*Nx*Nz
+  int nh;                // Nn*Nm*Np
+  long long nc;          // N_C = Ns*nh*plane
+  int tab_len;           // double2 entries in the table
+  int path;              // 0: fused 1D1V path; 1: general path
+  int tile;              // Hermite planes per CTA on the fused path
+  int ntiles;            // tiles per species on the fused path
+};
+
+// ------------------------------------------------------------------ complex helpers
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
+}
+// acc + a*b
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 acc) {
+  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, acc.x)), fma(a.x, b.y, fma(a.y, b.x, acc.y)));
+}
+// acc + s*a (s real)
+__device__ __forceinline__ double2 crfma(double s, double2 a, double2 acc) {
+  return make_double2(fma(s, a.x, acc.x), fma(s, a.y, acc.y));
+}
+template <bool INV>
+__device__ __forceinline__ double2 twiddle(double2 v, double2 w) {
+  return INV ? cmulc(v, w) : cmul(v, w);
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ double2 rot90(double2 a) {
+  return INV ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
+}
+
+// centered (fftshift) index <-> standard FFT index along an axis of length n
+__device__ __forceinline__ int std_index(int c, int n) { int k = c - n / 2; return k < 0 ? k + n : k; }
+
+// ------------------------------------------------------------------ line addressing
+// nl lines of length n inside one shared buffer: element e of line l sits at
+// base(l) + e*es with base(l) = (l / div)*shi + (l % div)*slo.
+struct Lines {
+  int nl, es, div, shi, slo;
+  __device__ __forceinline__ int base(int l) const { return (l / div) * shi + (l % div) * slo; }
+};
+
+// ------------------------------------------------------------------ register butterflies
+template <int R, bool INV> struct Dft;
+
+template <bool INV> struct Dft<2, INV> {
+  __device__ __forceinline__ static void run(double2* v) {
+    double2 a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+  }
+};
+template <bool INV> struct Dft<4, INV> {
+  __device__ __forceinline__ static void run(double2* v) {
+    double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    double2 s13 = cadd(v[1], v[3]), d13 = rot90<INV>(csub(v[1], v[3]));
+    v[0] = cadd(s02, s13); v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13); v[3] = csub(d02, d13);
+  }
+};
+template <bool INV> struct Dft<8, INV> {
+  __device__ __forceinline__ static void run(double2* v) {
+    const double h = 0.70710678118654752440;   // 1/sqrt(2)
+    double2 e[4] = {v[0], v[2], v[4], v[6]};
+    double2 o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<4, INV>::run(e);
+    Dft<4, INV>::run(o);
+    // o[k] *= w8^k,  w8 = exp(-+ i pi/4)
+    double2 o1, o3;
+    if (!INV) {
+      o1 = make_double2(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x));
+      o3 = make_double2(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y));
+    } else {
+      o1 = make_double2(h * (o[1].x - o[1].y), h * (o[1].x + o[1].y));
+      o3 = make_double2(-h * (o[3].x + o[3].y), h * (o[3].x - o[3].y));
+    }
+    double2 o2 = rot90<INV>(o[2]);
+    v[0] = cadd(e[0], o[0]); v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);   v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);   v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);   v[7] = csub(e[3], o3);
+  }
+};
+
+// One Stockham stage with an even radix R in registers.
+template <int R, bool INV>
+__device__ __forceinline__ void stage_even(const double2* __restrict__ in, double2* __restrict__ out,
+                                           int n, int Ns, const double2* __restrict__ tw,
+                                           const Lines& L) {
+  const int M = n / R;
+  const int ntask = L.nl * M;
+  for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+    const int l = t / M, j = t - l * M;
+    const int b = L.base(l);
+    const int k = j % Ns;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[b + (j + r * M) * L.es];
+    if (Ns > 1 && k > 0) {
+      const double2* w = tw + k * (R - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = twiddle<INV>(v[r], w[r - 1]);
+    }
+    Dft<R, INV>::run(v);
+    const int idx = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[b + (idx + r * Ns) * L.es] = v[r];
+  }
+}
+
+// One Stockham stage with an odd radix R (any R >= 3), two phases.
+// Phase 1, in place on `in`: apply twiddles and replace the pair (x_q, x_{R-q})
+// by (x_q + x_{R-q}, x_q - x_{R-q}).  Phase 2: one task per output pair (k, R-k).
+template <bool INV>
+__device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __restrict__ out, int n,
+                                          int R, int Ns, const double2* __restrict__ tw,
+                                          const double2* __restrict__ cs, const Lines& L) {
+  const int M = n / R;
+  const int h = (R - 1) >> 1;
+  {
+    const int ntask = L.nl * M * h;
+    for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+      const int q = t % h + 1;
+      const int lj = t / h;
+      const int l = lj / M, j = lj - l * M;
+      const int b = L.base(l);
+      const int i1 = b + (j + q * M) * L.es, i2 = b + (j + (R - q) * M) * L.es;
+      double2 x1 = in[i1], x2 = in[i2];
+      const int k = j % Ns;
+      if (Ns > 1 && k > 0) {
+        const double2* w = tw + k * (R - 1);
+        x1 = twiddle<INV>(x1, w[q - 1]);
+        x2 = twiddle<INV>(x2, w[R - q - 1]);
+      }
+      in[i1] = cadd(x1, x2);
+      in[i2] = csub(x1, x2);
+    }
+  }
+  __syncthreads();
+  {
+    const int ntask = L.nl * M * (h + 1);
+    for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+      const int kk = t % (h + 1);
+      const int lj = t / (h + 1);
+      const int l = lj / M, j = lj - l * M;
+      const int b = L.base(l);
+      double2 A = in[b + j * L.es];
+      double2 B = make_double2(0.0, 0.0);
+      int ang = 0;   // (q * kk) mod R
+      for (int q = 1; q <= h; ++q) {
+        ang += kk;
+        if (ang >= R) ang -= R;
+        const double2 cq = cs[ang];
+        const double2 aq = in[b + (j + q * M) * L.es];
+        const double2 bq = in[b + (j + (R - q) * M) * L.es];
+        A = crfma(cq.x, aq, A);
+        B = crfma(cq.y, bq, B);
+      }
+      const int k = j % Ns;
+      const int idx = (j / Ns) * Ns * R + k;
+      // forward: X_k = A - iB, X_{R-k} = A + iB ; inverse: signs swapped
+      const double2 iB = INV ? make_double2(-B.y, B.x) : make_double2(B.y, -B.x);
+      out[b + (idx + kk * Ns) * L.es] = cadd(A, iB);
+      if (kk > 0) out[b + (idx + (R - kk) * Ns) * L.es] = csub(A, iB);
+    }
+  }
+}
+
+// Transform all lines along one axis.  Returns the buffer holding the result
+// (either a or b); both buffers share the line layout.
+template <bool INV>
+__device__ double2* fft_axis(double2* a, double2* b, const AxisPlan& ap, const double2* tab,
+                             const Lines& L) {
+  for (int st = 0; st < ap.nst; ++st) {
+    const int R = ap.radix[st], Ns = ap.span[st];
+    const double2* tw = ap.tw[st] >= 0 ? tab + ap.tw[st] : nullptr;
+    switch (R) {
+      case 2: stage_even<2, INV>(a, b, ap.n, Ns, tw, L); break;
+      case 4: stage_even<4, INV>(a, b, ap.n, Ns, tw, L); break;
+      case 8: stage_even<8, INV>(a, b, ap.n, Ns, tw, L); break;
+      default: stage_odd<INV>(a, b, ap.n, R, Ns, tw, tab + ap.cs[st], L); break;
+    }
+    __syncthreads();
+    double2* t = a; a = b; b = t;
+  }
+  return a;
+}
+
+// 3-D transform of `np` contiguous planes of shape (Ny, Nx, Nz) (element
+// (y*Nx + x)*Nz + z of plane p at p*Ny*Nx*Nz) held in buffer a; b is the
+// ping-pong partner.  Returns the buffer holding the result.
+template <bool INV>
+__device__ double2* fft_planes(double2* a, double2* b, const DevPlan& P, const double2* tab,
+                               int np) {
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  if (Nz > 1) {   // z-lines, l = (p*Ny + y)*Nx + x, base = l*Nz
+    Lines L{np * Ny * Nx, 1, 1, Nz, 0};
+    double2* r = fft_axis<INV>(a, b, P.ax[2], tab, L);
+    if (r != a) { b = a; a = r; }
+  }
+  if (Nx > 1) {   // x-lines, l = (p*Ny + y)*Nz + z, base = (l/Nz)*Nx*Nz + l%Nz
+    Lines L{np * Ny * Nz, Nz, Nz, Nx * Nz, 1};
+    double2* r = fft_axis<INV>(a, b, P.ax[1], tab, L);
+    if (r != a) { b = a; a = r; }
+  }
+  if (Ny > 1) {   // y-lines, l = p*Nx*Nz + x*Nz + z, base = p*plane + l%(Nx*Nz)
+    Lines L{np * Nx * Nz, Nx * Nz, Nx * Nz, P.plane, 1};
+    double2* r = fft_axis<INV>(a, b, P.ax[0], tab, L);
+    if (r != a) { b = a; a = r; }
+  }
+  return a;
+}
+
+// k-table entry (k_c / L, k_c) of axis `ax` at centered index c.
+__device__ __forceinline__ double2 ktab(const DevPlan& P, const double2* tab, int ax, int c) {
+  return tab[P.ax[ax].kofs + c];
+}
+
+__device__ __forceinline__ bool kept(int c, int n, int cut) {
+  int k = c - n / 2;
+  k = k < 0 ? -k : k;
+  return k <= cut;
+}
+
+// hypercollision coefficient c(N, i); spectrax/_initialization.py:125-129
+__device__ __forceinline__ double colc(int N, int i) {
+  if (N <= 3) return 0.0;
+  return (double)i * (double)(i - 1) * (double)(i - 2) / ((double)(N - 1) * (double)(N - 2) * (double)(N - 3));
+}
+
+}  // namespace spx

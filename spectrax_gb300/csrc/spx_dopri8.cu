@@ -1,0 +1,652 @@
+// spx_dopri8.cu — device Prince-Dormand 8(7) solver for one large instance.
+//
+// One step attempt = 13 stage launches + 1 save launch, captured once as a CUDA
+// graph and replayed.  Every stage kernel is the fused right-hand side with a
+// Runge-Kutta epilogue: the value f_i(e) of each output entry is stored as the
+// stage vector K_i(e) and immediately combined into the next stage input
+// y + h*sum_j a(i+1, j) K_j(e), so no separate combination pass touches memory.
+// The last stage writes y_new and the scaled error; its last CTA to finish
+// (atomic ticket, no spin-wait) reduces the per-CTA partial sums in a fixed
+// order and runs the step-size controller on the device.  The host only
+// replays graphs and polls the status word.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "spx_plan.h"
+#include "spx_rhs.cuh"
+#include "spx_tableau.cuh"
+
+namespace spx {
+
+struct D8Dev {
+  double t, dt, t0, t1, rtol, atol;
+  long long accepted, rejected, evals, max_steps;
+  int status, adaptive, cur, k1_valid;
+  int isave, nsave, save_pending, save_lo, save_hi, saved;
+  unsigned int arrive;
+  int pad;
+};
+
+struct D8Args {
+  const DevPlan* plan;
+  const double2* tab;
+  D8Dev* st;
+  double2* Y[2];
+  double2* S[2];
+  double2* K;
+  double2* ws;
+  double* part;
+  const double* save_ts;
+  double2* saved;
+  double* energies;
+  const double* masses;
+  long long len;
+};
+
+// a(i+1, j) rows for i = 0..11, then b (row 12) and e (row 13); nonzero masks
+__constant__ double cCoef[14][13];
+__constant__ int cMask[14];
+
+struct Attempt {
+  double h, t_stop;
+  int landed, go;
+};
+
+__device__ __forceinline__ Attempt attempt_params(const D8Dev& s, const double* __restrict__ ts) {
+  Attempt a;
+  a.t_stop = (s.isave < s.nsave) ? fmin(ts[s.isave], s.t1) : s.t1;
+  a.h = s.dt;
+  a.landed = 0;
+  if (s.t + a.h * (1.0 + rk::SNAP) >= a.t_stop) { a.h = a.t_stop - s.t; a.landed = 1; }
+  const bool ok = !(a.h <= 0.0 || s.t + a.h == s.t);
+  a.go = (s.status == SPX_ST_RUNNING) && (s.accepted + s.rejected < s.max_steps) && ok;
+  return a;
+}
+
+// Epilogue of stages 0..11: store K_i, write the next stage input.
+struct EpiStage {
+  const double2* __restrict__ Y;
+  double2* __restrict__ K;
+  double2* __restrict__ Snext;
+  long long len;
+  int stage;
+  double h;
+  __device__ __forceinline__ void operator()(size_t e, double2 v) const {
+    K[(size_t)stage * len + e] = v;
+    double2 acc = Y[e];
+    const int row = stage;   // coefficients a(stage+1, j)
+    const int mask = cMask[row];
+    for (int j = 0; j < stage; ++j)
+      if (mask & (1 << j)) acc = crfma(h * cCoef[row][j], K[(size_t)j * len + e], acc);
+    acc = crfma(h * cCoef[row][stage], v, acc);
+    Snext[e] = acc;
+  }
+};
+
+// Epilogue of the last stage: y_new, scaled error, non-finite flag.
+struct EpiLast {
+  const double2* __restrict__ Y;
+  const double2* __restrict__ K;
+  double2* __restrict__ Ynew;
+  long long len;
+  double h, rtol, atol;
+  int adaptive;
+  double sq;
+  int nonfinite;
+  __device__ __forceinline__ void operator()(size_t e, double2 v) {
+    const double2 y0 = Y[e];
+    double2 yn = y0;
+    double2 er = make_double2(0.0, 0.0);
+    const int mb = cMask[12], me = cMask[13];
+    for (int j = 0; j < 12; ++j) {
+      const bool ub = mb & (1 << j), ue = me & (1 << j);
+      if (ub || ue) {
+        const double2 kj = K[(size_t)j * len + e];
+        if (ub) yn = crfma(h * cCoef[12][j], kj, yn);
+        if (ue) er = crfma(h * cCoef[13][j], kj, er);
+      }
+    }
+    yn = crfma(h * cCoef[12][12], v, yn);
+    er = crfma(h * cCoef[13][12], v, er);
+    Ynew[e] = yn;
+    if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
+    if (adaptive) {
+      const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
+      const double sc = fma(rtol, sqrt(fmax(m0, m1)), atol);
+      const double rx = er.x / sc, ry = er.y / sc;
+      sq = fma(rx, rx, fma(ry, ry, sq));
+    }
+  }
+};
+
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += red[i];
+  return r;   // valid in thread 0
+}
+
+// Last CTA of the last stage: reduce partials, accept/reject, advance the clock.
+__device__ void finalize_step(const D8Args& a, const Attempt& at, int nblocks) {
+  D8Dev* st = a.st;
+  double sum = 0.0;
+  int nonf = 0;
+  for (int b = 0; b < nblocks; ++b) {
+    sum += __ldcg(a.part + 2 * b);
+    nonf |= (__ldcg(a.part + 2 * b + 1) != 0.0);
+  }
+  const double en = sqrt(sum / (double)a.len);
+  bool accept;
+  double dt_next;
+  if (st->adaptive) {
+    accept = en < 1.0;
+    dt_next = at.h * rk::controller_factor(en, accept);
+    if (accept && at.landed && dt_next < st->dt) dt_next = st->dt;
+  } else {
+    accept = true;
+    dt_next = st->dt;
+  }
+  st->evals += st->k1_valid ? (rk::S - 1) : rk::S;
+  if (accept) {
+    st->t = at.landed ? at.t_stop : st->t + at.h;
+    st->cur ^= 1;
+    st->accepted += 1;
+    st->k1_valid = 0;
+    int lo = st->isave, hi = lo;
+    while (hi < st->nsave && __ldcg(a.save_ts + hi) <= st->t) ++hi;
+    if (hi > lo) { st->save_pending = 1; st->save_lo = lo; st->save_hi = hi; st->isave = hi; }
+    if (nonf) st->status = SPX_ST_NONFINITE;
+    else if (st->t >= st->t1) st->status = SPX_ST_DONE;
+  } else {
+    st->rejected += 1;
+    st->k1_valid = 1;
+  }
+  st->dt = dt_next;
+  st->arrive = 0;
+  __threadfence();
+}
+
+// Elements owned by CTA `b` on the fused 1D1V path (plane tiles, then the field CTA).
+template <class F>
+__device__ void for_each_owned_1v(const DevPlan& P, int b, F&& f) {
+  const int nblk = P.pb.Ns * P.ntiles;
+  if (b == nblk) {
+    const size_t n = 6 * (size_t)P.plane;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) f((size_t)P.nc + i);
+    return;
+  }
+  const int s = b / P.ntiles, tile = b % P.ntiles;
+  const int n0 = tile * P.tile;
+  const int nt = min(P.tile, P.pb.Nn - n0);
+  const int N = P.ax[1].n;
+  const size_t base = ((size_t)s * P.pb.Nn + n0) * N;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) f(base + i);
+}
+
+template <class F>
+__device__ void for_each_owned_gen(const DevPlan& P, int b, F&& f) {
+  const int nplanes = P.pb.Ns * P.nh;
+  const size_t pl = (size_t)P.plane;
+  const size_t base = (b == nplanes) ? (size_t)P.nc : (size_t)b * pl;
+  const size_t n = (b == nplanes) ? 6 * pl : pl;
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) f(base + i);
+}
+
+// Common tail of the last stage: per-CTA reduction and the ticket.
+template <class EL>
+__device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, double* red) {
+  const double s1 = block_sum(el.sq, red);
+  __syncthreads();
+  const double s2 = block_sum((double)el.nonfinite, red);
+  if (threadIdx.x == 0) {
+    a.part[2 * blockIdx.x] = s1;
+    a.part[2 * blockIdx.x + 1] = s2;
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&a.st->arrive, 1u);
+    if (ticket == gridDim.x - 1) {
+      __threadfence();
+      finalize_step(a, at, gridDim.x);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ stage kernels
+__global__ void __launch_bounds__(NTHREADS) k_d8_stage_1v(D8Args a, int stage) {
+  __shared__ DevPlan P;
+  __shared__ D8Dev s;
+  __shared__ double red[NTHREADS / 32];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  if (threadIdx.x == 0) {
+    s = *a.st;
+    if (stage == 0 && blockIdx.x == 0) a.st->save_pending = 0;
+  }
+  load_plan(P, stab, a.plan, a.tab);   // contains __syncthreads
+  const Attempt at = attempt_params(s, a.save_ts);
+  if (!at.go) {
+    if (stage == rk::S - 1 && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING) {
+      a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
+    }
+    return;
+  }
+  const double2* Y = a.Y[s.cur];
+  const double2* in = (stage == 0) ? Y : a.S[stage & 1];
+  const int nblk = P.pb.Ns * P.ntiles;
+  const int N = P.ax[1].n;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)(P.tile + 1) * N;
+  double* scoef = reinterpret_cast<double*>(sB + (size_t)(P.tile + 1) * N);
+  const int b = blockIdx.x;
+  const int sp = b / P.ntiles, tile = b % P.ntiles;
+  const int n0 = tile * P.tile;
+  const int nt = min(P.tile, P.pb.Nn - n0);
+  if (stage < rk::S - 1) {
+    EpiStage epi{Y, a.K, a.S[(stage + 1) & 1], a.len, stage, at.h};
+    if (stage == 0 && s.k1_valid) {
+      for_each_owned_1v(P, b, [&](size_t e) { epi(e, a.K[e]); });
+    } else if (b == nblk) {
+      maxwell_range(P, stab, in, 0, P.plane, epi);
+    } else if (nt > 0) {
+      rhs1v_tile(P, stab, in, sp, n0, nt, sA, sB, scoef, epi);
+    }
+  } else {
+    EpiLast el{Y, a.K, a.Y[s.cur ^ 1], a.len, at.h, s.rtol, s.atol, s.adaptive, 0.0, 0};
+    if (b == nblk) maxwell_range(P, stab, in, 0, P.plane, el);
+    else if (nt > 0) rhs1v_tile(P, stab, in, sp, n0, nt, sA, sB, scoef, el);
+    last_stage_tail(a, at, el, red);
+  }
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
+  __shared__ DevPlan P;
+  __shared__ D8Dev s;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  if (threadIdx.x == 0) s = *a.st;
+  load_plan(P, stab, a.plan, a.tab);
+  const Attempt at = attempt_params(s, a.save_ts);
+  if (!at.go || (stage == 0 && s.k1_valid)) return;
+  const double2* in = (stage == 0) ? a.Y[s.cur] : a.S[stage & 1];
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.plane;
+  general_to_real(P, stab, in, blockIdx.x, a.ws + (size_t)blockIdx.x * P.plane, sA, sB);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_d8_stage_gen(D8Args a, int stage) {
+  __shared__ DevPlan P;
+  __shared__ D8Dev s;
+  __shared__ double red[NTHREADS / 32];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  if (threadIdx.x == 0) {
+    s = *a.st;
+    if (stage == 0 && blockIdx.x == 0) a.st->save_pending = 0;
+  }
+  load_plan(P, stab, a.plan, a.tab);
+  const Attempt at = attempt_params(s, a.save_ts);
+  if (!at.go) {
+    if (stage == rk::S - 1 && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING) {
+      a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
+    }
+    return;
+  }
+  const double2* Y = a.Y[s.cur];
+  const double2* in = (stage == 0) ? Y : a.S[stage & 1];
+  const int nplanes = P.pb.Ns * P.nh;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.plane;
+  const int b = blockIdx.x;
+  const double2* GB = a.ws + (size_t)nplanes * P.plane;
+  if (stage < rk::S - 1) {
+    EpiStage epi{Y, a.K, a.S[(stage + 1) & 1], a.len, stage, at.h};
+    if (stage == 0 && s.k1_valid) {
+      for_each_owned_gen(P, b, [&](size_t e) { epi(e, a.K[e]); });
+    } else if (b == nplanes) {
+      maxwell_range(P, stab, in, 0, P.plane, epi);
+    } else {
+      general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, epi);
+    }
+  } else {
+    EpiLast el{Y, a.K, a.Y[s.cur ^ 1], a.len, at.h, s.rtol, s.atol, s.adaptive, 0.0, 0};
+    if (b == nplanes) maxwell_range(P, stab, in, 0, P.plane, el);
+    else general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, el);
+    last_stage_tail(a, at, el, red);
+  }
+}
+
+// Save: copy the state for pending save indices and compute the energies of
+// spectrax/_diagnostics.py:191-219 (EM, kinetic total, kinetic per species).
+__global__ void __launch_bounds__(NTHREADS) k_d8_save(D8Args a) {
+  __shared__ D8Dev s;
+  __shared__ double red[NTHREADS / 32];
+  if (threadIdx.x == 0) s = *a.st;
+  __syncthreads();
+  if (!s.save_pending) return;
+  const double2* Y = a.Y[s.cur];
+  if (a.saved) {
+    for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
+      double2* dst = a.saved + (size_t)idx * a.len;
+      for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.len;
+           i += (long long)gridDim.x * blockDim.x)
+        dst[i] = Y[i];
+    }
+  }
+  if (blockIdx.x != 0) return;
+  const DevPlan& P = *a.plan;
+  const spx_problem& pb = P.pb;
+  const size_t pl = (size_t)P.plane;
+  double em = 0.0;
+  for (size_t i = threadIdx.x; i < 6 * pl; i += blockDim.x) {
+    const double2 f = Y[P.nc + i];
+    em = fma(f.x, f.x, fma(f.y, f.y, em));
+  }
+  em = block_sum(em, red);
+  if (threadIdx.x == 0) {
+    const int Ns = pb.Ns;
+    const int Hs = P.nh;
+    const int kc = ((P.ax[0].n / 2) * P.ax[1].n + P.ax[1].n / 2) * P.ax[2].n + P.ax[2].n / 2;
+    const int offs[7] = {0, 1, pb.Nn, pb.Nn * pb.Nm, 2, 2 * pb.Nn, 2 * pb.Nn * pb.Nm};
+    const double O0 = pb.Omega_cs[0];
+    const double EM = 0.5 * em * O0 * O0;
+    double ke_tot = 0.0;
+    double kes[SPX_MAX_SPECIES];
+    for (int sp = 0; sp < Ns; ++sp) {
+      double c[7];
+      for (int k = 0; k < 7; ++k)
+        c[k] = (offs[k] >= 0 && offs[k] < Hs) ? Y[((size_t)sp * Hs + offs[k]) * pl + kc].x : 0.0;
+      const double a0 = pb.alpha_s[3 * sp], a1 = pb.alpha_s[3 * sp + 1], a2 = pb.alpha_s[3 * sp + 2];
+      const double u0 = pb.u_s[3 * sp], u1 = pb.u_s[3 * sp + 1], u2 = pb.u_s[3 * sp + 2];
+      const double m = a.masses[sp];
+      const double pref = 0.5 * m * a0 * a1 * a2;
+      const double t0 = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) + (u0 * u0 + u1 * u1 + u2 * u2);
+      const double t1 = 1.41421356237309504880 * (a0 * u0 * c[1] + a1 * u1 * c[2] + a2 * u2 * c[3]);
+      const double t2 = 0.70710678118654752440 * (a0 * a0 * c[4] + a1 * a1 * c[5] + a2 * a2 * c[6]);
+      kes[sp] = pref * (t0 * c[0] + t1 + t2);
+      ke_tot += kes[sp];
+    }
+    for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
+      double* e = a.energies + (size_t)idx * (2 + Ns);
+      e[0] = EM;
+      e[1] = ke_tot;
+      for (int sp = 0; sp < Ns; ++sp) e[2 + sp] = kes[sp];
+    }
+    a.st->saved = s.save_hi;
+  }
+}
+
+}  // namespace spx
+
+// ------------------------------------------------------------------ host side
+using namespace spx;
+
+struct spx_dopri8 {
+  const spx_plan* plan = nullptr;
+  D8Args args{};
+  D8Dev init{};
+  void* block = nullptr;
+  int nsave = 0;
+  int grid_stage = 0, grid_real = 0;
+  int attempts_per_graph = 8;
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int* h_status = nullptr;   // pinned
+  std::vector<double> ts;
+};
+
+static bool g_d8_consts = false;
+
+static int upload_consts() {
+  if (g_d8_consts) return SPX_OK;
+  double c[14][13];
+  int m[14];
+  std::memset(c, 0, sizeof(c));
+  for (int i = 0; i < 12; ++i) {
+    m[i] = 0;
+    for (int j = 0; j <= i; ++j) {
+      c[i][j] = rk::A(i + 1, j);
+      if (c[i][j] != 0.0) m[i] |= 1 << j;
+    }
+  }
+  m[12] = m[13] = 0;
+  for (int j = 0; j < 13; ++j) {
+    c[12][j] = rk::B(j);
+    c[13][j] = rk::E(j);
+    if (c[12][j] != 0.0) m[12] |= 1 << j;
+    if (c[13][j] != 0.0) m[13] |= 1 << j;
+  }
+  SPX_CUDA(cudaMemcpyToSymbol(cCoef, c, sizeof(c)));
+  SPX_CUDA(cudaMemcpyToSymbol(cMask, m, sizeof(m)));
+  g_d8_consts = true;
+  return SPX_OK;
+}
+
+static int d8_attrs() {
+  static bool done = false;
+  if (done) return SPX_OK;
+  const int optin = smem_optin();
+  cudaFuncAttributes fa;
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_real));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_real, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  done = true;
+  return SPX_OK;
+}
+
+static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
+  const DevPlan& P = s->plan->host;
+  for (int stage = 0; stage < rk::S; ++stage) {
+    if (P.path == 0) {
+      k_d8_stage_1v<<<s->grid_stage, NTHREADS, s->plan->smem_1v, st>>>(s->args, stage);
+    } else {
+      k_d8_real<<<s->grid_real, NTHREADS, s->plan->smem_gen, st>>>(s->args, stage);
+      k_d8_stage_gen<<<s->grid_stage, NTHREADS, s->plan->smem_gen, st>>>(s->args, stage);
+    }
+  }
+  k_d8_save<<<s->plan->nsm, NTHREADS, 0, st>>>(s->args);
+}
+
+static int d8_free(spx_dopri8* s) {
+  if (!s) return SPX_OK;
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  if (s->cap) cudaStreamDestroy(s->cap);
+  if (s->block) cudaFree(s->block);
+  if (s->h_status) cudaFreeHost(s->h_status);
+  delete s;
+  return SPX_OK;
+}
+
+extern "C" {
+
+int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8** out) {
+  if (!plan || !o || !out) { set_error("spx_dopri8_create: null argument"); return SPX_E_ARG; }
+  *out = nullptr;
+  if (!(o->t1 >= o->t0) || !(o->dt0 > 0.0) || o->nsave < 0 || (o->nsave > 0 && !o->save_ts) ||
+      o->max_steps <= 0) {
+    set_error("spx_dopri8_create: bad options"); return SPX_E_ARG;
+  }
+  if (o->adaptive && !(o->rtol >= 0.0 && o->atol >= 0.0 && o->rtol + o->atol > 0.0)) {
+    set_error("spx_dopri8_create: tolerances must be non-negative and not both zero"); return SPX_E_ARG;
+  }
+  for (int i = 1; i < o->nsave; ++i)
+    if (!(o->save_ts[i] >= o->save_ts[i - 1])) { set_error("save times must be non-decreasing"); return SPX_E_ARG; }
+  int rc;
+  if ((rc = upload_consts()) != SPX_OK) return rc;
+  if ((rc = d8_attrs()) != SPX_OK) return rc;
+  spx_dopri8* s = new spx_dopri8();
+  s->plan = plan;
+  const DevPlan& P = plan->host;
+  const long long len = (long long)P.nc + 6LL * P.plane;
+  const int Ns = P.pb.Ns;
+  s->nsave = o->nsave;
+  s->grid_stage = (P.path == 0) ? P.pb.Ns * P.ntiles + 1 : P.pb.Ns * P.nh + 1;
+  s->grid_real = (P.path == 0) ? 0 : P.pb.Ns * P.nh + 3 * Ns + 3;
+  // one allocation: st | part | save_ts | masses | energies | Y0 Y1 S0 S1 | K[13] | ws | saved
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t vec = al((size_t)len * sizeof(double2));
+  size_t off = 0;
+  const size_t o_st = off; off += al(sizeof(D8Dev));
+  const size_t o_part = off; off += al(2 * (size_t)s->grid_stage * sizeof(double));
+  const size_t o_ts = off; off += al(std::max(1, o->nsave) * sizeof(double));
+  const size_t o_m = off; off += al(SPX_MAX_SPECIES * sizeof(double));
+  const size_t o_en = off; off += al(std::max(1, o->nsave) * (size_t)(2 + Ns) * sizeof(double));
+  const size_t o_y = off; off += 4 * vec;
+  const size_t o_k = off; off += 13 * vec;
+  const size_t o_ws = off; off += al(plan->ws_bytes);
+  const size_t o_sv = off; off += o->save_states ? (size_t)std::max(1, o->nsave) * vec : 0;
+  cudaError_t e = cudaMalloc(&s->block, off);
+  if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "cudaMalloc(dopri8)"); }
+  char* b = static_cast<char*>(s->block);
+  D8Args& A = s->args;
+  A.plan = plan->d_plan;
+  A.tab = plan->d_tab;
+  A.st = reinterpret_cast<D8Dev*>(b + o_st);
+  A.part = reinterpret_cast<double*>(b + o_part);
+  A.save_ts = reinterpret_cast<const double*>(b + o_ts);
+  A.masses = reinterpret_cast<const double*>(b + o_m);
+  A.energies = reinterpret_cast<double*>(b + o_en);
+  for (int i = 0; i < 2; ++i) {
+    A.Y[i] = reinterpret_cast<double2*>(b + o_y + i * vec);
+    A.S[i] = reinterpret_cast<double2*>(b + o_y + (2 + i) * vec);
+  }
+  A.K = reinterpret_cast<double2*>(b + o_k);   // stage j at K + j*len
+  A.ws = reinterpret_cast<double2*>(b + o_ws);
+  A.saved = o->save_states ? reinterpret_cast<double2*>(b + o_sv) : nullptr;
+  A.len = len;
+  s->ts.assign(o->save_ts, o->save_ts + o->nsave);
+  double masses[SPX_MAX_SPECIES];
+  for (int i = 0; i < SPX_MAX_SPECIES; ++i) masses[i] = 1.0;
+  if (o->masses)
+    for (int i = 0; i < Ns; ++i) masses[i] = o->masses[i];
+  D8Dev& I = s->init;
+  std::memset(&I, 0, sizeof(I));
+  I.t = o->t0; I.t0 = o->t0; I.t1 = o->t1; I.dt = o->dt0;
+  I.rtol = o->rtol; I.atol = o->atol; I.adaptive = o->adaptive ? 1 : 0;
+  I.max_steps = o->max_steps; I.nsave = o->nsave; I.status = SPX_ST_RUNNING;
+  e = cudaMallocHost(&s->h_status, sizeof(int) * 4);
+  if (e == cudaSuccess && o->nsave > 0)
+    e = cudaMemcpy(b + o_ts, o->save_ts, o->nsave * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b + o_m, masses, sizeof(masses), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(b + o_en, 0, std::max(1, o->nsave) * (size_t)(2 + Ns) * sizeof(double));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "dopri8 set-up"); }
+  // capture `attempts_per_graph` step attempts into one graph
+  e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "cudaStreamBeginCapture"); }
+  for (int i = 0; i < s->attempts_per_graph; ++i) enqueue_attempt(s, s->cap);
+  e = cudaStreamEndCapture(s->cap, &s->graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
+  if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "dopri8 graph"); }
+  *out = s;
+  return SPX_OK;
+}
+
+int spx_dopri8_destroy(spx_dopri8* s) { return d8_free(s); }
+
+int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
+  if (!s || !y0) { set_error("spx_dopri8_reset: null argument"); return SPX_E_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  D8Dev I = s->init;
+  I.cur = 0;
+  // a save time at (or before) t0 is taken from y0
+  int hi = 0;
+  while (hi < s->nsave && s->ts[hi] <= I.t0) ++hi;
+  if (hi > 0) { I.save_pending = 1; I.save_lo = 0; I.save_hi = hi; I.isave = hi; }
+  if (I.t0 >= I.t1) I.status = SPX_ST_DONE;
+  SPX_CUDA(cudaMemcpyAsync(s->args.st, &I, sizeof(I), cudaMemcpyHostToDevice, st));
+  SPX_CUDA(cudaMemcpyAsync(s->args.Y[0], y0, (size_t)s->args.len * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  if (hi > 0) k_d8_save<<<s->plan->nsm, NTHREADS, 0, st>>>(s->args);
+  SPX_CUDA(cudaGetLastError());
+  // the init struct lives on the host stack: make the copy complete before returning
+  SPX_CUDA(cudaStreamSynchronize(st));
+  return SPX_OK;
+}
+
+int spx_dopri8_advance(spx_dopri8* s, int64_t max_attempts, void* stream, int32_t* status_out) {
+  if (!s) { set_error("spx_dopri8_advance: null solver"); return SPX_E_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t reps = (max_attempts + s->attempts_per_graph - 1) / s->attempts_per_graph;
+  int status = SPX_ST_RUNNING;
+  for (int64_t r = 0; r < reps; ++r) {
+    SPX_CUDA(cudaGraphLaunch(s->exec, st));
+    SPX_CUDA(cudaMemcpyAsync(s->h_status, &s->args.st->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SPX_CUDA(cudaStreamSynchronize(st));
+    status = *s->h_status;
+    if (status != SPX_ST_RUNNING) break;
+  }
+  if (status_out) *status_out = status;
+  return SPX_OK;
+}
+
+int spx_dopri8_run(spx_dopri8* s, void* stream, int32_t* status_out) {
+  if (!s) { set_error("spx_dopri8_run: null solver"); return SPX_E_ARG; }
+  int32_t status = SPX_ST_RUNNING;
+  while (status == SPX_ST_RUNNING) {
+    int rc = spx_dopri8_advance(s, 64LL * s->attempts_per_graph, stream, &status);
+    if (rc != SPX_OK) return rc;
+  }
+  if (status_out) *status_out = status;
+  return SPX_OK;
+}
+
+int spx_dopri8_stats_get(spx_dopri8* s, spx_dopri8_stats* out, void* stream) {
+  if (!s || !out) { set_error("spx_dopri8_stats_get: null argument"); return SPX_E_ARG; }
+  D8Dev d;
+  SPX_CUDA(cudaMemcpyAsync(&d, s->args.st, sizeof(d), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  SPX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  out->t = d.t; out->dt = d.dt;
+  out->accepted = d.accepted; out->rejected = d.rejected; out->rhs_evals = d.evals;
+  out->status = d.status; out->saved = d.saved;
+  return SPX_OK;
+}
+
+const void* spx_dopri8_state(spx_dopri8* s) {
+  if (!s) return nullptr;
+  D8Dev d;
+  if (cudaMemcpy(&d, s->args.st, sizeof(d), cudaMemcpyDeviceToHost) != cudaSuccess) return nullptr;
+  return s->args.Y[d.cur];
+}
+
+const void* spx_dopri8_saved_states(spx_dopri8* s) { return s ? s->args.saved : nullptr; }
+
+const double* spx_dopri8_saved_energies(spx_dopri8* s) { return s ? s->args.energies : nullptr; }
+
+int spx_dopri8_copy(spx_dopri8* s, int32_t what, void* dst, size_t bytes, void* stream) {
+  if (!s || !dst) { set_error("spx_dopri8_copy: null argument"); return SPX_E_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t vec = (size_t)s->args.len * sizeof(double2);
+  const void* src = nullptr;
+  size_t want = 0;
+  if (what == 0) {
+    D8Dev d;
+    SPX_CUDA(cudaMemcpyAsync(&d, s->args.st, sizeof(d), cudaMemcpyDeviceToHost, st));
+    SPX_CUDA(cudaStreamSynchronize(st));
+    src = s->args.Y[d.cur];
+    want = vec;
+  } else if (what == 1) {
+    if (!s->args.saved) { set_error("spx_dopri8_copy: states were not kept (save_states = 0)"); return SPX_E_ARG; }
+    src = s->args.saved;
+    want = (size_t)s->nsave * vec;
+  } else if (what == 2) {
+    src = s->args.energies;
+    want = (size_t)s->nsave * (2 + s->plan->host.pb.Ns) * sizeof(double);
+  } else {
+    set_error("spx_dopri8_copy: unknown item"); return SPX_E_ARG;
+  }
+  if (bytes != want) { set_error("spx_dopri8_copy: size mismatch"); return SPX_E_ARG; }
+  if (want) SPX_CUDA(cudaMemcpyAsync(dst, src, want, cudaMemcpyDefault, st));
+  return SPX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// spx_plan.h — host-side plan object shared by the translation units of the library.
+#pragma once
+#include <string>
+#include <vector>
+#include "spx_core.cuh"
+
+struct spx_plan {
+  spx::DevPlan host;            // host copy of the device header
+  std::vector<double2> tab;     // host copy of the table
+  spx::DevPlan* d_plan = nullptr;
+  double2* d_tab = nullptr;
+  void* d_block = nullptr;      // single allocation holding d_plan and d_tab
+  int device = 0;
+  int nsm = 0;
+  size_t smem_tab = 0;          // bytes of the table in shared memory
+  size_t smem_1v = 0;           // dynamic smem of the fused 1D1V kernel
+  size_t smem_gen = 0;          // dynamic smem of the general kernels
+  size_t ws_bytes = 0;          // scratch of spx_rhs
+};
+
+namespace spx {
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+// Fill `pl` (everything but the device pointers) from a problem; returns SPX_OK or an error code.
+int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl);
+// Launch helpers used by several entry points.
+int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, cudaStream_t st);
+// Opt-in shared memory per block of the current device (0 on failure).
+int smem_optin();
+}  // namespace spx
+
+#define SPX_CUDA(call)                                         \
+  do {                                                         \
+    cudaError_t e__ = (call);                                  \
+    if (e__ != cudaSuccess) return spx::cuda_fail(e__, #call); \
+  } while (0)

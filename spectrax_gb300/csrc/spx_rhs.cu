@@ -1,0 +1,504 @@
+// spx_rhs.cu — plan construction, right-hand-side kernels and their C ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "spx_plan.h"
+#include "spx_rhs.cuh"
+
+namespace spx {
+
+static thread_local std::string g_last_error = "no error";
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return SPX_E_CUDA;
+}
+
+// cos/sin(2*pi*p/q) with the angle reduced to |angle| <= pi/4 by exact quarter turns.
+static void sincos2pi(long long p, long long q, double* c, double* s) {
+  p %= q;
+  if (p < 0) p += q;
+  const long long m = (4 * p + q / 2) / q;         // nearest quarter turn
+  const long long num = 4 * p - m * q;             // remainder in units of 1/(4q) turns
+  const double ang = (2.0 * M_PI) * ((double)num / (double)(4 * q));
+  double cc = std::cos(ang), ss = std::sin(ang);
+  switch (m & 3) {
+    case 0: *c = cc; *s = ss; break;
+    case 1: *c = -ss; *s = cc; break;
+    case 2: *c = -cc; *s = -ss; break;
+    default: *c = ss; *s = -cc; break;
+  }
+}
+
+static std::vector<int> factorize(int n) {
+  std::vector<int> r;
+  int m = n;
+  while (m % 8 == 0) { r.push_back(8); m /= 8; }
+  while (m % 4 == 0) { r.push_back(4); m /= 4; }
+  while (m % 2 == 0) { r.push_back(2); m /= 2; }
+  for (int p = 3; m > 1; p += 2)
+    while (m % p == 0) { r.push_back(p); m /= p; }
+  std::sort(r.begin(), r.end(), [](int a, int b) { return a > b; });
+  return r;
+}
+
+static int build_axis(int n, int cut, double L, std::vector<double2>& tab, AxisPlan& ap) {
+  std::memset(&ap, 0, sizeof(ap));
+  ap.n = n;
+  ap.cut = cut;
+  const int fl = -((n + 1) / 2);     // floor(-n/2)
+  ap.koff = fl + 1;
+  ap.kofs = (int)tab.size();
+  for (int c = 0; c < n; ++c) {
+    const double k = (double)(2 * (c + ap.koff)) * M_PI;
+    tab.push_back(make_double2(k / L, k));
+  }
+  if (n == 1) { ap.nst = 0; return SPX_OK; }
+  std::vector<int> rad = factorize(n);
+  if ((int)rad.size() > MAXST) { set_error("FFT length has too many factors"); return SPX_E_UNSUPPORTED; }
+  ap.nst = (int)rad.size();
+  std::map<int, int> cs_of;
+  int Ns = 1;
+  for (int st = 0; st < ap.nst; ++st) {
+    const int R = rad[st];
+    ap.radix[st] = R;
+    ap.span[st] = Ns;
+    ap.tw[st] = -1;
+    ap.cs[st] = -1;
+    if (Ns > 1) {
+      ap.tw[st] = (int)tab.size();
+      for (int k = 0; k < Ns; ++k)
+        for (int r = 1; r < R; ++r) {
+          double c, s;
+          sincos2pi(-(long long)r * k, (long long)Ns * R, &c, &s);   // exp(-2 pi i r k / (Ns R))
+          tab.push_back(make_double2(c, s));
+        }
+    }
+    if (R % 2 == 1) {
+      auto it = cs_of.find(R);
+      if (it == cs_of.end()) {
+        cs_of[R] = (int)tab.size();
+        for (int j = 0; j < R; ++j) {
+          double c, s;
+          sincos2pi(j, R, &c, &s);
+          tab.push_back(make_double2(c, s));
+        }
+      }
+      ap.cs[st] = cs_of[R];
+    }
+    Ns *= R;
+  }
+  return SPX_OK;
+}
+
+int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl) {
+  if (!pb) { set_error("null problem"); return SPX_E_ARG; }
+  const spx_problem& p = *pb;
+  if (p.Nx < 1 || p.Ny < 1 || p.Nz < 1 || p.Nn < 1 || p.Nm < 1 || p.Np < 1 || p.Ns < 1) {
+    set_error("all sizes must be >= 1"); return SPX_E_ARG;
+  }
+  if (p.Ns > SPX_MAX_SPECIES) { set_error("too many species"); return SPX_E_ARG; }
+  if (p.Nx > SPX_MAX_AXIS || p.Ny > SPX_MAX_AXIS || p.Nz > SPX_MAX_AXIS) {
+    set_error("an axis is longer than SPX_MAX_AXIS"); return SPX_E_UNSUPPORTED;
+  }
+  for (int s = 0; s < p.Ns; ++s)
+    for (int d = 0; d < 3; ++d)
+      if (!(p.alpha_s[3 * s + d] != 0.0)) { set_error("alpha_s must be non-zero"); return SPX_E_ARG; }
+  if (!(p.Omega_cs[0] != 0.0)) { set_error("Omega_cs[0] must be non-zero"); return SPX_E_ARG; }
+  if (!(p.Lx != 0.0) || !(p.Ly != 0.0) || !(p.Lz != 0.0)) { set_error("L must be non-zero"); return SPX_E_ARG; }
+
+  DevPlan& P = pl->host;
+  std::memset(&P, 0, sizeof(P));
+  P.pb = p;
+  pl->tab.clear();
+  int rc;
+  if ((rc = build_axis(p.Ny, p.cut_y, p.Ly, pl->tab, P.ax[0])) != SPX_OK) return rc;
+  if ((rc = build_axis(p.Nx, p.cut_x, p.Lx, pl->tab, P.ax[1])) != SPX_OK) return rc;
+  if ((rc = build_axis(p.Nz, p.cut_z, p.Lz, pl->tab, P.ax[2])) != SPX_OK) return rc;
+  P.plane = p.Ny * p.Nx * p.Nz;
+  P.nh = p.Nn * p.Nm * p.Np;
+  P.nc = (long long)p.Ns * P.nh * P.plane;
+  P.tab_len = (int)pl->tab.size();
+  pl->nsm = nsm > 0 ? nsm : 152;
+  pl->smem_tab = ((size_t)P.tab_len * sizeof(double2) + 255) / 256 * 256;
+  const size_t smem_max = 227 * 1024 - 4096;
+  const bool onev = (p.Ny == 1 && p.Nz == 1 && p.Nm == 1 && p.Np == 1);
+  if (onev) {
+    P.path = 0;
+    const int N = p.Nx;
+    const long long planes = (long long)p.Ns * p.Nn;
+    int T = (int)((planes + pl->nsm - 1) / pl->nsm);
+    T = std::max(1, std::min(T, 16));
+    // shared memory of the widest user (the JVP): 2*(2T+2)*N double2 + table
+    while (T > 1 && pl->smem_tab + 2 * (size_t)(2 * T + 2) * N * sizeof(double2) > smem_max) --T;
+    int ntiles = (p.Nn + T - 1) / T;
+    T = (p.Nn + ntiles - 1) / ntiles;   // even out the tiles
+    P.tile = T;
+    P.ntiles = ntiles;
+    pl->smem_1v = pl->smem_tab + 2 * (size_t)(2 * T + 2) * N * sizeof(double2) + 16 * 4 * sizeof(double);
+    // the VJP keeps one partial field line per (species, tile)
+    pl->ws_bytes = (size_t)p.Ns * ntiles * N * sizeof(double2);
+  } else {
+    P.path = 1;
+    pl->smem_gen = pl->smem_tab + 2 * (size_t)P.plane * sizeof(double2);
+    if (pl->smem_gen > smem_max) {
+      set_error("a Fourier plane of this size does not fit in shared memory");
+      return SPX_E_UNSUPPORTED;
+    }
+    // real-space planes of y (RHS) and of y and v (JVP)
+    const size_t nreal = (size_t)p.Ns * P.nh + 3 * (size_t)p.Ns + 3;
+    pl->ws_bytes = 2 * nreal * P.plane * sizeof(double2);
+  }
+  if (pl->smem_1v > smem_max) { set_error("Nx too large for the fused path"); return SPX_E_UNSUPPORTED; }
+  return SPX_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(NTHREADS) k_rhs1v(const DevPlan* __restrict__ gP,
+                                                    const double2* __restrict__ gtab,
+                                                    const double2* __restrict__ y,
+                                                    double2* __restrict__ dy) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  EpiStore epi{dy};
+  const int nblk = P.pb.Ns * P.ntiles;
+  if ((int)blockIdx.x == nblk) {
+    maxwell_range(P, stab, y, 0, P.plane, epi);
+    return;
+  }
+  const int s = blockIdx.x / P.ntiles, tile = blockIdx.x % P.ntiles;
+  const int n0 = tile * P.tile;
+  const int nt = min(P.tile, P.pb.Nn - n0);
+  if (nt <= 0) return;
+  const int N = P.ax[1].n;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)(P.tile + 1) * N;
+  double* scoef = reinterpret_cast<double*>(sB + (size_t)(P.tile + 1) * N);
+  rhs1v_tile(P, stab, y, s, n0, nt, sA, sB, scoef, epi);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_gen_real(const DevPlan* __restrict__ gP,
+                                                       const double2* __restrict__ gtab,
+                                                       const double2* __restrict__ y,
+                                                       double2* __restrict__ ws) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.plane;
+  const int id = blockIdx.x;
+  general_to_real(P, stab, y, id, ws + (size_t)id * P.plane, sA, sB);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_gen_nl(const DevPlan* __restrict__ gP,
+                                                     const double2* __restrict__ gtab,
+                                                     const double2* __restrict__ y,
+                                                     const double2* __restrict__ ws,
+                                                     double2* __restrict__ dy) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  EpiStore epi{dy};
+  const int nplanes = P.pb.Ns * P.nh;
+  if ((int)blockIdx.x == nplanes) {
+    maxwell_range(P, stab, y, 0, P.plane, epi);
+    return;
+  }
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.plane;
+  const double2* GB = ws + (size_t)nplanes * P.plane;
+  general_nl_plane(P, stab, y, ws, GB, blockIdx.x, sA, sB, epi);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_jvp1v(const DevPlan* __restrict__ gP,
+                                                    const double2* __restrict__ gtab,
+                                                    const double2* __restrict__ y,
+                                                    const double2* __restrict__ v,
+                                                    double2* __restrict__ out) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  EpiStore epi{out};
+  const int nblk = P.pb.Ns * P.ntiles;
+  if ((int)blockIdx.x == nblk) {
+    maxwell_range(P, stab, v, 0, P.plane, epi);   // Maxwell + current are linear
+    return;
+  }
+  const int s = blockIdx.x / P.ntiles, tile = blockIdx.x % P.ntiles;
+  const int n0 = tile * P.tile;
+  const int nt = min(P.tile, P.pb.Nn - n0);
+  if (nt <= 0) return;
+  const int N = P.ax[1].n;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)(2 * P.tile + 2) * N;
+  double* scoef = reinterpret_cast<double*>(sB + (size_t)(2 * P.tile + 2) * N);
+  rhs1v_tile_t<true>(P, stab, y, v, s, n0, nt, sA, sB, scoef, epi);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_vjp1v(const DevPlan* __restrict__ gP,
+                                                    const double2* __restrict__ gtab,
+                                                    const double2* __restrict__ y,
+                                                    const double2* __restrict__ w,
+                                                    double2* __restrict__ g,
+                                                    double2* __restrict__ part) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  const int s = blockIdx.x / P.ntiles, tile = blockIdx.x % P.ntiles;
+  const int m0 = tile * P.tile;
+  const int nt = min(P.tile, P.pb.Nn - m0);
+  const int N = P.ax[1].n;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)(2 * P.tile + 2) * N;
+  double* scoef = reinterpret_cast<double*>(sB + (size_t)(2 * P.tile + 2) * N);
+  if (nt <= 0) {
+    for (int x = threadIdx.x; x < N; x += blockDim.x)
+      part[((size_t)s * P.ntiles + tile) * N + x] = make_double2(0.0, 0.0);
+    return;
+  }
+  vjp1v_tile(P, stab, y, w, g, part, s, tile, m0, nt, sA, sB, scoef);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_vjp1v_fields(const DevPlan* __restrict__ gP,
+                                                           const double2* __restrict__ gtab,
+                                                           const double2* __restrict__ w,
+                                                           double2* __restrict__ g,
+                                                           const double2* __restrict__ part) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  const int N = P.ax[1].n;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)P.pb.Ns * N;
+  vjp1v_fields(P, stab, w, g, part, sA, sB);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_jvp_real(const DevPlan* __restrict__ gP,
+                                                       const double2* __restrict__ gtab,
+                                                       const double2* __restrict__ y,
+                                                       const double2* __restrict__ v,
+                                                       double2* __restrict__ ws) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.plane;
+  const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
+  const int b = blockIdx.x;
+  const bool second = b >= nreal;
+  const int id = second ? b - nreal : b;
+  general_to_real(P, stab, second ? v : y, id, ws + (size_t)b * P.plane, sA, sB);
+}
+
+__global__ void __launch_bounds__(NTHREADS) k_jvp_nl(const DevPlan* __restrict__ gP,
+                                                     const double2* __restrict__ gtab,
+                                                     const double2* __restrict__ v,
+                                                     const double2* __restrict__ ws,
+                                                     double2* __restrict__ out) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  EpiStore epi{out};
+  const int nplanes = P.pb.Ns * P.nh;
+  if ((int)blockIdx.x == nplanes) {
+    maxwell_range(P, stab, v, 0, P.plane, epi);
+    return;
+  }
+  const size_t pl = (size_t)P.plane;
+  const int nreal = nplanes + 3 * P.pb.Ns + 3;
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.plane;
+  const double2* Cy = ws;
+  const double2* Gy = ws + (size_t)nplanes * pl;
+  const double2* Cv = ws + (size_t)nreal * pl;
+  const double2* Gv = Cv + (size_t)nplanes * pl;
+  general_nl_plane_t<true>(P, stab, v, Cv, Gy, Cy, Gv, blockIdx.x, sA, sB, epi);
+}
+
+static bool g_attr_done = false;
+
+// Allow each kernel the opt-in shared memory minus its static part.
+template <class K>
+static int allow_smem(K kernel, int optin) {
+  cudaFuncAttributes fa;
+  SPX_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  SPX_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                optin - (int)fa.sharedSizeBytes));
+  return SPX_OK;
+}
+
+int smem_optin() {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  return optin;
+}
+
+static int set_attrs() {
+  if (g_attr_done) return SPX_OK;
+  const int optin = smem_optin();
+  if (optin <= 0) { set_error("cannot query shared memory limit"); return SPX_E_CUDA; }
+  int rc;
+  if ((rc = allow_smem(k_rhs1v, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_gen_real, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_gen_nl, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_jvp1v, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_vjp1v, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_vjp1v_fields, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_jvp_real, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_jvp_nl, optin)) != SPX_OK) return rc;
+  g_attr_done = true;
+  return SPX_OK;
+}
+
+int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, cudaStream_t st) {
+  const DevPlan& P = pl->host;
+  if (P.path == 0) {
+    const int grid = P.pb.Ns * P.ntiles + 1;
+    k_rhs1v<<<grid, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, y, dy);
+  } else {
+    const int nplanes = P.pb.Ns * P.nh;
+    k_gen_real<<<nplanes + 3 * P.pb.Ns + 3, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws);
+    k_gen_nl<<<nplanes + 1, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws, dy);
+  }
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+}  // namespace spx
+
+// ------------------------------------------------------------------ C ABI
+using namespace spx;
+
+extern "C" {
+
+const char* spx_last_error(void) { return g_last_error.c_str(); }
+
+const char* spx_version(void) { return "spectrax_gb300 0.1 (sm_103a, FP64)"; }
+
+int64_t spx_state_len(const spx_problem* pb) {
+  if (!pb) return -1;
+  const int64_t plane = (int64_t)pb->Nx * pb->Ny * pb->Nz;
+  return (int64_t)pb->Ns * pb->Nn * pb->Nm * pb->Np * plane + 6 * plane;
+}
+
+int spx_plan_create(const spx_problem* pb, spx_plan** out) {
+  if (!out) { set_error("null output pointer"); return SPX_E_ARG; }
+  *out = nullptr;
+  int dev = 0;
+  SPX_CUDA(cudaGetDevice(&dev));
+  int nsm = 0;
+  SPX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  spx_plan* pl = new spx_plan();
+  pl->device = dev;
+  int rc = build_plan_host(pb, nsm, pl);
+  if (rc != SPX_OK) { delete pl; return rc; }
+  rc = set_attrs();
+  if (rc != SPX_OK) { delete pl; return rc; }
+  const size_t hdr = (sizeof(DevPlan) + 255) / 256 * 256;
+  const size_t bytes = hdr + pl->tab.size() * sizeof(double2);
+  cudaError_t e = cudaMalloc(&pl->d_block, bytes);
+  if (e != cudaSuccess) { delete pl; return cuda_fail(e, "cudaMalloc(plan)"); }
+  pl->d_plan = reinterpret_cast<DevPlan*>(pl->d_block);
+  pl->d_tab = reinterpret_cast<double2*>(reinterpret_cast<char*>(pl->d_block) + hdr);
+  e = cudaMemcpy(pl->d_plan, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !pl->tab.empty())
+    e = cudaMemcpy(pl->d_tab, pl->tab.data(), pl->tab.size() * sizeof(double2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(pl->d_block); delete pl; return cuda_fail(e, "cudaMemcpy(plan)"); }
+  *out = pl;
+  return SPX_OK;
+}
+
+int spx_plan_destroy(spx_plan* pl) {
+  if (!pl) return SPX_OK;
+  if (pl->d_block) cudaFree(pl->d_block);
+  delete pl;
+  return SPX_OK;
+}
+
+size_t spx_rhs_workspace_bytes(const spx_plan* pl) { return pl ? pl->ws_bytes : 0; }
+
+int spx_rhs(const spx_plan* pl, const void* y, void* dy, void* ws, size_t ws_bytes, void* stream) {
+  if (!pl || !y || !dy) { set_error("spx_rhs: null argument"); return SPX_E_ARG; }
+  if (y == dy) { set_error("spx_rhs: y and dy must not alias"); return SPX_E_ARG; }
+  if (((uintptr_t)y | (uintptr_t)dy) & 15) { set_error("spx_rhs: pointers must be 16-byte aligned"); return SPX_E_ARG; }
+  if (pl->ws_bytes > 0 && (!ws || ws_bytes < pl->ws_bytes || ((uintptr_t)ws & 15))) {
+    set_error("spx_rhs: workspace too small or misaligned");
+    return SPX_E_WORKSPACE;
+  }
+  return launch_rhs(pl, static_cast<const double2*>(y), static_cast<double2*>(dy),
+                    static_cast<double2*>(ws), static_cast<cudaStream_t>(stream));
+}
+
+static int check_vec_args(const spx_plan* pl, const void* a, const void* b, const void* c, void* ws,
+                          size_t ws_bytes, const char* who) {
+  if (!pl || !a || !b || !c) { set_error(std::string(who) + ": null argument"); return SPX_E_ARG; }
+  if (c == a || c == b) { set_error(std::string(who) + ": output must not alias an input"); return SPX_E_ARG; }
+  if (((uintptr_t)a | (uintptr_t)b | (uintptr_t)c) & 15) {
+    set_error(std::string(who) + ": pointers must be 16-byte aligned"); return SPX_E_ARG;
+  }
+  if (pl->ws_bytes > 0 && (!ws || ws_bytes < pl->ws_bytes || ((uintptr_t)ws & 15))) {
+    set_error(std::string(who) + ": workspace too small or misaligned"); return SPX_E_WORKSPACE;
+  }
+  return SPX_OK;
+}
+
+int spx_jvp(const spx_plan* pl, const void* y, const void* v, void* Jv, void* ws, size_t ws_bytes,
+            void* stream) {
+  int rc = check_vec_args(pl, y, v, Jv, ws, ws_bytes, "spx_jvp");
+  if (rc != SPX_OK) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const DevPlan& P = pl->host;
+  const double2* yy = static_cast<const double2*>(y);
+  const double2* vv = static_cast<const double2*>(v);
+  double2* out = static_cast<double2*>(Jv);
+  double2* w = static_cast<double2*>(ws);
+  if (P.path == 0) {
+    k_jvp1v<<<P.pb.Ns * P.ntiles + 1, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, yy, vv, out);
+  } else {
+    const int nplanes = P.pb.Ns * P.nh;
+    const int nreal = nplanes + 3 * P.pb.Ns + 3;
+    k_jvp_real<<<2 * nreal, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, vv, w);
+    k_jvp_nl<<<nplanes + 1, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w, out);
+  }
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws, size_t ws_bytes,
+            void* stream) {
+  int rc = check_vec_args(pl, y, wv, g, ws, ws_bytes, "spx_vjp");
+  if (rc != SPX_OK) return rc;
+  const DevPlan& P = pl->host;
+  if (P.path != 0) {
+    set_error("spx_vjp: only the 1D1V layout (Ny = Nz = Nm = Np = 1) has a transpose kernel");
+    return SPX_E_UNSUPPORTED;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double2* part = static_cast<double2*>(ws);
+  k_vjp1v<<<P.pb.Ns * P.ntiles, NTHREADS, pl->smem_1v, st>>>(
+      pl->d_plan, pl->d_tab, static_cast<const double2*>(y), static_cast<const double2*>(wv),
+      static_cast<double2*>(g), part);
+  k_vjp1v_fields<<<1, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(wv),
+                                                   static_cast<double2*>(g), part);
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+}  // extern "C"

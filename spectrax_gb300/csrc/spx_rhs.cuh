@@ -1,0 +1,566 @@
+// spx_rhs.cuh — the fused right-hand-side tile routines (device), shared by the
+// plain RHS entry point, the Dopri8 stage kernels and the batched solver.
+//
+// Each routine computes the derivative of a block of Hermite planes and hands
+// every output value to an epilogue functor `epi(flat_index, value)`, so a
+// caller can store it (plain RHS), or turn it into a Runge-Kutta stage vector
+// plus the next stage input (Dopri8) without another pass over memory.
+#pragma once
+#include "spx_core.cuh"
+
+namespace spx {
+
+// Load the plan header and the table into shared memory (whole CTA).
+__device__ __forceinline__ void load_plan(DevPlan& sP, double2* stab, const DevPlan* __restrict__ gP,
+                                          const double2* __restrict__ gtab) {
+  const int* src = reinterpret_cast<const int*>(gP);
+  int* dst = reinterpret_cast<int*>(&sP);
+  for (int i = threadIdx.x; i < (int)(sizeof(DevPlan) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < sP.tab_len; i += blockDim.x) stab[i] = gtab[i];
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------
+// Fused 1D1V tile (Ny = Nz = 1, Nm = Np = 1): species s, Hermite planes
+// n0 .. n0+nt-1.  With one velocity dimension the nonlinear bracket of
+// spectrax/_model.py:168-184,205-209 reduces to
+//     sqrt(2n)/a0 * (E_x + u_y B_z - u_z B_y)(x) * C_{n-1}(x),
+// so one inverse FFT per plane (C_{n-1}), one for the species field
+// combination G, one product and one forward FFT per plane suffice.
+//
+// JVP = false: the right-hand side at y (yl is ignored).
+// JVP = true : the linearisation at y applied to v = yl:
+//     L v + N(F_y, C_v) + N(F_v, C_y)   (the bracket is bilinear in (F, C)).
+// sA, sB: 2*L*Nx double2 of shared memory with L = nt+1 (RHS) or 2*nt+2 (JVP).
+// ------------------------------------------------------------------------
+template <bool JVP, class Epi>
+__device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
+                             const double2* __restrict__ y, const double2* __restrict__ yl,
+                             int s, int n0, int nt, double2* sA, double2* sB, double* scoef, Epi& epi) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  const double2* __restrict__ lin = JVP ? yl : y;              // source of the linear terms
+  const double2* __restrict__ Cs = y + (size_t)s * Nn * N;
+  const double2* __restrict__ Ls = lin + (size_t)s * Nn * N;
+  const double2* __restrict__ Fk = y + P.nc;
+  const double a0 = P.pb.alpha_s[3 * s];
+  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
+  // lines: RHS  [G_y | C_{n-1}(y) x nt]
+  //        JVP  [G_y | G_v | C_{n-1}(v) x nt | C_{n-1}(y) x nt]
+  const int ng = JVP ? 2 : 1;
+  const int nl = JVP ? 2 * nt + 2 : nt + 1;
+
+  if (threadIdx.x < nt) {
+    const int n = n0 + threadIdx.x;
+    double* c = scoef + 4 * threadIdx.x;
+    c[0] = sqrt((double)(n + 1) * 0.5);
+    c[1] = sqrt((double)n * 0.5);
+    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
+    c[3] = P.pb.nu * colc(Nn, n);
+  }
+  for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    double2 v = make_double2(0.0, 0.0);
+    if (kept(c, N, cut)) {
+      if (l < ng) {
+        const double2* F = (l == 0 ? y : yl) + P.nc;
+        v = F[c];
+        v = crfma(u1, F[5 * N + c], v);
+        v = crfma(-u2, F[4 * N + c], v);
+      } else {
+        const int q = l - ng;                      // 0 .. nt-1 (first set), nt .. 2nt-1 (second)
+        const bool second = JVP && q >= nt;
+        const int nm1 = n0 + (second ? q - nt : q) - 1;
+        const double2* src = (JVP && !second) ? (yl + (size_t)s * Nn * N) : Cs;
+        if (nm1 >= 0) v = src[(size_t)nm1 * N + c];
+      }
+    }
+    sA[l * N + std_index(c, N)] = v;
+  }
+  __syncthreads();
+  double2* r = fft_axis<true>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0});
+  double2* o = (r == sA) ? sB : sA;
+  // real-space products into the lines right after the G lines
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int x = i % N;
+    double2 pr = cmul(r[x], r[ng * N + i]);
+    if (JVP) pr = cfma(r[N + x], r[(ng + nt) * N + i], pr);
+    r[ng * N + i] = pr;
+  }
+  __syncthreads();
+  double2* f = fft_axis<false>(r + ng * N, o + ng * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0});
+  const double ua = u0 / a0;
+  const double Dd = P.pb.D;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    const int n = n0 + l;
+    const double* cf = scoef + 4 * l;
+    const double2 kt = ktab(P, tab, 1, c);
+    const double w = kt.x * a0;
+    const double2 C0 = Ls[(size_t)n * N + c];
+    const double2 Cp = (n + 1 < Nn) ? Ls[(size_t)(n + 1) * N + c] : make_double2(0.0, 0.0);
+    const double2 Cm = (n >= 1) ? Ls[(size_t)(n - 1) * N + c] : make_double2(0.0, 0.0);
+    double2 t = cscale(ua, C0);
+    t = crfma(cf[0], Cp, t);
+    t = crfma(cf[1], Cm, t);
+    double d = cf[3];
+    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
+    double re = fma(w, t.y, -d * C0.x);
+    double im = fma(-w, t.x, -d * C0.y);
+    if (n >= 1 && kept(c, N, cut)) {
+      const double2 nl2 = f[l * N + std_index(c, N)];
+      re = fma(cf[2], nl2.x, re);
+      im = fma(cf[2], nl2.y, im);
+    }
+    epi((size_t)(s * Nn + n) * N + c, make_double2(re, im));
+  }
+}
+
+template <class Epi>
+__device__ __forceinline__ void rhs1v_tile(const DevPlan& P, const double2* __restrict__ tab,
+                                           const double2* __restrict__ y, int s, int n0, int nt,
+                                           double2* sA, double2* sB, double* scoef, Epi& epi) {
+  rhs1v_tile_t<false>(P, tab, y, y, s, n0, nt, sA, sB, scoef, epi);
+}
+
+// ------------------------------------------------------------------------
+// Maxwell + current for Fourier points [p0, p1) of the field planes.
+// ------------------------------------------------------------------------
+template <class Epi>
+__device__ void maxwell_range(const DevPlan& P, const double2* __restrict__ tab,
+                              const double2* __restrict__ y, int p0, int p1, Epi& epi) {
+  const spx_problem& pb = P.pb;
+  const int Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const size_t pl = (size_t)P.plane;
+  const double2* __restrict__ F = y + P.nc;
+  const double rs2 = 0.70710678118654752440;
+  const double iO = 1.0 / pb.Omega_cs[0];
+  for (int pt = p0 + threadIdx.x; pt < p1; pt += blockDim.x) {
+    const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
+    const double Kx = ktab(P, tab, 1, cx).x, Ky = ktab(P, tab, 0, cy).x, Kz = ktab(P, tab, 2, cz).x;
+    double2 J0 = make_double2(0, 0), J1 = make_double2(0, 0), J2 = make_double2(0, 0);
+    for (int s = 0; s < pb.Ns; ++s) {
+      const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
+      const double pre = pb.qs[s] * a0 * a1 * a2;
+      const size_t b0 = (size_t)s * P.nh * pl + pt;
+      const double2 C000 = y[b0];
+      const double2 C100 = pb.Nn > 1 ? y[b0 + pl] : make_double2(0, 0);
+      const double2 C010 = pb.Nm > 1 ? y[b0 + (size_t)pb.Nn * pl] : make_double2(0, 0);
+      const double2 C001 = pb.Np > 1 ? y[b0 + (size_t)pb.Nn * pb.Nm * pl] : make_double2(0, 0);
+      J0 = crfma(pre, crfma(pb.u_s[3 * s], C000, cscale(a0 * rs2, C100)), J0);
+      J1 = crfma(pre, crfma(pb.u_s[3 * s + 1], C000, cscale(a1 * rs2, C010)), J1);
+      J2 = crfma(pre, crfma(pb.u_s[3 * s + 2], C000, cscale(a2 * rs2, C001)), J2);
+    }
+    const double2 Ex = F[pt], Ey = F[pl + pt], Ez = F[2 * pl + pt];
+    const double2 Bx = F[3 * pl + pt], By = F[4 * pl + pt], Bz = F[5 * pl + pt];
+    const double2 kbx = csub(cscale(Ky, Bz), cscale(Kz, By));
+    const double2 kby = csub(cscale(Kz, Bx), cscale(Kx, Bz));
+    const double2 kbz = csub(cscale(Kx, By), cscale(Ky, Bx));
+    const double2 kex = csub(cscale(Ky, Ez), cscale(Kz, Ey));
+    const double2 key = csub(cscale(Kz, Ex), cscale(Kx, Ez));
+    const double2 kez = csub(cscale(Kx, Ey), cscale(Ky, Ex));
+    const size_t f0 = (size_t)P.nc + pt;
+    // dE = i K x B - J / Omega_0 ; dB = -i K x E   (spectrax/_simulation.py:103-106)
+    epi(f0, make_double2(fma(-J0.x, iO, -kbx.y), fma(-J0.y, iO, kbx.x)));
+    epi(f0 + pl, make_double2(fma(-J1.x, iO, -kby.y), fma(-J1.y, iO, kby.x)));
+    epi(f0 + 2 * pl, make_double2(fma(-J2.x, iO, -kbz.y), fma(-J2.y, iO, kbz.x)));
+    epi(f0 + 3 * pl, make_double2(kex.y, -kex.x));
+    epi(f0 + 4 * pl, make_double2(key.y, -key.x));
+    epi(f0 + 5 * pl, make_double2(kez.y, -kez.x));
+  }
+}
+
+// ------------------------------------------------------------------------
+// General path, pass 1: masked inverse 3-D FFT of one plane into `out`
+// (natural real-space order).  Plane ids: [0, Ns*nh) are Hermite planes of y;
+// then 3*Ns species field combinations G_s = E + u_s x B, then B (3 planes).
+// ------------------------------------------------------------------------
+__device__ __forceinline__ double2 field_combo_point(const DevPlan& P, const double2* __restrict__ F,
+                                                     int id, size_t pt) {
+  const size_t pl = (size_t)P.plane;
+  const int Ns = P.pb.Ns;
+  if (id >= 3 * Ns) return F[(size_t)(3 + id - 3 * Ns) * pl + pt];
+  const int s = id / 3, comp = id % 3;
+  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+  const double2 Bx = F[3 * pl + pt], By = F[4 * pl + pt], Bz = F[5 * pl + pt];
+  double2 v = F[(size_t)comp * pl + pt];
+  if (comp == 0) { v = crfma(u1, Bz, v); v = crfma(-u2, By, v); }        // E_x + u_y B_z - u_z B_y
+  else if (comp == 1) { v = crfma(u2, Bx, v); v = crfma(-u0, Bz, v); }   // E_y + u_z B_x - u_x B_z
+  else { v = crfma(u0, By, v); v = crfma(-u1, Bx, v); }                  // E_z + u_x B_y - u_y B_x
+  return v;
+}
+
+__device__ inline void general_to_real(const DevPlan& P, const double2* __restrict__ tab,
+                                const double2* __restrict__ y, int id, double2* __restrict__ out,
+                                double2* sA, double2* sB) {
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const int pl = P.plane;
+  const int nplanes = P.pb.Ns * P.nh;
+  for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+    const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
+    double2 v = make_double2(0.0, 0.0);
+    if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut)) {
+      v = (id < nplanes) ? y[(size_t)id * pl + pt] : field_combo_point(P, y + P.nc, id - nplanes, pt);
+    }
+    const int d = (std_index(cy, Ny) * Nx + std_index(cx, Nx)) * Nz + std_index(cz, Nz);
+    sA[d] = v;
+  }
+  __syncthreads();
+  double2* r = fft_planes<true>(sA, sB, P, tab, 1);
+  for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) out[pt] = r[pt];
+}
+
+// Per-plane coefficients of the general nonlinear bracket (spectrax/_model.py:168-184).
+struct NlCoef {
+  double gx, gy, gz;           // sqrt(2n)/a0, sqrt(2m)/a1, sqrt(2p)/a2 on C_{n-1}, C_{m-1}, C_{p-1}
+  double bx[3], by[3], bz[3];  // B-bracket weights (0 when the neighbour is outside the box)
+  int ix[3], iy[3], iz[3];     // neighbour plane ids (-1 when absent)
+  int in_, im_, ip_;           // plane ids of C_{n-1}, C_{m-1}, C_{p-1} (-1 when absent)
+};
+
+__device__ __forceinline__ NlCoef nl_coef(const DevPlan& P, int s, int n, int m, int p) {
+  const spx_problem& pb = P.pb;
+  const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np;
+  const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
+  const double sn = sqrt((double)n), sm = sqrt((double)m), sp = sqrt((double)p);
+  const double sn1 = sqrt((double)(n + 1)), sm1 = sqrt((double)(m + 1)), sp1 = sqrt((double)(p + 1));
+  const double r2 = 1.41421356237309504880;
+  const int base = s * P.nh;
+  auto id = [&](int nn, int mm, int pp) -> int {
+    if (nn < 0 || nn >= Nn || mm < 0 || mm >= Nm || pp < 0 || pp >= Np) return -1;
+    return base + (pp * Nm + mm) * Nn + nn;
+  };
+  NlCoef c;
+  c.gx = r2 * sn / a0; c.gy = r2 * sm / a1; c.gz = r2 * sp / a2;
+  c.in_ = n >= 1 ? id(n - 1, m, p) : -1;
+  c.im_ = m >= 1 ? id(n, m - 1, p) : -1;
+  c.ip_ = p >= 1 ? id(n, m, p - 1) : -1;
+  // B_x: C_{m-1,p-1}, C_{m-1,p+1}, C_{m+1,p-1}
+  c.bx[0] = sm * sp * (a2 / a1 - a1 / a2); c.ix[0] = (m >= 1 && p >= 1) ? id(n, m - 1, p - 1) : -1;
+  c.bx[1] = sm * sp1 * (a2 / a1);          c.ix[1] = (m >= 1) ? id(n, m - 1, p + 1) : -1;
+  c.bx[2] = -sm1 * sp * (a1 / a2);         c.ix[2] = (p >= 1) ? id(n, m + 1, p - 1) : -1;
+  // B_y: C_{n-1,p-1}, C_{n+1,p-1}, C_{n-1,p+1}
+  c.by[0] = sn * sp * (a0 / a2 - a2 / a0); c.iy[0] = (n >= 1 && p >= 1) ? id(n - 1, m, p - 1) : -1;
+  c.by[1] = sn1 * sp * (a0 / a2);          c.iy[1] = (p >= 1) ? id(n + 1, m, p - 1) : -1;
+  c.by[2] = -sn * sp1 * (a2 / a0);         c.iy[2] = (n >= 1) ? id(n - 1, m, p + 1) : -1;
+  // B_z: C_{n-1,m-1}, C_{n-1,m+1}, C_{n+1,m-1}
+  c.bz[0] = sn * sm * (a1 / a0 - a0 / a1); c.iz[0] = (n >= 1 && m >= 1) ? id(n - 1, m - 1, p) : -1;
+  c.bz[1] = sn * sm1 * (a1 / a0);          c.iz[1] = (n >= 1) ? id(n - 1, m + 1, p) : -1;
+  c.bz[2] = -sn1 * sm * (a0 / a1);         c.iz[2] = (m >= 1) ? id(n + 1, m - 1, p) : -1;
+  for (int k = 0; k < 3; ++k) {
+    if (c.ix[k] < 0) c.bx[k] = 0.0;
+    if (c.iy[k] < 0) c.by[k] = 0.0;
+    if (c.iz[k] < 0) c.bz[k] = 0.0;
+  }
+  return c;
+}
+
+// sum_k w[k] * R[ids[k]][pt] over the present neighbours
+__device__ __forceinline__ double2 combo3(const double2* __restrict__ R, size_t pl, const int* ids,
+                                          const double* w, size_t pt) {
+  double2 t = make_double2(0.0, 0.0);
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (ids[k] >= 0) t = crfma(w[k], R[(size_t)ids[k] * pl + pt], t);
+  return t;
+}
+
+// Real-space bracket at one point for plane coefficients `cf`:
+// Gx*gx*C_{n-1} + Gy*gy*C_{m-1} + Gz*gz*C_{p-1} + Bx*(..) + By*(..) + Bz*(..).
+struct FieldPlanes {
+  const double2 *Gx, *Gy, *Gz, *Bx, *By, *Bz;
+};
+
+__device__ __forceinline__ FieldPlanes field_planes(const double2* GB, int s, int Ns, size_t pl) {
+  FieldPlanes f;
+  f.Gx = GB + (size_t)(3 * s) * pl;
+  f.Gy = f.Gx + pl;
+  f.Gz = f.Gy + pl;
+  f.Bx = GB + (size_t)(3 * Ns) * pl;
+  f.By = f.Bx + pl;
+  f.Bz = f.By + pl;
+  return f;
+}
+
+__device__ __forceinline__ double2 bracket_point(const NlCoef& cf, const double2* __restrict__ Cr,
+                                                 const FieldPlanes& F, size_t pl, size_t pt,
+                                                 bool anyx, bool anyy, bool anyz, double2 acc) {
+  if (cf.in_ >= 0) acc = cfma(F.Gx[pt], cscale(cf.gx, Cr[(size_t)cf.in_ * pl + pt]), acc);
+  if (cf.im_ >= 0) acc = cfma(F.Gy[pt], cscale(cf.gy, Cr[(size_t)cf.im_ * pl + pt]), acc);
+  if (cf.ip_ >= 0) acc = cfma(F.Gz[pt], cscale(cf.gz, Cr[(size_t)cf.ip_ * pl + pt]), acc);
+  if (anyx) acc = cfma(F.Bx[pt], combo3(Cr, pl, cf.ix, cf.bx, pt), acc);
+  if (anyy) acc = cfma(F.By[pt], combo3(Cr, pl, cf.iy, cf.by, pt), acc);
+  if (anyz) acc = cfma(F.Bz[pt], combo3(Cr, pl, cf.iz, cf.bz, pt), acc);
+  return acc;
+}
+
+// ------------------------------------------------------------------------
+// General path, pass 2: real-space bracket of plane `id`, forward FFT, mask,
+// plus streaming, collisions and diffusion of `lin`.
+//   RHS: bracket(C_y, G_y),           lin = y
+//   JVP: bracket(C_v, G_y) + bracket(C_y, G_v), lin = v
+// RA/GA: real-space Hermite planes and field combinations of the first
+// operand; RB/GB2 of the second (JVP only).
+// ------------------------------------------------------------------------
+template <bool JVP, class Epi>
+__device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__ tab,
+                                   const double2* __restrict__ lin,
+                                   const double2* __restrict__ RA, const double2* __restrict__ GA,
+                                   const double2* __restrict__ RB, const double2* __restrict__ GB2,
+                                   int id, double2* sA, double2* sB, Epi& epi) {
+  const spx_problem& pb = P.pb;
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const size_t pl = (size_t)P.plane;
+  const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np, Ns = pb.Ns;
+  const int s = id / P.nh, h = id % P.nh;
+  const int n = h % Nn, m = (h / Nn) % Nm, p = h / (Nn * Nm);
+  const NlCoef cf = nl_coef(P, s, n, m, p);
+  const bool anyx = cf.ix[0] >= 0 || cf.ix[1] >= 0 || cf.ix[2] >= 0;
+  const bool anyy = cf.iy[0] >= 0 || cf.iy[1] >= 0 || cf.iy[2] >= 0;
+  const bool anyz = cf.iz[0] >= 0 || cf.iz[1] >= 0 || cf.iz[2] >= 0;
+  // RHS: (RA = C_y, GA = G_y).  JVP: RA = C_v, GA = G_y, RB = C_y, GB2 = G_v.
+  const FieldPlanes FA = field_planes(GA, s, Ns, pl);
+  FieldPlanes FB;
+  if (JVP) FB = field_planes(GB2, s, Ns, pl);
+  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+    double2 acc = bracket_point(cf, RA, FA, pl, pt, anyx, anyy, anyz, make_double2(0.0, 0.0));
+    if (JVP) acc = bracket_point(cf, RB, FB, pl, pt, anyx, anyy, anyz, acc);
+    sA[pt] = acc;
+  }
+  __syncthreads();
+  double2* f = fft_planes<false>(sA, sB, P, tab, 1);
+
+  const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
+  const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
+  const double sc = pb.qs[s] * pb.Omega_cs[s] / (double)pl;
+  const double dcol = pb.nu * (colc(Nn, n) + colc(Nm, m) + colc(Np, p));
+  const double rh = 0.5;
+  const double snp = sqrt((n + 1) * rh), snm = sqrt(n * rh);
+  const double smp = sqrt((m + 1) * rh), smm = sqrt(m * rh);
+  const double spp = sqrt((p + 1) * rh), spm = sqrt(p * rh);
+  const double2* Cp = lin + (size_t)id * pl;
+  const size_t sn_ = pl, sm_ = (size_t)Nn * pl, sp_ = (size_t)Nn * Nm * pl;
+  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+    const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
+    const double2 C0 = Cp[pt];
+    double re = 0.0, im = 0.0;
+    double k2 = 0.0;
+    if (Nx > 1) {
+      const double2 kt = ktab(P, tab, 1, cx);
+      double2 t = cscale(u0 / a0, C0);
+      if (n + 1 < Nn) t = crfma(snp, Cp[pt + sn_], t);
+      if (n >= 1) t = crfma(snm, Cp[pt - sn_], t);
+      const double w = kt.x * a0;
+      re = fma(w, t.y, re); im = fma(-w, t.x, im);
+      k2 = fma(kt.y, kt.y, k2);
+    }
+    if (Ny > 1) {
+      const double2 kt = ktab(P, tab, 0, cy);
+      double2 t = cscale(u1 / a1, C0);
+      if (m + 1 < Nm) t = crfma(smp, Cp[pt + sm_], t);
+      if (m >= 1) t = crfma(smm, Cp[pt - sm_], t);
+      const double w = kt.x * a1;
+      re = fma(w, t.y, re); im = fma(-w, t.x, im);
+      k2 = fma(kt.y, kt.y, k2);
+    }
+    if (Nz > 1) {
+      const double2 kt = ktab(P, tab, 2, cz);
+      double2 t = cscale(u2 / a2, C0);
+      if (p + 1 < Np) t = crfma(spp, Cp[pt + sp_], t);
+      if (p >= 1) t = crfma(spm, Cp[pt - sp_], t);
+      const double w = kt.x * a2;
+      re = fma(w, t.y, re); im = fma(-w, t.x, im);
+      k2 = fma(kt.y, kt.y, k2);
+    }
+    const double d = fma(pb.D, k2, dcol);
+    re = fma(-d, C0.x, re);
+    im = fma(-d, C0.y, im);
+    if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut)) {
+      const int sidx = (std_index(cy, Ny) * Nx + std_index(cx, Nx)) * Nz + std_index(cz, Nz);
+      const double2 v = f[sidx];
+      re = fma(sc, v.x, re);
+      im = fma(sc, v.y, im);
+    }
+    epi((size_t)id * pl + pt, make_double2(re, im));
+  }
+}
+
+template <class Epi>
+__device__ __forceinline__ void general_nl_plane(const DevPlan& P, const double2* __restrict__ tab,
+                                                 const double2* __restrict__ y,
+                                                 const double2* __restrict__ Creal,
+                                                 const double2* __restrict__ GB, int id,
+                                                 double2* sA, double2* sB, Epi& epi) {
+  general_nl_plane_t<false>(P, tab, y, Creal, GB, nullptr, nullptr, id, sA, sB, epi);
+}
+
+// ------------------------------------------------------------------------
+// VJP of the fused 1D1V path, pass 1 (planes).  g = J(y)^T w (plain
+// transpose).  For output planes m in [m0, m0+nt) of species s:
+//   * streaming + damping: the Hermite streaming matrix is symmetric, so its
+//     transpose applied to w is the forward formula with C := w;
+//   * nonlinear term: NL_n = k_n M P_f FFT(G . IFFT(P_i M C_{n-1})) with
+//     k_n = q Omega sqrt(2n) / a0 / N, so its transpose gives
+//     g_{n-1} += k_n M P_f IFFT(G . FFT(P_i M w_n))   (FFT directions swapped)
+//     and, for the field combination G, the per-species real-space sum
+//     R_s(x) = sum_n k_n c_{n-1}(x) W_n(x), written per tile to `part`;
+//   * Maxwell: the current J depends on C_{s,0} and C_{s,1}; its transpose adds
+//     -(q a0 a1 a2 / Omega_0)(u . w_E) to g_{s,0} and -(q a0^2 a1 a2/(sqrt2 Omega_0)) w_Ex
+//     to g_{s,1}.
+// sA/sB: 2*(2 nt + 1)*N double2.
+// ------------------------------------------------------------------------
+__device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ tab,
+                                  const double2* __restrict__ y, const double2* __restrict__ w,
+                                  double2* __restrict__ g, double2* __restrict__ part,
+                                  int s, int tile, int m0, int nt, double2* sA, double2* sB,
+                                  double* scoef) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  const double2* __restrict__ Cs = y + (size_t)s * Nn * N;
+  const double2* __restrict__ Ws = w + (size_t)s * Nn * N;
+  const double2* __restrict__ Fk = y + P.nc;
+  const double2* __restrict__ Wf = w + P.nc;
+  const double a0 = P.pb.alpha_s[3 * s], a1 = P.pb.alpha_s[3 * s + 1], a2 = P.pb.alpha_s[3 * s + 2];
+  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
+  // lines: [G_y | c_m (nt) | W_{m+1} (nt)]
+  const int nl = 2 * nt + 1;
+  if (threadIdx.x < nt) {
+    const int m = m0 + threadIdx.x;
+    double* c = scoef + 4 * threadIdx.x;
+    c[0] = sqrt((double)(m + 1) * 0.5);
+    c[1] = sqrt((double)m * 0.5);
+    c[2] = (m + 1 < Nn) ? qOc * sqrt(2.0 * (double)(m + 1)) / a0 / (double)N : 0.0;   // k_{m+1}
+    c[3] = P.pb.nu * colc(Nn, m);
+  }
+  for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    double2 v = make_double2(0.0, 0.0);
+    if (kept(c, N, cut)) {
+      if (l == 0) {
+        v = Fk[c];
+        v = crfma(u1, Fk[5 * N + c], v);
+        v = crfma(-u2, Fk[4 * N + c], v);
+      } else if (l <= nt) {
+        v = Cs[(size_t)(m0 + l - 1) * N + c];
+      } else {
+        const int n = m0 + (l - 1 - nt) + 1;
+        if (n < Nn) v = Ws[(size_t)n * N + c];
+      }
+    }
+    sA[l * N + std_index(c, N)] = v;
+  }
+  __syncthreads();
+  // both transforms have the same number of stages, so both results land in `r`
+  double2* r = fft_axis<true>(sA, sB, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0});
+  double2* o = (r == sA) ? sB : sA;
+  {
+    double2* r2 = fft_axis<false>(sA + (nt + 1) * N, sB + (nt + 1) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0});
+    (void)r2;
+  }
+  // partial field sum R_s(x) for this tile (fixed order over planes), then Q = G . W in place
+  double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
+  for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int l = 0; l < nt; ++l) {
+      const double k = scoef[4 * l + 2];
+      acc = cfma(cscale(k, r[(1 + l) * N + x]), r[(1 + nt + l) * N + x], acc);
+    }
+    Rp[x] = acc;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int x = i % N;
+    r[(1 + nt) * N + i] = cmul(r[x], r[(1 + nt) * N + i]);
+  }
+  __syncthreads();
+  double2* q = fft_axis<true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0});
+  const double ua = u0 / a0;
+  const double Dd = P.pb.D;
+  const double iO = 1.0 / P.pb.Omega_cs[0];
+  const double pre = P.pb.qs[s] * a0 * a1 * a2;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    const int m = m0 + l;
+    const double* cf = scoef + 4 * l;
+    const double2 kt = ktab(P, tab, 1, c);
+    const double wk = kt.x * a0;
+    const double2 W0 = Ws[(size_t)m * N + c];
+    const double2 Wp = (m + 1 < Nn) ? Ws[(size_t)(m + 1) * N + c] : make_double2(0.0, 0.0);
+    const double2 Wm = (m >= 1) ? Ws[(size_t)(m - 1) * N + c] : make_double2(0.0, 0.0);
+    double2 t = cscale(ua, W0);
+    t = crfma(cf[0], Wp, t);
+    t = crfma(cf[1], Wm, t);
+    double d = cf[3];
+    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
+    double re = fma(wk, t.y, -d * W0.x);
+    double im = fma(-wk, t.x, -d * W0.y);
+    if (m + 1 < Nn && kept(c, N, cut)) {
+      const double2 v = q[l * N + std_index(c, N)];
+      re = fma(cf[2], v.x, re);
+      im = fma(cf[2], v.y, im);
+    }
+    if (m == 0) {
+      const double2 ex = Wf[c], ey = Wf[N + c], ez = Wf[2 * N + c];
+      const double co = -pre * iO;
+      re = fma(co, fma(u0, ex.x, fma(u1, ey.x, u2 * ez.x)), re);
+      im = fma(co, fma(u0, ex.y, fma(u1, ey.y, u2 * ez.y)), im);
+    } else if (m == 1) {
+      const double co = -pre * iO * a0 * 0.70710678118654752440;
+      re = fma(co, Wf[c].x, re);
+      im = fma(co, Wf[c].y, im);
+    }
+    g[(size_t)(s * Nn + m) * N + c] = make_double2(re, im);
+  }
+}
+
+// VJP of the fused 1D1V path, pass 2 (fields): one CTA.
+//   g_E = i K x w_B + sum_s gG_s e_x,  g_B = -i K x w_E + sum_s gG_s (0, -u_z, u_y)
+// with gG_s = M P_f IFFT(sum_tiles R_s).
+__device__ inline void vjp1v_fields(const DevPlan& P, const double2* __restrict__ tab,
+                                    const double2* __restrict__ w, double2* __restrict__ g,
+                                    const double2* __restrict__ part, double2* sA, double2* sB) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Ns = P.pb.Ns;
+  for (int i = threadIdx.x; i < Ns * N; i += blockDim.x) {
+    const int s = i / N, x = i - s * N;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int t = 0; t < P.ntiles; ++t) acc = cadd(acc, part[((size_t)s * P.ntiles + t) * N + x]);
+    sA[s * N + x] = acc;
+  }
+  __syncthreads();
+  double2* r = fft_axis<true>(sA, sB, P.ax[1], tab, Lines{Ns, 1, 1, N, 0});
+  const double2* Wf = w + P.nc;
+  double2* gF = g + P.nc;
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    double2 gx = make_double2(0, 0), gy = make_double2(0, 0), gz = make_double2(0, 0);
+    if (kept(c, N, cut)) {
+      for (int s = 0; s < Ns; ++s) {
+        const double2 v = r[s * N + std_index(c, N)];
+        gx = cadd(gx, v);
+        gy = crfma(-P.pb.u_s[3 * s + 2], v, gy);   // d G / d B_y = -u_z
+        gz = crfma(P.pb.u_s[3 * s + 1], v, gz);    // d G / d B_z = +u_y
+      }
+    }
+    const double Kx = ktab(P, tab, 1, c).x;   // Ky = Kz = 0 on this path
+    const double2 wEy = Wf[N + c], wEz = Wf[2 * N + c];
+    const double2 wBy = Wf[4 * N + c], wBz = Wf[5 * N + c];
+    // i K x w_B with K = (Kx, 0, 0): (0, -Kx wBz, Kx wBy) * i
+    const double2 kbx = make_double2(0, 0);
+    const double2 kby = cscale(-Kx, wBz), kbz = cscale(Kx, wBy);
+    const double2 kex = make_double2(0, 0);
+    const double2 key = cscale(-Kx, wEz), kez = cscale(Kx, wEy);
+    gF[c] = make_double2(-kbx.y + gx.x, kbx.x + gx.y);
+    gF[N + c] = make_double2(-kby.y, kby.x);
+    gF[2 * N + c] = make_double2(-kbz.y, kbz.x);
+    gF[3 * N + c] = make_double2(kex.y, -kex.x);
+    gF[4 * N + c] = make_double2(key.y + gy.x, -key.x + gy.y);
+    gF[5 * N + c] = make_double2(kez.y + gz.x, -kez.x + gz.y);
+  }
+}
+
+struct EpiStore {
+  double2* __restrict__ dy;
+  __device__ __forceinline__ void operator()(size_t e, double2 v) const { dy[e] = v; }
+};
+
+}  // namespace spx

@@ -1,0 +1,168 @@
+"""Device Dopri8 solver and the ``simulation`` driver (spectrax/_simulation.py:113-194).
+
+``Dopri8Solver`` wraps ``spx_dopri8_*``: stage buffers, a CUDA graph of step
+attempts, and an on-device controller (Diffrax PIDController defaults or a
+constant step).  ``simulation`` mirrors the reference driver: it builds the
+merged parameters, integrates from 0 to t_max saving at
+``linspace(0, t_max, timesteps)``, and returns the same output dictionary
+(Ck, Fk, time, dCk, the parameters and the energy diagnostics).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import Dopri8, ImplicitMidpoint, initial_state, initialize_simulation_parameters
+from .vector_field import Plan, _stream_ptr, plan_for_params
+
+
+def species_masses(params):
+    """spectrax/_diagnostics.py:44-68: (1, mi_me) for two species, else ``ms``/ones."""
+    Ns = int(params["Ns"])
+    if "ms" in params:
+        return np.asarray(params["ms"], np.float64)
+    if "masses" in params:
+        return np.asarray(params["masses"], np.float64)
+    if Ns == 2 and "mi_me" in params:
+        return np.array([1.0, float(params["mi_me"])])
+    return np.ones(Ns)
+
+
+class Dopri8Solver:
+    def __init__(self, plan: Plan, t0: float, t1: float, dt0: float, ts=None, adaptive=True,
+                 rtol=1e-10, atol=1e-12, max_steps=1_000_000, save_states=True, masses=None):
+        L = _lib.lib()
+        self.plan = plan
+        self.ts = np.ascontiguousarray(np.asarray([] if ts is None else ts, np.float64))
+        self.nsave = len(self.ts)
+        self.Ns = plan.problem.Ns
+        self._masses = np.ascontiguousarray(np.ones(self.Ns) if masses is None else np.asarray(masses, np.float64))
+        o = _lib.spx_dopri8_opts()
+        o.t0, o.t1, o.dt0, o.rtol, o.atol = float(t0), float(t1), float(dt0), float(rtol), float(atol)
+        o.adaptive = 1 if adaptive else 0
+        o.nsave = self.nsave
+        o.save_ts = self.ts.ctypes.data_as(C.POINTER(C.c_double)) if self.nsave else None
+        o.max_steps = int(max_steps)
+        o.save_states = 1 if save_states else 0
+        o.masses = self._masses.ctypes.data_as(C.POINTER(C.c_double))
+        self.save_states = bool(save_states)
+        h = C.c_void_p()
+        with torch.cuda.device(plan.device):
+            _lib.check(L.spx_dopri8_create(plan.handle, C.byref(o), C.byref(h)), "spx_dopri8_create")
+        self.handle = h
+
+    def reset(self, y0, stream=None):
+        y0 = torch.as_tensor(y0).to(self.plan.device, torch.complex128).contiguous()
+        self.plan.check_state(y0, "y0")
+        _lib.check(_lib.lib().spx_dopri8_reset(self.handle, C.c_void_p(y0.data_ptr()), _stream_ptr(stream)),
+                   "spx_dopri8_reset")
+        return self
+
+    def advance(self, attempts: int, stream=None) -> int:
+        st = C.c_int32()
+        _lib.check(_lib.lib().spx_dopri8_advance(self.handle, int(attempts), _stream_ptr(stream), C.byref(st)),
+                   "spx_dopri8_advance")
+        return int(st.value)
+
+    def run(self, stream=None) -> int:
+        st = C.c_int32()
+        _lib.check(_lib.lib().spx_dopri8_run(self.handle, _stream_ptr(stream), C.byref(st)), "spx_dopri8_run")
+        return int(st.value)
+
+    def stats(self, stream=None) -> dict:
+        s = _lib.spx_dopri8_stats()
+        _lib.check(_lib.lib().spx_dopri8_stats_get(self.handle, C.byref(s), _stream_ptr(stream)), "stats")
+        return dict(t=s.t, dt=s.dt, accepted=s.accepted, rejected=s.rejected, rhs_evals=s.rhs_evals,
+                    status=s.status, status_name=_lib.STATUS_NAMES.get(s.status, "?"), saved=s.saved)
+
+    def _copy(self, what, out):
+        _lib.check(_lib.lib().spx_dopri8_copy(self.handle, what, C.c_void_p(out.data_ptr()),
+                                              out.numel() * out.element_size(), _stream_ptr()), "copy")
+        return out
+
+    def state(self) -> torch.Tensor:
+        return self._copy(0, torch.empty(self.plan.state_len, dtype=torch.complex128, device=self.plan.device))
+
+    def saved_states(self) -> torch.Tensor:
+        out = torch.empty((self.nsave, self.plan.state_len), dtype=torch.complex128, device=self.plan.device)
+        return self._copy(1, out) if self.nsave else out
+
+    def energies(self) -> torch.Tensor:
+        out = torch.empty((self.nsave, 2 + self.Ns), dtype=torch.float64, device=self.plan.device)
+        return self._copy(2, out) if self.nsave else out
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            try:
+                _lib._lib.spx_dopri8_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+def solve(params, y0=None, t_max=None, dt=None, ts=None, adaptive=True, rtol=None, atol=None,
+          max_steps=1_000_000, save_states=True, mask_mode=None):
+    """Integrate one instance; returns (solver, status)."""
+    plan = plan_for_params(params, mask_mode)
+    y0 = initial_state(params) if y0 is None else y0
+    t_max = float(params["t_max"] if t_max is None else t_max)
+    dt = float(params["dt"] if dt is None else dt)
+    tol = float(params.get("ode_tolerance", 1e-12))
+    s = Dopri8Solver(plan, 0.0, t_max, dt, ts=ts, adaptive=adaptive,
+                     rtol=tol if rtol is None else rtol, atol=tol if atol is None else atol,
+                     max_steps=max_steps, save_states=save_states, masses=species_masses(params))
+    s.reset(torch.as_tensor(np.asarray(y0, np.complex128)))
+    status = s.run()
+    return s, status
+
+
+def simulation(input_parameters=None, Nx=33, Ny=1, Nz=1, Nn=20, Nm=1, Np=1, Ns=2, timesteps=200,
+               dt=0.01, solver=None, adaptive_time_step=True, mask_mode=None, max_steps=1_000_000):
+    """Mirror of spectrax/_simulation.py:113-194 running on the GPU."""
+    solver = Dopri8() if solver is None else solver
+    p = initialize_simulation_parameters(input_parameters or {}, Nx, Ny, Nz, Nn, Nm, Np, Ns, timesteps, dt)
+    time = np.linspace(0, p["t_max"], timesteps)
+    if isinstance(solver, ImplicitMidpoint):
+        from .midpoint import midpoint_solve
+        ys, en, info = midpoint_solve(p, time, solver, mask_mode=mask_mode)
+    else:
+        s, status = solve(p, ts=time, adaptive=adaptive_time_step, dt=dt, max_steps=max_steps,
+                          mask_mode=mask_mode)
+        if status not in (1,):
+            raise RuntimeError(f"Dopri8 solve ended with status {_lib.STATUS_NAMES.get(status, status)}")
+        ys = s.saved_states().cpu().numpy()
+        en = s.energies().cpu().numpy()
+        info = s.stats()
+    NF = 6 * Nx * Ny * Nz
+    Ck = ys[:, :-NF].reshape(len(time), Ns * Nn * Nm * Np, Ny, Nx, Nz)
+    Fk = ys[:, -NF:].reshape(len(time), 6, Ny, Nx, Nz)
+    dCk = Ck.copy()
+    c = (int((Ny - 1) / 2), int((Nx - 1) / 2), int((Nz - 1) / 2))
+    dCk[:, 0, c[0], c[1], c[2]] = 0
+    dCk[:, Nn * Nm * Np, c[0], c[1], c[2]] = 0
+    out = {"Ck": Ck, "Fk": Fk, "time": time, "dCk": dCk, **p}
+    out.update(diagnostics_from_energies(p, en))
+    out["solver_stats"] = info
+    return out
+
+
+def diagnostics_from_energies(p, en):
+    """Keys added by spectrax/_diagnostics.py:221-233 from the device energies."""
+    Ns = int(p["Ns"])
+    alpha_s = np.asarray(p["alpha_s"], np.float64)
+    if Ns == 2 and "mi_me" in p:
+        lam = np.sqrt(1.0 / (2.0 * (1.0 / alpha_s[0] ** 2 + 1.0 / (p["mi_me"] * alpha_s[3] ** 2))))
+    else:
+        ax = alpha_s.reshape(Ns, 3)[:, 0]
+        lam = np.sqrt(1.0 / (2.0 * np.sum(1.0 / ax ** 2)))
+    d = {"Ns": Ns, "lambda_D": lam, "k_norm": np.sqrt(2.0) * np.pi * alpha_s[0] / p["Lx"],
+         "EM_energy": en[:, 0], "kinetic_energy": en[:, 1], "kinetic_energy_species": en[:, 2:],
+         "total_energy": en[:, 0] + en[:, 1]}
+    for s in range(Ns):
+        d[f"kinetic_energy_species{s + 1}"] = en[:, 2 + s]
+    return d
+

@@ -1,0 +1,152 @@
+"""Torch-facing right-hand side: the drop-in for ``spectrax._simulation.ode_system``.
+
+``ode_system(Nx, Ny, Nz, Nn, Nm, Np, Ns, t, Ck_Fk, args)`` has the reference's
+signature and flat complex128 layout (spectrax/_simulation.py:55-111).  It runs
+the hand-written sm_103a kernels of ``libspectrax_gb300.so``; there is no CPU
+path.  A CUDA tensor in gives a CUDA tensor out on the current torch stream; a
+NumPy array in is copied to the GPU and the result copied back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import get_mask_mode, problem_from_args, problem_from_params
+
+_cache_lock = threading.Lock()
+_plan_cache: dict = {}
+
+
+def _stream_ptr(stream=None):
+    s = torch.cuda.current_stream() if stream is None else stream
+    return C.c_void_p(s.cuda_stream)
+
+
+class Plan:
+    """Owns one ``spx_plan`` (device tables) plus a cached workspace."""
+
+    def __init__(self, problem: _lib.spx_problem, device=None):
+        L = _lib.lib()
+        self.problem = problem
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        with torch.cuda.device(self.device):
+            h = C.c_void_p()
+            _lib.check(L.spx_plan_create(C.byref(problem), C.byref(h)), "spx_plan_create")
+        self.handle = h
+        self.state_len = int(L.spx_state_len(C.byref(problem)))
+        self.ws_bytes = int(L.spx_rhs_workspace_bytes(h))
+        self._ws = None
+
+    @property
+    def shape(self):
+        p = self.problem
+        return (p.Nx, p.Ny, p.Nz, p.Nn, p.Nm, p.Np, p.Ns)
+
+    def workspace(self):
+        if self.ws_bytes and self._ws is None:
+            self._ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def ws_ptr(self):
+        ws = self.workspace()
+        return (C.c_void_p(ws.data_ptr()), C.c_size_t(ws.numel())) if ws is not None else (None, 0)
+
+    def check_state(self, y: torch.Tensor, name="y"):
+        if not isinstance(y, torch.Tensor) or not y.is_cuda:
+            raise TypeError(f"{name} must be a CUDA tensor")
+        if y.dtype != torch.complex128:
+            raise TypeError(f"{name} must be complex128, got {y.dtype}")
+        if y.numel() != self.state_len or not y.is_contiguous():
+            raise ValueError(f"{name} must be contiguous with {self.state_len} entries")
+        if y.device != self.device:
+            raise ValueError(f"{name} is on {y.device}, plan on {self.device}")
+
+    def rhs_into(self, y: torch.Tensor, dy: torch.Tensor, stream=None):
+        self.check_state(y)
+        self.check_state(dy, "dy")
+        ws, nb = self.ws_ptr()
+        _lib.check(_lib.lib().spx_rhs(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(dy.data_ptr()),
+                                      ws, nb, _stream_ptr(stream)), "spx_rhs")
+        return dy
+
+    def rhs(self, y: torch.Tensor, stream=None):
+        dy = torch.empty_like(y)
+        return self.rhs_into(y, dy, stream)
+
+    def jvp_into(self, y, v, out, stream=None):
+        for t, nm in ((y, "y"), (v, "v"), (out, "out")):
+            self.check_state(t, nm)
+        ws, nb = self.ws_ptr()
+        _lib.check(_lib.lib().spx_jvp(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(v.data_ptr()),
+                                      C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_jvp")
+        return out
+
+    def vjp_into(self, y, w, out, stream=None):
+        for t, nm in ((y, "y"), (w, "w"), (out, "out")):
+            self.check_state(t, nm)
+        ws, nb = self.ws_ptr()
+        _lib.check(_lib.lib().spx_vjp(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
+                                      C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_vjp")
+        return out
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            try:
+                _lib._lib.spx_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+def get_plan(problem: _lib.spx_problem, device=None) -> Plan:
+    dev = torch.cuda.current_device() if device is None else device
+    key = (bytes(problem), dev)
+    with _cache_lock:
+        pl = _plan_cache.get(key)
+        if pl is None:
+            pl = Plan(problem, dev)
+            _plan_cache[key] = pl
+        return pl
+
+
+def plan_for_params(params, mask_mode=None, device=None) -> Plan:
+    return get_plan(problem_from_params(params, mask_mode or get_mask_mode()), device)
+
+
+def _as_cuda_state(y, dev):
+    if isinstance(y, torch.Tensor):
+        return (y if y.is_cuda else y.to(dev)).to(torch.complex128).contiguous(), "torch_cpu" if not y.is_cuda else "torch"
+    arr = np.ascontiguousarray(np.asarray(y, dtype=np.complex128))
+    return torch.from_numpy(arr).to(dev), "numpy"
+
+
+def ode_system(Nx, Ny, Nz, Nn, Nm, Np, Ns, t, Ck_Fk, args, mask_mode=None):
+    """Drop-in for spectrax/_simulation.py:55-111 (same signature and layout)."""
+    del t
+    pb = problem_from_args(Nx, Ny, Nz, Nn, Nm, Np, Ns, args, mask_mode or get_mask_mode())
+    plan = get_plan(pb)
+    y, kind = _as_cuda_state(Ck_Fk, plan.device)
+    dy = plan.rhs(y)
+    if kind == "numpy":
+        return dy.cpu().numpy()
+    if kind == "torch_cpu":
+        return dy.cpu()
+    return dy
+
+
+def rhs(t, y, params, mask_mode=None):
+    """dy/dt for a merged parameter dict (``initialize_simulation_parameters`` output)."""
+    del t
+    plan = plan_for_params(params, mask_mode)
+    yy, kind = _as_cuda_state(y, plan.device)
+    dy = plan.rhs(yy)
+    if kind == "numpy":
+        return dy.cpu().numpy()
+    if kind == "torch_cpu":
+        return dy.cpu()
+    return dy

@@ -1,0 +1,100 @@
+"""GPU: linearised right-hand side (JVP) and its transpose (VJP) against the oracle.
+
+The right-hand side is affine plus bilinear, so the oracle JVP is the exact
+central difference (f(y+v) - f(y-v)) / 2, and the oracle VJP is the transpose of
+the Jacobian assembled column by column from it."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import rhs as orhs
+from oracle import tables as otab
+
+TOL = 1e-12
+
+
+def _params(shape, seed=0):
+    rng = np.random.default_rng(seed)
+    Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
+    user = dict(Lx=float(rng.uniform(3, 12)), Ly=float(rng.uniform(3, 12)), Lz=float(rng.uniform(3, 12)),
+                nu=float(rng.uniform(0.2, 2)), D=float(rng.uniform(0, 0.05)),
+                qs=list(rng.choice([-1.0, 1.0], Ns)), alpha_s=list(rng.uniform(0.3, 1.4, 3 * Ns)),
+                u_s=list(rng.uniform(-0.8, 0.8, 3 * Ns)), Omega_cs=list(rng.uniform(0.2, 1.5, Ns)))
+    return otab.initialize_simulation_parameters(user, *shape, 5, 0.01)
+
+
+def _n(shape):
+    Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
+    return Ns * Nn * Nm * Np * Nx * Ny * Nz + 6 * Nx * Ny * Nz
+
+
+def _rand(n, rng):
+    return rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+
+def _plan(p):
+    from spectrax_gb300 import vector_field
+    return vector_field.plan_for_params(p, "divide")
+
+
+JVP_SHAPES = [(17, 1, 1, 20, 1, 1, 2), (33, 1, 1, 7, 1, 1, 3), (64, 1, 1, 5, 1, 1, 1),
+              (6, 5, 1, 2, 3, 2, 2), (5, 1, 4, 3, 2, 2, 1), (8, 8, 1, 2, 2, 2, 1)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", JVP_SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_jvp_matches_central_difference(shape):
+    import torch
+    p = _params(shape, 1)
+    rng = np.random.default_rng(2)
+    n = _n(shape)
+    y, v = _rand(n, rng), _rand(n, rng)
+    ref = 0.5 * (orhs.rhs(p, y + v) - orhs.rhs(p, y - v))
+    plan = _plan(p)
+    yt, vt = torch.from_numpy(y).cuda(), torch.from_numpy(v).cuda()
+    out = torch.empty_like(yt)
+    plan.jvp_into(yt, vt, out)
+    assert rel_err(out.cpu().numpy(), ref) <= TOL
+
+
+VJP_SHAPES = [(9, 1, 1, 6, 1, 1, 2), (16, 1, 1, 5, 1, 1, 3), (17, 1, 1, 40, 1, 1, 2)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", VJP_SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_vjp_is_transpose(shape):
+    import torch
+    p = _params(shape, 3)
+    rng = np.random.default_rng(4)
+    n = _n(shape)
+    y, w = _rand(n, rng), _rand(n, rng)
+    plan = _plan(p)
+    yt, wt = torch.from_numpy(y).cuda(), torch.from_numpy(w).cuda()
+    g = torch.empty_like(yt)
+    plan.vjp_into(yt, wt, g)
+    g = g.cpu().numpy()
+    if n <= 400:
+        # assemble J column by column (exact for a quadratic map)
+        Jm = np.empty((n, n), np.complex128)
+        for j in range(n):
+            e = np.zeros(n, np.complex128)
+            e[j] = 1.0
+            Jm[:, j] = 0.5 * (orhs.rhs(p, y + e) - orhs.rhs(p, y - e))
+        assert rel_err(g, Jm.T @ w) <= TOL
+    # bilinear adjoint identity <w, J v> = <J^T w, v> for random v
+    v = _rand(n, rng)
+    Jv = 0.5 * (orhs.rhs(p, y + v) - orhs.rhs(p, y - v))
+    lhs, rhs = np.sum(w * Jv), np.sum(g * v)
+    assert abs(lhs - rhs) <= 1e-11 * abs(lhs)
+
+
+@pytest.mark.gpu
+def test_vjp_general_layout_is_rejected():
+    import torch
+    from spectrax_gb300 import SpectraxError
+    shape = (6, 5, 1, 2, 2, 2, 1)
+    p = _params(shape)
+    plan = _plan(p)
+    z = torch.zeros(_n(shape), dtype=torch.complex128, device="cuda")
+    with pytest.raises(SpectraxError):
+        plan.vjp_into(z, z.clone(), torch.empty_like(z))

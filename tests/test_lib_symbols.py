@@ -1,0 +1,57 @@
+"""CPU: the C-ABI library loads and exports every function include/*.h declares.
+
+No compute call is made here (no GPU in this environment)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for fn in sorted(os.listdir(inc)):
+        if fn.endswith(".h"):
+            src = open(os.path.join(inc, fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"\b(spx_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_library_exports_header():
+    from spectrax_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from spectrax_gb300 import build
+        build.build()
+    L = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+    assert len(declared_functions()) >= 10
+
+
+def test_version_and_errors_without_gpu():
+    from spectrax_gb300 import _lib
+    L = _lib.lib()
+    assert b"sm_103a" in L.spx_version()
+    # argument validation happens before any CUDA call
+    assert L.spx_rhs(None, None, None, None, 0, None) == _lib.SPX_E_ARG
+    assert b"null" in L.spx_last_error()
+
+
+def test_problem_struct_layout():
+    from spectrax_gb300 import _lib
+    # 10 int32 + 5 doubles + 8 + 8 + 24 + 24 doubles
+    assert ctypes.sizeof(_lib.spx_problem) == 40 + 5 * 8 + 64 * 8
+
+
+def test_no_cpu_fallback_in_product():
+    # nothing under the package imports the oracle
+    pkg = os.path.join(ROOT, "spectrax_gb300")
+    for dp, _, fns in os.walk(pkg):
+        for fn in fns:
+            if fn.endswith(".py"):
+                src = open(os.path.join(dp, fn)).read()
+                assert "oracle" not in re.findall(r"^\s*(?:from|import)\s+(\w+)", src, flags=re.M), fn

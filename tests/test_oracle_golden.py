@@ -1,0 +1,89 @@
+"""CPU: the oracle against fixtures generated from the reference's own source."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases, golden_params, rel_err
+from oracle import diag, fits, rhs, tables
+
+
+G, NAMES = golden_cases()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_rhs_matches_reference_source(name):
+    p = golden_params(G, name)
+    dy = rhs.rhs(p, G[name + "/y"])
+    assert rel_err(dy, G[name + "/dy"]) <= 1e-13
+
+
+def test_tables_match_reference_source():
+    t = np.load(os.path.join(GOLDEN, "tables.npz"))
+    for name in NAMES:
+        if name == "defaults":
+            continue
+        p = golden_params(G, name)
+        for k in ("kx_grid", "ky_grid", "kz_grid", "k2_grid", "nabla", "collision_matrix",
+                  "sqrt_n_plus", "sqrt_m_minus", "sqrt_p_plus"):
+            np.testing.assert_allclose(p[k], t[f"{name}/{k}"], rtol=0, atol=0)
+        Nx, Ny, Nz = (int(v) for v in G[name + "/shape"][:3])
+        np.testing.assert_array_equal(rhs.twothirds_mask(Ny, Nx, Nz), t[f"{name}/mask"])
+    p = tables.initialize_simulation_parameters({}, 33, 1, 1, 20, 1, 1, 2, 10, 0.01)
+    assert p["vte"] == t["defaults/vte"] and p["vti"] == t["defaults/vti"]
+    np.testing.assert_array_equal(tables.initial_state(p), G["defaults/y"])
+
+
+def test_energies_match_reference_source():
+    g = np.load(os.path.join(GOLDEN, "diag.npz"))
+    for name in sorted({k.split("/")[0] for k in g.files}):
+        Nx, Ny, Nz, Nn, Nm, Np, Ns = (int(v) for v in g[name + "/shape"])
+        e = diag.energies(g[name + "/ys"], Nx, Ny, Nz, Nn, Nm, Np, Ns, g[name + "/alpha_s"],
+                          g[name + "/u_s"], g[name + "/Omega_cs"], mi_me=float(g[name + "/mi_me"]))
+        for k in ("EM_energy", "kinetic_energy", "total_energy", "kinetic_energy_species"):
+            np.testing.assert_allclose(e[k], g[f"{name}/{k}"], rtol=1e-14, atol=0)
+
+
+def test_mask_edge_rounding():
+    # N=33: JAX's divide form keeps |k| <= 11 (23 modes); the multiply form 21 modes
+    assert rhs.centered_cutoff(33, "divide") == 11
+    assert rhs.centered_cutoff(33, "multiply") == 10
+    for n in (17, 64, 65, 129):
+        assert rhs.centered_cutoff(n, "divide") == rhs.centered_cutoff(n, "multiply") == n // 3
+    assert rhs.twothirds_mask(1, 33, 1, "divide").sum() == 23
+    assert rhs.twothirds_mask(1, 33, 1, "multiply").sum() == 21
+
+
+def test_hermite_neighbor_direction():
+    # shift_multi(C, dn=+1) reads C_{n+1} (spectrax/_model.py:79-97)
+    C = np.arange(2 * 1 * 1 * 4, dtype=np.complex128).reshape(2, 1, 1, 4, 1, 1, 1)
+    up = rhs.hermite_neighbor(C, 1, 0, 0)
+    dn = rhs.hermite_neighbor(C, -1, 0, 0)
+    assert up[0, 0, 0, 0, 0, 0, 0] == C[0, 0, 0, 1, 0, 0, 0] and up[0, 0, 0, 3, 0, 0, 0] == 0
+    assert dn[0, 0, 0, 1, 0, 0, 0] == C[0, 0, 0, 0, 0, 0, 0] and dn[0, 0, 0, 0, 0, 0, 0] == 0
+
+
+def test_rhs_is_affine_plus_bilinear():
+    # f(y) = L y + N(F, C): check the bilinear identity on the golden 2D3V case
+    name = "2d3v_6x5"
+    p = golden_params(G, name)
+    rng = np.random.default_rng(3)
+    n = len(G[name + "/y"])
+    a = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    f = lambda y: rhs.rhs(p, y)
+    # s -> f(a + s b) is a quadratic polynomial: its third difference vanishes
+    third = f(a + 3 * b) - 3 * f(a + 2 * b) + 3 * f(a + b) - f(a)
+    assert np.linalg.norm(third) <= 1e-12 * np.linalg.norm(f(a + 3 * b))
+    # and the map is not affine (the nonlinear term is really there)
+    second = f(a + 2 * b) - 2 * f(a + b) + f(a)
+    assert np.linalg.norm(second) > 1e-3 * np.linalg.norm(f(a))
+
+
+def test_fits_on_synthetic_signals():
+    t = np.linspace(0, 40, 801)
+    E = np.exp(2 * -0.15 * t) * (1.1 + np.cos(2.8 * t))
+    assert abs(fits.landau_rate(t, E, 100) - (-0.15)) < 5e-3
+    E2 = 1e-8 * np.exp(2 * 0.2 * t)
+    assert abs(fits.growth_rate(t, E2, 300) - 0.2) < 1e-10
+    assert abs(fits.window_slope(t, E2, 10, 40) - 0.4) < 1e-10
