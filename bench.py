@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark: adaptive Dopri8 steps of the 1D1V two-stream workload on GB300.
+
+Workload (the two-stream configuration): 3 species (two counter-streaming
+electron beams at +-u with u = 1.0 alpha, alpha = 0.5, half density each;
+ions with mi/me = 1836), Nx = 129 Fourier modes, Nn = 256 Hermite modes,
+k_min = 0.2 (Lx = 10 pi), nu = 1, 2/3 de-aliasing, complex128, seeded random
+phases of amplitude 1e-3 on modes 1..8, Diffrax-default PID controller with
+rtol = 1e-10, atol = 1e-12.  Synthetic, seeded data (the reference publishes no
+dataset for this path).
+
+One step = one Dopri8 step attempt (13 fused right-hand-side stage launches
+plus the on-device controller).  `value` is right-hand-side evaluations per
+second over the timed steps (max over ranks, summed over ranks); L2 is flushed
+before every timed step.  `e2e` repeats the measurement through the public
+Python API with the state copied host->device and device->host every step.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np
+
+SHAPE = (129, 1, 1, 256, 1, 1, 3)       # Nx, Ny, Nz, Nn, Nm, Np, Ns
+RTOL, ATOL = 1e-10, 1e-12
+METRIC = "rhs_evals_per_s"
+UNIT = "RHS evals/s"
+WORKLOAD = "two-stream 1D1V, Nx=129, Nn=256, Ns=3, adaptive Dopri8 (rtol 1e-10, atol 1e-12)"
+
+
+def two_stream_params(seed=0):
+    """Parameter dict + initial state of the two-stream workload."""
+    Nx, Ny, Nz, Nn, Nm, Np, Ns = SHAPE
+    alpha, u, mi_me = 0.5, 0.5, 1836.0
+    ai = alpha * np.sqrt(1.0 / mi_me)
+    user = dict(Lx=2 * np.pi / 0.2, nu=1.0, D=0.0, qs=[-1.0, -1.0, 1.0],
+                alpha_s=[alpha] * 6 + [ai] * 3, u_s=[u, 0, 0, -u, 0, 0, 0, 0, 0],
+                Omega_cs=[1.0, 1.0, 1.0 / mi_me], mi_me=mi_me, ms=[1.0, 1.0, mi_me],
+                t_max=100.0, ode_tolerance=RTOL)
+    from spectrax_gb300.params import initialize_simulation_parameters
+    p = initialize_simulation_parameters(user, Nx, Ny, Nz, Nn, Nm, Np, Ns, 101, 0.01)
+    rng = np.random.default_rng(seed)
+    c0 = Nx // 2
+    Ck = np.zeros((Ns, Nn, Nx), np.complex128)
+    dens = [0.5, 0.5, 1.0]
+    for s in range(Ns):
+        Ck[s, 0, c0] = dens[s] / p["alpha_s"][3 * s] ** 3
+    rho = np.zeros(Nx, np.complex128)
+    for j in range(1, 9):
+        d = 1e-3 * np.exp(2j * np.pi * rng.random())
+        for s in (0, 1):
+            Ck[s, 0, c0 + j] = 0.5 * Ck[s, 0, c0] * d
+            Ck[s, 0, c0 - j] = np.conj(Ck[s, 0, c0 + j])
+    a = np.asarray(p["alpha_s"]).reshape(Ns, 3)
+    for s in range(Ns):
+        rho += p["qs"][s] * a[s].prod() * Ck[s, 0]
+    Fk = np.zeros((6, Nx), np.complex128)
+    K = p["kx_grid"][0, :, 0] / p["Lx"]
+    nz = np.abs(K) > 0
+    Fk[0, nz] = -1j * rho[nz] / (K[nz] * p["Omega_cs"][0])
+    y0 = np.concatenate([Ck.ravel(), Fk.ravel()])
+    return p, y0
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per stage launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "dopri8_stage_two_stream.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch, lib):
+    """Live FP64 FMA-rate probe (the compute roofline)."""
+    import ctypes as C
+    blocks = 152 * 8
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    iters = 20000
+    for _ in range(2):
+        lib.spx_probe_fp64(C.c_void_p(out.data_ptr()), blocks, iters, None)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(3):
+        e0.record()
+        lib.spx_probe_fp64(C.c_void_p(out.data_ptr()), blocks, iters, None)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 16.0 * iters * blocks * 256 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def cpu_sample(p, y0, seconds=10.0, workers=None):
+    """Oracle (NumPy/SciPy FP64 port) right-hand sides per second on host cores."""
+    from oracle import rhs as orhs
+    orhs.set_fft_workers(workers)
+    try:
+        orhs.rhs(p, y0)
+        n = 0
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            orhs.rhs(p, y0)
+            n += 1
+        dt = time.perf_counter() - t0
+    finally:
+        orhs.set_fft_workers(None)
+    return n / dt, n
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, local = dist_setup(args)
+    if rank != 0:
+        return 0
+    from oracle import dopri8 as od
+    from oracle import rhs as orhs
+    p, y0 = two_stream_params()
+    workers = os.cpu_count() or 1
+    orhs.set_fft_workers(workers)
+    f = lambda t, y: orhs.rhs(p, y)
+    h = 0.01
+    for _ in range(args.warmup):
+        od.dopri8_step(f, 0.0, y0, h)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        od.dopri8_step(f, 0.0, y0, h)
+    dt = time.perf_counter() - t0
+    orhs.set_fft_workers(None)
+    evals = 13 * args.steps
+    value = evals / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "step": "one Dopri8 step (13 RHS evaluations)",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                             "sample": f"{args.steps} oracle Dopri8 steps (NumPy/SciPy FP64 restatement; "
+                                       "JAX is not installable here, so the reference itself cannot run)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from spectrax_gb300 import _lib, perf
+    from spectrax_gb300.dopri8 import Dopri8Solver
+    from spectrax_gb300.vector_field import plan_for_params
+
+    p, y0 = two_stream_params(seed=rank)
+    plan = plan_for_params(p, "divide")
+    n = plan.state_len
+    solver = Dopri8Solver(plan, 0.0, 1e9, 0.01, ts=None, adaptive=True, rtol=RTOL, atol=ATOL,
+                          max_steps=1 << 40, save_states=False, masses=[1.0, 1.0, 1836.0])
+    solver.reset(torch.from_numpy(y0))
+    solver.enqueue(max(3, args.warmup))
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > L2 (129 MB)
+    st0 = solver.stats()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            evs[i][0].record()
+            solver.enqueue(1)
+            evs[i][1].record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t_ms = sum(a.elapsed_time(b) for a, b in evs)
+    st1 = solver.stats()
+    evals = st1["rhs_evals"] - st0["rhs_evals"]
+    acc = st1["accepted"] - st0["accepted"]
+    # e2e: through the public API with host buffers every step
+    host_in = torch.from_numpy(y0).pin_memory()
+    host_out = torch.empty(n, dtype=torch.complex128).pin_memory()
+    e2e_solver = Dopri8Solver(plan, 0.0, 1e9, max(st1["dt"], 1e-6), ts=None, adaptive=True, rtol=RTOL, atol=ATOL,
+                              max_steps=1 << 40, save_states=False)
+    for _ in range(2):
+        e2e_solver.reset(host_in)
+        e2e_solver.enqueue(1)
+        e2e_solver._copy(0, host_out)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_solver.reset(host_in)                  # host -> device copy of the state
+        e2e_solver.enqueue(1)                      # first attempt after a reset: 13 RHS evaluations
+        e2e_solver._copy(0, host_out)              # device -> host copy of the result
+        torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_evals = 13 * args.steps
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms, e2e_s, float(evals), float(e2e_evals)], dtype=torch.float64, device="cuda")
+        mx = tt.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = tt.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        t_ms, e2e_s = float(mx[0]), float(mx[1])
+        evals_all, e2e_evals_all = float(sm[2]), float(sm[3])
+    else:
+        evals_all, e2e_evals_all = float(evals), float(e2e_evals)
+    if rank != 0:
+        return 0
+    value = evals_all / (t_ms * 1e-3)
+    ms_per_step = t_ms / args.steps
+    hbm_peak, hbm_src = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch, _lib.lib())
+    stage_ms = ms_per_step / 13.0
+    bytes_launch = perf.dopri8_vectors_per_step() * n * 16 / 13.0
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    Ns_, Nn_ = SHAPE[6], SHAPE[3]
+    T = max(1, min(16, -(-Ns_ * Nn_ // nsm)))
+    ntiles = -(-Nn_ // T)
+    ops = perf.rhs_ops(SHAPE, T, ntiles)
+    # per-stage FP64 work: one RHS + the fused Runge-Kutta combination (~2 FMA per read vector)
+    flops_stage = ops.flops + 4.0 * (perf.dopri8_vectors_per_step() / 13.0) * n
+    achieved_gbs = bytes_launch / (stage_ms * 1e-3) / 1e9
+    achieved_tf = flops_stage / (stage_ms * 1e-3) / 1e12
+    traffic = profile_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "step": "one Dopri8 step attempt (13 fused RHS stages + controller)",
+                   "state_len": n, "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "accepted_steps_per_s": (acc * world) / (t_ms * 1e-3),
+        "e2e": {"value": e2e_evals_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+                "d2h_bytes_per_step": n * 16},
+        "gpu_launches": args.steps * 14,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                     "peak_source": hbm_src,
+                     "kernel": "k_d8_stage_1v (duration = step time / 13)"},
+        "fp64": {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                 "frac": achieved_tf / fp64_peak, "peak_source": "live FMA probe (spx_probe_fp64)",
+                 "note": "the binding ceiling of this path on GB300"},
+        "clocks": clk.summary(),
+    }
+    if world == 1:
+        cpu_v, cpu_n = cpu_sample(p, y0, seconds=args.cpu_seconds, workers=os.cpu_count())
+        line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{cpu_n} oracle RHS evaluations of the same state "
+                                          f"(~{args.cpu_seconds:.0f} s, scipy.fft with all host threads)"}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -143,6 +143,10 @@ int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream);
 /* Replay up to `max_attempts` step attempts (accepted or rejected); returns
  * after the solve ends or the attempts are used.  *status_out gets the status. */
 int spx_dopri8_advance(spx_dopri8* s, int64_t max_attempts, void* stream, int32_t* status_out);
+/* Enqueue exactly `attempts` step attempts on `stream` without waiting (attempts
+ * after the end of the solve do nothing).  For timing and for callers that poll
+ * the status themselves. */
+int spx_dopri8_enqueue(spx_dopri8* s, int64_t attempts, void* stream);
 /* Run to the end (advance in chunks until status != RUNNING). */
 int spx_dopri8_run(spx_dopri8* s, void* stream, int32_t* status_out);
 int spx_dopri8_stats_get(spx_dopri8* s, spx_dopri8_stats* out, void* stream);

@@ -22,6 +22,30 @@ import numpy as np
 _AX = (-3, -2, -1)
 SQRT2 = np.sqrt(2.0)
 
+# FFT backend: NumPy (default) or scipy.fft with a worker count, so the CPU
+# baseline can use every host core the way XLA's CPU FFT would.
+_FFT_WORKERS = None
+
+
+def set_fft_workers(n):
+    """Use scipy.fft with `n` threads (None: NumPy's single-threaded FFT)."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = n
+
+
+def _ifftn(x):
+    if _FFT_WORKERS:
+        import scipy.fft as sf
+        return sf.ifftn(x, axes=_AX, norm="forward", workers=_FFT_WORKERS)
+    return np.fft.ifftn(x, axes=_AX, norm="forward")
+
+
+def _fftn(x):
+    if _FFT_WORKERS:
+        import scipy.fft as sf
+        return sf.fftn(x, axes=_AX, norm="forward", workers=_FFT_WORKERS)
+    return np.fft.fftn(x, axes=_AX, norm="forward")
+
 
 # --------------------------------------------------------------------------- mask
 def _fftfreq_times_n(n: int, mode: str) -> np.ndarray:
@@ -171,7 +195,7 @@ def hermite_fourier_system(Ck, C, F, P, Nn, Nm, Np, Ns, mask):
                + (smm * SQRT2 / a1) * Ey * nb(C, 0, -1, 0)
                + (spm * SQRT2 / a2) * Ez * nb(C, 0, 0, -1)
                + Bx * aux_x + By * aux_y + Bz * aux_z)
-    nonlinear = np.fft.fftshift(np.fft.fftn(bracket, axes=_AX, norm="forward"), axes=_AX) * mask
+    nonlinear = np.fft.fftshift(_fftn(bracket), axes=_AX) * mask
 
     kx, ky, kz, k2 = P["kx_grid"], P["ky_grid"], P["kz_grid"], P["k2_grid"]
     col = P["col"][None, :, :, :, None, None, None]
@@ -193,8 +217,8 @@ def ode_system(Nx, Ny, Nz, Nn, Nm, Np, Ns, t, Ck_Fk, args, mask_mode: str = "div
     Ck = y[:NC].reshape(Nn * Nm * Np * Ns, Ny, Nx, Nz)
     Fk = y[NC:].reshape(6, Ny, Nx, Nz)
     mask = twothirds_mask(Ny, Nx, Nz, mask_mode)
-    F = np.fft.ifftn(np.fft.ifftshift(Fk * mask, axes=_AX), axes=_AX, norm="forward")
-    C = np.fft.ifftn(np.fft.ifftshift(Ck * mask, axes=_AX), axes=_AX, norm="forward")
+    F = _ifftn(np.fft.ifftshift(Fk * mask, axes=_AX))
+    C = _ifftn(np.fft.ifftshift(Ck * mask, axes=_AX))
     dCk = hermite_fourier_system(Ck, C, F, P, Nn, Nm, Np, Ns, mask)
     dBk = -1j * cross_product(P["nabla"], Fk[:3])
     J = plasma_current(P["qs"], P["alpha_s"], P["u_s"], Ck, Nn, Nm, Np, Ns)

@@ -91,6 +91,7 @@ _PROTOS = {
     "spx_dopri8_reset": (C.c_int, [_VP, _VP, _VP]),
     "spx_dopri8_advance": (C.c_int, [_VP, C.c_int64, _VP, C.POINTER(C.c_int32)]),
     "spx_dopri8_run": (C.c_int, [_VP, _VP, C.POINTER(C.c_int32)]),
+    "spx_dopri8_enqueue": (C.c_int, [_VP, C.c_int64, _VP]),
     "spx_dopri8_stats_get": (C.c_int, [_VP, C.POINTER(spx_dopri8_stats), _VP]),
     "spx_dopri8_state": (_VP, [_VP]),
     "spx_dopri8_saved_states": (_VP, [_VP]),

@@ -395,8 +395,8 @@ struct spx_dopri8 {
   int grid_stage = 0, grid_real = 0;
   int attempts_per_graph = 8;
   cudaStream_t cap = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr, graph1 = nullptr;
+  cudaGraphExec_t exec = nullptr, exec1 = nullptr;   // `attempts_per_graph` attempts / one attempt
   int* h_status = nullptr;   // pinned
   std::vector<double> ts;
 };
@@ -460,6 +460,8 @@ static int d8_free(spx_dopri8* s) {
   if (!s) return SPX_OK;
   if (s->exec) cudaGraphExecDestroy(s->exec);
   if (s->graph) cudaGraphDestroy(s->graph);
+  if (s->exec1) cudaGraphExecDestroy(s->exec1);
+  if (s->graph1) cudaGraphDestroy(s->graph1);
   if (s->cap) cudaStreamDestroy(s->cap);
   if (s->block) cudaFree(s->block);
   if (s->h_status) cudaFreeHost(s->h_status);
@@ -547,6 +549,12 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   for (int i = 0; i < s->attempts_per_graph; ++i) enqueue_attempt(s, s->cap);
   e = cudaStreamEndCapture(s->cap, &s->graph);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    enqueue_attempt(s, s->cap);
+    e = cudaStreamEndCapture(s->cap, &s->graph1);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec1, s->graph1, 0);
   if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "dopri8 graph"); }
   *out = s;
   return SPX_OK;
@@ -576,16 +584,33 @@ int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
 int spx_dopri8_advance(spx_dopri8* s, int64_t max_attempts, void* stream, int32_t* status_out) {
   if (!s) { set_error("spx_dopri8_advance: null solver"); return SPX_E_ARG; }
   cudaStream_t st = (cudaStream_t)stream;
-  const int64_t reps = (max_attempts + s->attempts_per_graph - 1) / s->attempts_per_graph;
   int status = SPX_ST_RUNNING;
-  for (int64_t r = 0; r < reps; ++r) {
-    SPX_CUDA(cudaGraphLaunch(s->exec, st));
+  int64_t left = max_attempts;
+  while (left > 0) {
+    // replay whole graphs of `attempts_per_graph` attempts, then single attempts
+    if (left >= s->attempts_per_graph) {
+      SPX_CUDA(cudaGraphLaunch(s->exec, st));
+      left -= s->attempts_per_graph;
+    } else {
+      SPX_CUDA(cudaGraphLaunch(s->exec1, st));
+      left -= 1;
+      if (left > 0) continue;
+    }
     SPX_CUDA(cudaMemcpyAsync(s->h_status, &s->args.st->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     SPX_CUDA(cudaStreamSynchronize(st));
     status = *s->h_status;
     if (status != SPX_ST_RUNNING) break;
   }
   if (status_out) *status_out = status;
+  return SPX_OK;
+}
+
+int spx_dopri8_enqueue(spx_dopri8* s, int64_t attempts, void* stream) {
+  if (!s || attempts < 0) { set_error("spx_dopri8_enqueue: bad argument"); return SPX_E_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int64_t i = 0; i + s->attempts_per_graph <= attempts; i += s->attempts_per_graph)
+    SPX_CUDA(cudaGraphLaunch(s->exec, st));
+  for (int64_t i = 0; i < attempts % s->attempts_per_graph; ++i) SPX_CUDA(cudaGraphLaunch(s->exec1, st));
   return SPX_OK;
 }
 

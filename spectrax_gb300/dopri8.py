@@ -67,6 +67,11 @@ class Dopri8Solver:
                    "spx_dopri8_advance")
         return int(st.value)
 
+    def enqueue(self, attempts: int, stream=None):
+        """Queue exactly `attempts` step attempts without synchronising."""
+        _lib.check(_lib.lib().spx_dopri8_enqueue(self.handle, int(attempts), _stream_ptr(stream)),
+                   "spx_dopri8_enqueue")
+
     def run(self, stream=None) -> int:
         st = C.c_int32()
         _lib.check(_lib.lib().spx_dopri8_run(self.handle, _stream_ptr(stream), C.byref(st)), "spx_dopri8_run")

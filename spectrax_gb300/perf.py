@@ -1,0 +1,110 @@
+"""Algorithmic cost model of the GPU path (bytes and FP64 operations).
+
+Bytes follow the definition "read every input vector once, write every output
+vector once" (16 B per complex128 entry).  FP64 operations count the double
+instructions the kernels issue (an FMA counts as 2 flops), from the FFT plan
+(radices and spans) and the fused epilogues; they are checked against ncu's
+SASS counters in ``profiles/``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+# RK8(7)13M: per stage i (0-based) the number of earlier stage vectors the
+# fused epilogue reads to form the next stage input (nonzero a(i+1, j), j < i),
+# and for the last stage the number of stage vectors read for y_new and the error.
+_NEXT_INPUT_READS = [0, 1, 1, 2, 2, 3, 4, 5, 6, 7, 8, 9]
+_LAST_STAGE_READS = 8
+
+
+def dopri8_vectors_per_step() -> int:
+    """State-sized vectors read + written by one 13-stage step of the fused stepper."""
+    total = 3                              # stage 0: read y, write K0 and the next input
+    for m in _NEXT_INPUT_READS[1:]:
+        total += 4 + m                     # read input and y, write K_i and next input
+    total += 2 + _LAST_STAGE_READS + 1     # last stage: input, y, K_j, write y_new
+    return total
+
+
+def factorize(n: int):
+    r = []
+    m = n
+    while m % 8 == 0:
+        r.append(8); m //= 8
+    while m % 4 == 0:
+        r.append(4); m //= 4
+    while m % 2 == 0:
+        r.append(2); m //= 2
+    p = 3
+    while m > 1:
+        while m % p == 0:
+            r.append(p); m //= p
+        p += 2
+    return sorted(r, reverse=True)
+
+
+@dataclass
+class Ops:
+    instr: float = 0.0   # FP64 instructions (lane ops)
+    flops: float = 0.0
+
+    def add(self, fma=0, addmul=0, mult=1.0):
+        self.instr += mult * (fma + addmul)
+        self.flops += mult * (2 * fma + addmul)
+
+
+def fft_line_ops(n: int) -> Ops:
+    """FP64 work of one length-n line through the Stockham engine."""
+    o = Ops()
+    if n == 1:
+        return o
+    Ns = 1
+    for R in factorize(n):
+        M = n // R
+        tw_tasks = (M - M // Ns) if Ns > 1 else 0
+        if R % 2 == 0:
+            o.add(fma=2 * (R - 1), addmul=2 * (R - 1), mult=tw_tasks)   # twiddle cmuls
+            dft = {2: 4, 4: 16, 8: 56}[R]
+            o.add(addmul=dft, mult=M)
+        else:
+            h = (R - 1) // 2
+            o.add(fma=4, addmul=4, mult=tw_tasks * h)                   # two twiddles per pair
+            o.add(addmul=4, mult=M * h)                                 # sum / difference
+            o.add(fma=4 * h, addmul=4, mult=M * (h + 1))                # symmetric direct DFT
+        Ns *= R
+    return o
+
+
+def rhs_ops(shape, tile=None, ntiles=None) -> Ops:
+    """FP64 work of one right-hand-side evaluation (fused 1D1V or general path)."""
+    Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
+    o = Ops()
+    plane = Nx * Ny * Nz
+    if Ny == 1 and Nz == 1 and Nm == 1 and Np == 1:
+        f = fft_line_ops(Nx)
+        ntiles = ntiles or 1
+        lines_inv = Ns * (Nn + ntiles)          # C_{n-1} per plane + one G per tile
+        lines_fwd = Ns * Nn
+        o.instr += f.instr * (lines_inv + lines_fwd)
+        o.flops += f.flops * (lines_inv + lines_fwd)
+        o.add(fma=2, addmul=2, mult=Ns * Nn * Nx)            # G * C
+        o.add(fma=6, addmul=4, mult=Ns * Nn * Nx)            # streaming, damping, NL add
+        o.add(fma=4, addmul=2, mult=Ns * Nx)                 # G combination
+        o.add(fma=8 * Ns + 6, addmul=24, mult=Nx)            # Maxwell + current
+        return o
+    fy, fx, fz = fft_line_ops(Ny), fft_line_ops(Nx), fft_line_ops(Nz)
+    per_plane = Ops(instr=fy.instr * Nx * Nz + fx.instr * Ny * Nz + fz.instr * Ny * Nx,
+                    flops=fy.flops * Nx * Nz + fx.flops * Ny * Nz + fz.flops * Ny * Nx)
+    nplanes = Ns * Nn * Nm * Np
+    ntr = 2 * nplanes + 3 * Ns + 3
+    o.instr += per_plane.instr * ntr
+    o.flops += per_plane.flops * ntr
+    o.add(fma=30, addmul=12, mult=nplanes * plane)           # real-space bracket (interior planes)
+    o.add(fma=12, addmul=8, mult=nplanes * plane)            # streaming x/y/z, damping, NL add
+    o.add(fma=8 * Ns + 6, addmul=24, mult=plane)
+    return o
+
+
+def state_len(shape) -> int:
+    Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
+    return Ns * Nn * Nm * Np * Nx * Ny * Nz + 6 * Nx * Ny * Nz
