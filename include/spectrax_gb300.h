@@ -107,6 +107,23 @@ int spx_jvp(const spx_plan* plan, const void* y, const void* v, void* Jv, void* 
 int spx_vjp(const spx_plan* plan, const void* y, const void* w, void* g, void* ws,
             size_t ws_bytes, void* stream);
 
+/*
+ * Allocation-free g = J(y)^T w for the 1D1V layout (no counterpart in the
+ * reference).  For callers that cannot allocate device memory where they need
+ * the VJP — inside a CUDA stream capture, in real-time loops that must not
+ * allocate after start-up, or under a host framework that owns every device
+ * byte — this variant keeps spx_vjp's scratch (the per-tile partial sums of the
+ * field gradient) in a fixed file-scope device array of
+ * SPX_VJP_NOALLOC_MAX_ENTRIES complex128 values (1 MiB, held by every GPU that
+ * loads the library until exit) and allocates nothing.  Problems needing more
+ * than that (Ns * Hermite tiles * Nx entries) get SPX_E_UNSUPPORTED.  All calls
+ * share the array: calls that overlap on the GPU race, so serialise them.  The
+ * first call on a device looks up the array's address and should come before
+ * any stream capture.  `plan` comes from spx_plan_create at set-up.
+ */
+#define SPX_VJP_NOALLOC_MAX_ENTRIES 65536
+int spx_vjp_noalloc(const spx_plan* plan, const void* y, const void* w, void* g, void* stream);
+
 /* ------------------------------------------------------------------ Dopri8 */
 typedef struct spx_dopri8_opts {
   double t0, t1;     /* integration interval */

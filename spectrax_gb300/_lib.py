@@ -86,6 +86,7 @@ _PROTOS = {
     "spx_rhs": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_jvp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_vjp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
+    "spx_vjp_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "spx_dopri8_create": (C.c_int, [_VP, C.POINTER(spx_dopri8_opts), C.POINTER(_VP)]),
     "spx_dopri8_destroy": (C.c_int, [_VP]),
     "spx_dopri8_reset": (C.c_int, [_VP, _VP, _VP]),

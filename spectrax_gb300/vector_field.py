@@ -93,6 +93,20 @@ class Plan:
                                       C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_vjp")
         return out
 
+    def vjp_noalloc_into(self, y, w, out, stream=None):
+        """J(y)^T w through spx_vjp_noalloc: no workspace, nothing allocated.
+
+        For callers that may not allocate device memory at this point (inside a
+        stream capture, real-time loops, host frameworks that own all device
+        memory).  The scratch is a fixed 1 MiB device array shared by all calls;
+        calls that overlap on the GPU race."""
+        for t, nm in ((y, "y"), (w, "w"), (out, "out")):
+            self.check_state(t, nm)
+        _lib.check(_lib.lib().spx_vjp_noalloc(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
+                                              C.c_void_p(out.data_ptr()), _stream_ptr(stream)),
+                   "spx_vjp_noalloc")
+        return out
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h is not None and h.value and _lib._lib is not None:
