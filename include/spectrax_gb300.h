@@ -179,6 +179,49 @@ const double* spx_dopri8_saved_energies(spx_dopri8* s);
  * `bytes` must equal the size of that item. */
 int spx_dopri8_copy(spx_dopri8* s, int32_t what, void* dst, size_t bytes, void* stream);
 
+/* ------------------------------------------------------------------ batch */
+/*
+ * Many independent 1D1V instances (different Nx, Nn, Ns, L, nu, alpha, u),
+ * each integrated by adaptive (or constant-step) Dopri8 to t1, all in ONE
+ * persistent launch: each thread-block cluster of `cluster` CTAs takes the next
+ * instance from a largest-first work queue.  Replaces the serial scan loop of
+ * Examples/1D_Landau_damping_dr_curve.py:149-175 (one simulation() per k).
+ * The launch is captured once as a CUDA graph.
+ */
+typedef struct spx_batch_opts {
+  double t1, dt0, rtol, atol;
+  int64_t max_steps;     /* per instance */
+  int32_t adaptive;      /* 1: Diffrax PIDController defaults; 0: constant step dt0 */
+  int32_t nsave;         /* shared save times (energies recorded at each) */
+  const double* save_ts; /* host, nsave increasing times in [0, t1] */
+  int32_t cluster;       /* CTAs per instance, 1..8 */
+  int32_t tile;          /* Hermite planes per tile (0: 8) */
+  const double* masses;  /* host, n x SPX_MAX_SPECIES species masses (NULL: ones) */
+} spx_batch_opts;
+
+typedef struct spx_batch_stats {
+  double t, dt;
+  int64_t accepted, rejected, rhs_evals;
+  int32_t status, saved;
+} spx_batch_stats;
+
+typedef struct spx_batch spx_batch;
+
+int spx_batch_create(int32_t n, const spx_problem* problems, const spx_batch_opts* opts, spx_batch** out);
+int spx_batch_destroy(spx_batch* b);
+/* Offset (complex128 entries) of instance i in the packed state arrays; i = n gives the total. */
+int64_t spx_batch_offset(const spx_batch* b, int32_t i);
+/* Offset (doubles) of instance i in the packed energies (nsave x (2 + Ns) per instance). */
+int32_t spx_batch_energy_offset(const spx_batch* b, int32_t i);
+/* CTAs of the persistent grid. */
+int32_t spx_batch_grid(const spx_batch* b);
+/* Copy the packed initial states in (host or device), replay the graph, copy the
+ * packed final states out (if y_final is not NULL).  Asynchronous on `stream`. */
+int spx_batch_run(spx_batch* b, const void* y0, void* y_final, void* stream);
+/* Per-instance counters (host array of n, synchronises) and packed energies
+ * (host or device, may be NULL). */
+int spx_batch_results(spx_batch* b, spx_batch_stats* stats, double* energies, void* stream);
+
 /* ------------------------------------------------------------ measurement */
 /*
  * FP64 issue-rate probe (no counterpart in the reference): `blocks` CTAs of 256

@@ -66,12 +66,20 @@ class spx_dopri8_stats(C.Structure):
 
 class spx_batch_opts(C.Structure):
     _fields_ = [
-        ("t1", C.c_double), ("rtol", C.c_double), ("atol", C.c_double),
+        ("t1", C.c_double), ("dt0", C.c_double), ("rtol", C.c_double), ("atol", C.c_double),
         ("max_steps", C.c_int64),
-        ("nsave", C.c_int32),
-        ("cluster", C.c_int32),
-        ("threads", C.c_int32),
-        ("adaptive", C.c_int32),
+        ("adaptive", C.c_int32), ("nsave", C.c_int32),
+        ("save_ts", C.POINTER(C.c_double)),
+        ("cluster", C.c_int32), ("tile", C.c_int32),
+        ("masses", C.POINTER(C.c_double)),
+    ]
+
+
+class spx_batch_stats(C.Structure):
+    _fields_ = [
+        ("t", C.c_double), ("dt", C.c_double),
+        ("accepted", C.c_int64), ("rejected", C.c_int64), ("rhs_evals", C.c_int64),
+        ("status", C.c_int32), ("saved", C.c_int32),
     ]
 
 
@@ -98,6 +106,13 @@ _PROTOS = {
     "spx_dopri8_saved_states": (_VP, [_VP]),
     "spx_dopri8_saved_energies": (_VP, [_VP]),
     "spx_dopri8_copy": (C.c_int, [_VP, C.c_int32, _VP, C.c_size_t, _VP]),
+    "spx_batch_create": (C.c_int, [C.c_int32, C.POINTER(spx_problem), C.POINTER(spx_batch_opts), C.POINTER(_VP)]),
+    "spx_batch_destroy": (C.c_int, [_VP]),
+    "spx_batch_offset": (C.c_int64, [_VP, C.c_int32]),
+    "spx_batch_energy_offset": (C.c_int32, [_VP, C.c_int32]),
+    "spx_batch_grid": (C.c_int32, [_VP]),
+    "spx_batch_run": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "spx_batch_results": (C.c_int, [_VP, C.POINTER(spx_batch_stats), C.POINTER(C.c_double), _VP]),
     "spx_probe_fp64": (C.c_int, [_VP, C.c_int, C.c_int, _VP]),
 }
 

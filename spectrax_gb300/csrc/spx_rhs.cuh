@@ -10,6 +10,16 @@
 
 namespace spx {
 
+// Global-load policies.  Kernels that only read data written by earlier
+// launches use plain loads; a persistent kernel that reads what other CTAs of
+// the same launch wrote uses L2-coherent loads (ld.global.cg, no L1/texture).
+struct LdPlain {
+  __device__ __forceinline__ static double2 ld(const double2* p) { return *p; }
+};
+struct LdCG {
+  __device__ __forceinline__ static double2 ld(const double2* p) { return __ldcg(p); }
+};
+
 // Load the plan header and the table into shared memory (whole CTA).
 __device__ __forceinline__ void load_plan(DevPlan& sP, double2* stab, const DevPlan* __restrict__ gP,
                                           const double2* __restrict__ gtab) {
@@ -34,15 +44,15 @@ __device__ __forceinline__ void load_plan(DevPlan& sP, double2* stab, const DevP
 //     L v + N(F_y, C_v) + N(F_v, C_y)   (the bracket is bilinear in (F, C)).
 // sA, sB: 2*L*Nx double2 of shared memory with L = nt+1 (RHS) or 2*nt+2 (JVP).
 // ------------------------------------------------------------------------
-template <bool JVP, class Epi>
+template <bool JVP, class Epi, class LD = LdPlain>
 __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
-                             const double2* __restrict__ y, const double2* __restrict__ yl,
+                             const double2* y, const double2* yl,
                              int s, int n0, int nt, double2* sA, double2* sB, double* scoef, Epi& epi) {
   const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
-  const double2* __restrict__ lin = JVP ? yl : y;              // source of the linear terms
-  const double2* __restrict__ Cs = y + (size_t)s * Nn * N;
-  const double2* __restrict__ Ls = lin + (size_t)s * Nn * N;
-  const double2* __restrict__ Fk = y + P.nc;
+  const double2* lin = JVP ? yl : y;              // source of the linear terms
+  const double2* Cs = y + (size_t)s * Nn * N;
+  const double2* Ls = lin + (size_t)s * Nn * N;
+  const double2* Fk = y + P.nc;
   const double a0 = P.pb.alpha_s[3 * s];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
   const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
@@ -65,15 +75,15 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
     if (kept(c, N, cut)) {
       if (l < ng) {
         const double2* F = (l == 0 ? y : yl) + P.nc;
-        v = F[c];
-        v = crfma(u1, F[5 * N + c], v);
-        v = crfma(-u2, F[4 * N + c], v);
+        v = LD::ld(F + c);
+        v = crfma(u1, LD::ld(F + 5 * N + c), v);
+        v = crfma(-u2, LD::ld(F + 4 * N + c), v);
       } else {
         const int q = l - ng;                      // 0 .. nt-1 (first set), nt .. 2nt-1 (second)
         const bool second = JVP && q >= nt;
         const int nm1 = n0 + (second ? q - nt : q) - 1;
         const double2* src = (JVP && !second) ? (yl + (size_t)s * Nn * N) : Cs;
-        if (nm1 >= 0) v = src[(size_t)nm1 * N + c];
+        if (nm1 >= 0) v = LD::ld(src + (size_t)nm1 * N + c);
       }
     }
     sA[l * N + std_index(c, N)] = v;
@@ -98,9 +108,9 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
     const double* cf = scoef + 4 * l;
     const double2 kt = ktab(P, tab, 1, c);
     const double w = kt.x * a0;
-    const double2 C0 = Ls[(size_t)n * N + c];
-    const double2 Cp = (n + 1 < Nn) ? Ls[(size_t)(n + 1) * N + c] : make_double2(0.0, 0.0);
-    const double2 Cm = (n >= 1) ? Ls[(size_t)(n - 1) * N + c] : make_double2(0.0, 0.0);
+    const double2 C0 = LD::ld(Ls + (size_t)n * N + c);
+    const double2 Cp = (n + 1 < Nn) ? LD::ld(Ls + (size_t)(n + 1) * N + c) : make_double2(0.0, 0.0);
+    const double2 Cm = (n >= 1) ? LD::ld(Ls + (size_t)(n - 1) * N + c) : make_double2(0.0, 0.0);
     double2 t = cscale(ua, C0);
     t = crfma(cf[0], Cp, t);
     t = crfma(cf[1], Cm, t);
@@ -127,13 +137,13 @@ __device__ __forceinline__ void rhs1v_tile(const DevPlan& P, const double2* __re
 // ------------------------------------------------------------------------
 // Maxwell + current for Fourier points [p0, p1) of the field planes.
 // ------------------------------------------------------------------------
-template <class Epi>
+template <class Epi, class LD = LdPlain>
 __device__ void maxwell_range(const DevPlan& P, const double2* __restrict__ tab,
-                              const double2* __restrict__ y, int p0, int p1, Epi& epi) {
+                              const double2* y, int p0, int p1, Epi& epi) {
   const spx_problem& pb = P.pb;
   const int Nx = P.ax[1].n, Nz = P.ax[2].n;
   const size_t pl = (size_t)P.plane;
-  const double2* __restrict__ F = y + P.nc;
+  const double2* F = y + P.nc;
   const double rs2 = 0.70710678118654752440;
   const double iO = 1.0 / pb.Omega_cs[0];
   for (int pt = p0 + threadIdx.x; pt < p1; pt += blockDim.x) {
@@ -144,16 +154,16 @@ __device__ void maxwell_range(const DevPlan& P, const double2* __restrict__ tab,
       const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
       const double pre = pb.qs[s] * a0 * a1 * a2;
       const size_t b0 = (size_t)s * P.nh * pl + pt;
-      const double2 C000 = y[b0];
-      const double2 C100 = pb.Nn > 1 ? y[b0 + pl] : make_double2(0, 0);
-      const double2 C010 = pb.Nm > 1 ? y[b0 + (size_t)pb.Nn * pl] : make_double2(0, 0);
-      const double2 C001 = pb.Np > 1 ? y[b0 + (size_t)pb.Nn * pb.Nm * pl] : make_double2(0, 0);
+      const double2 C000 = LD::ld(y + b0);
+      const double2 C100 = pb.Nn > 1 ? LD::ld(y + b0 + pl) : make_double2(0, 0);
+      const double2 C010 = pb.Nm > 1 ? LD::ld(y + b0 + (size_t)pb.Nn * pl) : make_double2(0, 0);
+      const double2 C001 = pb.Np > 1 ? LD::ld(y + b0 + (size_t)pb.Nn * pb.Nm * pl) : make_double2(0, 0);
       J0 = crfma(pre, crfma(pb.u_s[3 * s], C000, cscale(a0 * rs2, C100)), J0);
       J1 = crfma(pre, crfma(pb.u_s[3 * s + 1], C000, cscale(a1 * rs2, C010)), J1);
       J2 = crfma(pre, crfma(pb.u_s[3 * s + 2], C000, cscale(a2 * rs2, C001)), J2);
     }
-    const double2 Ex = F[pt], Ey = F[pl + pt], Ez = F[2 * pl + pt];
-    const double2 Bx = F[3 * pl + pt], By = F[4 * pl + pt], Bz = F[5 * pl + pt];
+    const double2 Ex = LD::ld(F + pt), Ey = LD::ld(F + pl + pt), Ez = LD::ld(F + 2 * pl + pt);
+    const double2 Bx = LD::ld(F + 3 * pl + pt), By = LD::ld(F + 4 * pl + pt), Bz = LD::ld(F + 5 * pl + pt);
     const double2 kbx = csub(cscale(Ky, Bz), cscale(Kz, By));
     const double2 kby = csub(cscale(Kz, Bx), cscale(Kx, Bz));
     const double2 kbz = csub(cscale(Kx, By), cscale(Ky, Bx));
