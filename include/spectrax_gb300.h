@@ -124,6 +124,29 @@ int spx_vjp(const spx_plan* plan, const void* y, const void* w, void* g, void* w
 #define SPX_VJP_NOALLOC_MAX_ENTRIES 65536
 int spx_vjp_noalloc(const spx_plan* plan, const void* y, const void* w, void* g, void* stream);
 
+/* ------------------------------------------------------- adjoint building blocks */
+/*
+ * One fixed Prince-Dormand 8(7) step of size h from y (1D1V layout) that keeps
+ * every stage input Ystages[j] (13 x state_len; Ystages[0] = y) and stage
+ * derivative Kstages[j] = f(Ystages[j]) (13 x state_len), and writes
+ * ynext = y + h sum_j b_j K_j.  y may be Ystages itself (no copy then).  The discrete adjoint linearises at the stage
+ * inputs.  (The reference differentiates through diffeqsolve with jax.grad;
+ * this is the device-side replacement of that forward recomputation.)
+ */
+int spx_rk_step_store(const spx_plan* plan, const void* y, double h, void* Ystages, void* Kstages,
+                      void* ynext, void* stream);
+/* out = sum_{i < nterms} coefs[i] * vecs[i] over len complex128 entries
+ * (vecs: host array of device pointers, nterms <= 16; out may alias an input). */
+int spx_lincomb(int64_t len, int32_t nterms, const void* const* vecs, const double* coefs, void* out,
+                void* stream);
+/*
+ * acc[0] += Re sum_e g_e (d f/d nu)_e ; acc[1] += Re sum_e g_e (k d f/d k)_e (the parts
+ * of f linear in the wavenumbers, with L = 2 pi / k) ; acc[2+s] += Re sum_e g_e
+ * (d f / d u_x,s)_e, all at state y (1D1V layout; acc is a device array of
+ * 2 + Ns doubles the caller zeroes).
+ */
+int spx_param_dots(const spx_plan* plan, const void* y, const void* g, double* acc, void* stream);
+
 /* ------------------------------------------------------------------ Dopri8 */
 typedef struct spx_dopri8_opts {
   double t0, t1;     /* integration interval */

@@ -1,0 +1,320 @@
+"""Hand-written discrete adjoint of fixed-step Dopri8, with sqrt(N) checkpointing.
+
+The reference has no adjoint code: gradients would come from ``jax.grad``
+through ``diffeqsolve``.  Here the gradient of a scalar loss of the field-energy
+history is computed exactly for the discrete solution:
+
+* forward: the fused device stepper (``Dopri8Solver``), keeping every
+  m-th state (m = ceil(sqrt(N))) and the field energy of every step;
+* backward, segment by segment in reverse: recompute the segment's steps with
+  ``spx_rk_step_store`` (keeping the 13 stage inputs of each step), then sweep
+  back through the steps with the Runge-Kutta adjoint recursion
+      gk_j = h b_j lam + sum_{i>j} h a_ij gY_i ,   gY_j = J(Y_j)^H gk_j ,
+      lam_n = lam_{n+1} + sum_j gY_j ,
+  using ``spx_vjp`` (plain transpose) on conjugated adjoints:
+  conj(J^H lam) = J^T conj(lam), so every adjoint vector is stored conjugated;
+* parameter gradients accumulate Re sum conj(gk_j) . df/dtheta(Y_j) on the device
+  (``spx_param_dots``) for theta = (nu, k, u_x per species), plus the initial-state
+  terms for k and the perturbation amplitude.
+
+``TwoStreamLoss`` puts this behind ``torch.autograd.Function`` for the adjoint
+workload (1D1V two-stream, loss = LSQ slope of log E over t in [10, 40] plus
+the final field energy; parameters k, nu, u, amplitude).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .dopri8 import Dopri8Solver
+from .params import initialize_simulation_parameters
+from .vector_field import Plan, _stream_ptr, plan_for_params
+
+# Prince-Dormand RK8(7)13M weights (the same published rationals as the device tableau)
+_A = {
+    1: {0: 1 / 18}, 2: {0: 1 / 48, 1: 1 / 16}, 3: {0: 1 / 32, 2: 3 / 32},
+    4: {0: 5 / 16, 2: -75 / 64, 3: 75 / 64}, 5: {0: 3 / 80, 3: 3 / 16, 4: 3 / 20},
+    6: {0: 29443841 / 614563906, 3: 77736538 / 692538347, 4: -28693883 / 1125000000,
+        5: 23124283 / 1800000000},
+    7: {0: 16016141 / 946692911, 3: 61564180 / 158732637, 4: 22789713 / 633445777,
+        5: 545815736 / 2771057229, 6: -180193667 / 1043307555},
+    8: {0: 39632708 / 573591083, 3: -433636366 / 683701615, 4: -421739975 / 2616292301,
+        5: 100302831 / 723423059, 6: 790204164 / 839813087, 7: 800635310 / 3783071287},
+    9: {0: 246121993 / 1340847787, 3: -37695042795 / 15268766246, 4: -309121744 / 1061227803,
+        5: -12992083 / 490766935, 6: 6005943493 / 2108947869, 7: 393006217 / 1396673457,
+        8: 123872331 / 1001029789},
+    10: {0: -1028468189 / 846180014, 3: 8478235783 / 508512852, 4: 1311729495 / 1432422823,
+         5: -10304129995 / 1701304382, 6: -48777925059 / 3047939560, 7: 15336726248 / 1032824649,
+         8: -45442868181 / 3398467696, 9: 3065993473 / 597172653},
+    11: {0: 185892177 / 718116043, 3: -3185094517 / 667107341, 4: -477755414 / 1098053517,
+         5: -703635378 / 230739211, 6: 5731566787 / 1027545527, 7: 5232866602 / 850066563,
+         8: -4093664535 / 808688257, 9: 3962137247 / 1805957418, 10: 65686358 / 487910083},
+    12: {0: 403863854 / 491063109, 3: -5068492393 / 434740067, 4: -411421997 / 543043805,
+         5: 652783627 / 914296604, 6: 11173962825 / 925320556, 7: -13158990841 / 6184727034,
+         8: 3936647629 / 1978049680, 9: -160528059 / 685178525, 10: 248638103 / 1413531060},
+}
+_B = [14005451 / 335480064, 0, 0, 0, 0, -59238493 / 1068277825, 181606767 / 758867731,
+      561292985 / 797845732, -1041891430 / 1371343529, 760417239 / 1151165299,
+      118820643 / 751138087, -528747749 / 2220607170, 1 / 4]
+S = 13
+
+
+def _ptr(t: torch.Tensor):
+    return C.c_void_p(t.data_ptr())
+
+
+def lincomb(out: torch.Tensor, terms):
+    """out = sum c_i v_i on the device (terms: list of (coef, tensor), <= 16)."""
+    terms = [(float(c), v) for c, v in terms if c != 0.0]
+    n = len(terms)
+    vecs = (C.c_void_p * max(1, n))(*[v.data_ptr() for _, v in terms])
+    coefs = (C.c_double * max(1, n))(*[c for c, _ in terms])
+    _lib.check(_lib.lib().spx_lincomb(out.numel(), n, vecs, coefs, _ptr(out), _stream_ptr()), "spx_lincomb")
+    return out
+
+
+class Dopri8Adjoint:
+    """Fixed-step Dopri8 trajectory with its discrete adjoint."""
+
+    def __init__(self, plan: Plan, dt: float, nsteps: int, ckpt_every: int | None = None, masses=None):
+        if plan.problem.Ny != 1 or plan.problem.Nz != 1 or plan.problem.Nm != 1 or plan.problem.Np != 1:
+            raise ValueError("the adjoint is implemented for the 1D1V layout")
+        self.plan, self.dt, self.N = plan, float(dt), int(nsteps)
+        self.m = int(ckpt_every or math.ceil(math.sqrt(self.N)))
+        self.masses = masses
+        self.n = plan.state_len
+        self.nc = self.n - 6 * plan.problem.Nx
+        self.O0 = float(plan.problem.Omega_cs[0])
+        dev = plan.device
+        self.ts = np.arange(self.N + 1) * self.dt
+
+    # ------------------------------------------------------------------ forward
+    def forward(self, y0: torch.Tensor):
+        s = Dopri8Solver(self.plan, 0.0, self.ts[-1], self.dt, ts=self.ts, adaptive=False,
+                         save_states=False, masses=self.masses, max_steps=self.N + 10)
+        s.reset(y0)
+        ckpts = [y0.clone()]
+        done = 0
+        while done < self.N:
+            k = min(self.m, self.N - done)
+            s.advance(k)
+            done += k
+            ckpts.append(s.state())
+        st = s.stats()
+        if st["status"] != 1 or st["accepted"] != self.N:
+            raise RuntimeError(f"forward solve failed: {st}")
+        E = s.energies()[:, 0].clone()
+        self.ckpts = ckpts
+        return E, ckpts[-1]
+
+    # ------------------------------------------------------------------ backward
+    def _buffers(self):
+        if getattr(self, "_buf", None) is None:
+            dev, n, m = self.plan.device, self.n, self.m
+            self._buf = dict(
+                Ys=torch.empty((m + 1, S, n), dtype=torch.complex128, device=dev),
+                Kb=torch.empty((S, n), dtype=torch.complex128, device=dev),
+                gY=torch.empty((S, n), dtype=torch.complex128, device=dev),
+                gk=torch.empty(n, dtype=torch.complex128, device=dev),
+                mu=torch.empty(n, dtype=torch.complex128, device=dev),
+                acc=torch.zeros(2 + self.plan.problem.Ns, dtype=torch.float64, device=dev),
+                coef=torch.zeros(m + 1, dtype=torch.float64, device=dev),
+            )
+            self._graphs = {}
+        return self._buf
+
+    def _recompute(self, steps):
+        """Recompute `steps` steps from Ys[0, 0], keeping the stage inputs Ys[q]."""
+        B = self._buffers()
+        L = _lib.lib()
+        for q in range(steps):
+            _lib.check(L.spx_rk_step_store(self.plan.handle, _ptr(B["Ys"][q, 0]), C.c_double(self.dt),
+                                           _ptr(B["Ys"][q]), _ptr(B["Kb"]), _ptr(B["Ys"][q + 1, 0]),
+                                           _stream_ptr()), "spx_rk_step_store")
+
+    def _sweep(self, steps):
+        """Adjoint sweep back over `steps` steps (stage inputs in Ys), seeding the
+        field-energy gradient coef[q] * Omega0^2 conj(F(y_q)) after each step."""
+        B = self._buffers()
+        L = _lib.lib()
+        ws, wsb = self.plan.ws_ptr()
+        h, nc, c2 = self.dt, self.nc, self.O0 ** 2
+        mu, gY, gk, acc = B["mu"], B["gY"], B["gk"], B["acc"]
+        accp = C.cast(C.c_void_p(acc.data_ptr()), C.POINTER(C.c_double))
+        for q in reversed(range(steps)):
+            Yq = B["Ys"][q]
+            for j in reversed(range(S)):
+                terms = [(h * _B[j], mu)]
+                for i in range(j + 1, S):
+                    aij = _A.get(i, {}).get(j, 0.0)
+                    if aij != 0.0:
+                        terms.append((h * aij, gY[i]))
+                lincomb(gk, terms)
+                _lib.check(L.spx_vjp(self.plan.handle, _ptr(Yq[j]), _ptr(gk), _ptr(gY[j]), ws, wsb,
+                                     _stream_ptr()), "spx_vjp")
+                _lib.check(L.spx_param_dots(self.plan.handle, _ptr(Yq[j]), _ptr(gk), accp, _stream_ptr()),
+                           "spx_param_dots")
+            lincomb(mu, [(1.0, mu)] + [(1.0, gY[j]) for j in range(S)])
+            mu[nc:].add_((B["coef"][q] * c2) * Yq[0, nc:].conj())
+
+    def _run(self, kind, steps, use_graphs):
+        fn = self._recompute if kind == "recompute" else self._sweep
+        if not use_graphs:
+            fn(steps)
+            return
+        key = (kind, steps)
+        g = self._graphs.get(key)
+        if g is None:
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                self.plan.workspace()
+                fn(steps) if kind == "recompute" else None     # warm-up outside capture (recompute is idempotent)
+            torch.cuda.current_stream().wait_stream(s)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                fn(steps)
+            self._graphs[key] = g
+        g.replay()
+
+    def backward(self, dLdE: torch.Tensor, mu_final=None, use_graphs=True):
+        """dLdE: (N+1,) field-energy sensitivities.  Returns (conj of dL/dy0, param dots
+        (2 + Ns): [nu, k d/dk, u_x per species])."""
+        B = self._buffers()
+        dev = self.plan.device
+        dLdE = dLdE.to(dev, torch.float64)
+        mu, acc = B["mu"], B["acc"]
+        if mu_final is None:
+            mu.zero_()
+        else:
+            mu.copy_(mu_final)
+        acc.zero_()
+        c2 = self.O0 ** 2
+        mu[self.nc:].add_((dLdE[self.N] * c2) * self.ckpts[-1][self.nc:].conj())
+        m = self.m
+        starts = list(range(0, self.N, m))
+        for g in reversed(range(len(starts))):
+            a = starts[g]
+            b = min(a + m, self.N)
+            B["Ys"][0, 0].copy_(self.ckpts[g])
+            B["coef"][: b - a].copy_(dLdE[a:b])
+            self._run("recompute", b - a, use_graphs)
+            self._run("sweep", b - a, use_graphs)
+        return mu.clone(), acc.clone()
+
+
+# ----------------------------------------------------------------- two-stream workload
+def two_stream_setup(k=0.2, nu=1.0, u=0.5, amp=1e-3, Nx=65, Nn=128, alpha=0.5, mi_me=1836.0, seed=0):
+    """Parameters and initial state of the adjoint workload.
+
+    Three species: beams at +-u (half density each, thermal alpha) and ions;
+    perturbation of amplitude `amp` with seeded random phases on modes 1..8,
+    the field from Gauss's law (i K E_x = rho / Omega_0).
+    Returns (params, bg, delta, ddelta_dk) with y0 = bg + amp * delta.
+    """
+    ai = alpha * np.sqrt(1.0 / mi_me)
+    user = dict(Lx=2 * np.pi / k, nu=nu, D=0.0, qs=[-1.0, -1.0, 1.0], alpha_s=[alpha] * 6 + [ai] * 3,
+                u_s=[u, 0, 0, -u, 0, 0, 0, 0, 0], Omega_cs=[1.0, 1.0, 1.0 / mi_me], mi_me=mi_me,
+                ms=[1.0, 1.0, mi_me])
+    p = initialize_simulation_parameters(user, Nx, 1, 1, Nn, 1, 1, 3, 2, 0.05)
+    rng = np.random.default_rng(seed)
+    c0 = Nx // 2
+    Ns = 3
+    dens = [0.5, 0.5, 1.0]
+    a = np.asarray(p["alpha_s"]).reshape(Ns, 3)
+    bg = np.zeros((Ns, Nn, Nx), np.complex128)
+    dC = np.zeros((Ns, Nn, Nx), np.complex128)
+    for s in range(Ns):
+        bg[s, 0, c0] = dens[s] / a[s, 0] ** 3
+    for j in range(1, min(8, (Nx - 1) // 2) + 1):
+        ph = np.exp(2j * np.pi * rng.random())
+        for s in (0, 1):
+            dC[s, 0, c0 + j] = 0.5 * bg[s, 0, c0] * ph
+            dC[s, 0, c0 - j] = np.conj(dC[s, 0, c0 + j])
+    rho = sum(p["qs"][s] * a[s].prod() * dC[s, 0] for s in range(Ns))
+    K = p["kx_grid"][0, :, 0] / p["Lx"]
+    nz = np.abs(K) > 0
+    dF = np.zeros((6, Nx), np.complex128)
+    dF[0, nz] = -1j * rho[nz] / (K[nz] * p["Omega_cs"][0])
+    dFdk = np.zeros_like(dF)
+    dFdk[0] = -dF[0] / k                      # K = j k  =>  E ~ 1/k
+    bgv = np.concatenate([bg.ravel(), np.zeros(6 * Nx, np.complex128)])
+    delta = np.concatenate([dC.ravel(), dF.ravel()])
+    ddk = np.concatenate([np.zeros(dC.size, np.complex128), dFdk.ravel()])
+    return p, bgv, delta, ddk
+
+
+def window_weights(ts, ta=10.0, tb=40.0):
+    """w with slope = sum w_i log E_i for the least-squares line over [ta, tb]."""
+    ts = np.asarray(ts, np.float64)
+    sel = (ts >= ta - 1e-12) & (ts <= tb + 1e-12)
+    tt = ts[sel]
+    w = np.zeros_like(ts)
+    w[sel] = (tt - tt.mean()) / np.sum((tt - tt.mean()) ** 2)
+    return w
+
+
+def loss_from_energy(E, w):
+    E = np.asarray(E, np.float64)
+    return float(np.sum(w * np.log(E)) + E[-1])
+
+
+class TwoStreamProblem:
+    """Forward loss and adjoint gradients of the two-stream adjoint workload."""
+
+    def __init__(self, Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0, ckpt_every=None, window=(10.0, 40.0)):
+        self.Nx, self.Nn, self.dt, self.N, self.seed = Nx, Nn, dt, nsteps, seed
+        self.ckpt_every = ckpt_every
+        self.window = window
+
+    def _build(self, k, nu, u, amp):
+        p, bg, delta, ddk = two_stream_setup(k, nu, u, amp, self.Nx, self.Nn, seed=self.seed)
+        plan = plan_for_params(p, "divide")
+        adj = Dopri8Adjoint(plan, self.dt, self.N, self.ckpt_every, masses=[1.0, 1.0, 1836.0])
+        y0 = torch.from_numpy(bg + amp * delta).to(plan.device)
+        return p, plan, adj, y0, delta, ddk
+
+    def loss(self, k, nu, u, amp):
+        p, plan, adj, y0, _, _ = self._build(k, nu, u, amp)
+        E, _ = adj.forward(y0)
+        w = window_weights(adj.ts, *self.window)
+        return loss_from_energy(E.cpu().numpy(), w)
+
+    def loss_and_grad(self, k, nu, u, amp):
+        p, plan, adj, y0, delta, ddk = self._build(k, nu, u, amp)
+        E, _ = adj.forward(y0)
+        En = E.cpu().numpy()
+        w = window_weights(adj.ts, *self.window)
+        L = loss_from_energy(En, w)
+        dLdE = w / En
+        dLdE[-1] += 1.0
+        mu0, acc = adj.backward(torch.from_numpy(dLdE))
+        mu0 = mu0.cpu().numpy()
+        acc = acc.cpu().numpy()
+        # mu0 = conj(dL/dy0): Re sum mu0 * dy0/dtheta is the directional derivative
+        g_amp = float(np.real(np.sum(mu0 * delta)))
+        g_k = float(acc[1] / k + np.real(np.sum(mu0 * amp * ddk)))
+        g_nu = float(acc[0])
+        g_u = float(acc[2] - acc[3])           # beams at +u and -u
+        return L, dict(k=g_k, nu=g_nu, u=g_u, amp=g_amp)
+
+
+class TwoStreamLoss(torch.autograd.Function):
+    """loss(k, nu, u, amp) with the hand-written discrete adjoint as its backward."""
+
+    @staticmethod
+    def forward(ctx, k, nu, u, amp, problem: TwoStreamProblem):
+        vals = [float(x) for x in (k, nu, u, amp)]
+        L, g = problem.loss_and_grad(*vals)
+        ctx.save_for_backward(torch.tensor([g["k"], g["nu"], g["u"], g["amp"]], dtype=torch.float64))
+        return torch.tensor(L, dtype=torch.float64)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (g,) = ctx.saved_tensors
+        g = g * gout
+        return g[0], g[1], g[2], g[3], None

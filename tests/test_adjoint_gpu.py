@@ -1,0 +1,70 @@
+"""GPU: the discrete adjoint of fixed-step Dopri8 against central finite differences (h = 1e-6)."""
+import numpy as np
+import pytest
+
+FD_H = 1e-6
+
+
+def _problem(nsteps=60, ckpt=None):
+    from spectrax_gb300.adjoint import TwoStreamProblem
+    # a small two-stream case; loss window shrunk to the short horizon
+    return TwoStreamProblem(Nx=17, Nn=16, dt=0.05, nsteps=nsteps, seed=3, ckpt_every=ckpt, window=(0.5, 2.0))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ckpt", [None, 7, 1000])
+def test_parameter_gradients_match_central_differences(ckpt):
+    prob = _problem(ckpt=ckpt)
+    theta = dict(k=0.35, nu=1.0, u=0.5, amp=1e-3)
+    L, g = prob.loss_and_grad(**theta)
+    for name in ("k", "nu", "u", "amp"):
+        tp, tm = dict(theta), dict(theta)
+        tp[name] += FD_H
+        tm[name] -= FD_H
+        fd = (prob.loss(**tp) - prob.loss(**tm)) / (2 * FD_H)
+        assert abs(g[name] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(L)), (name, g[name], fd)
+
+
+@pytest.mark.gpu
+def test_initial_state_gradient_direction():
+    import torch
+    from spectrax_gb300.adjoint import Dopri8Adjoint, two_stream_setup, window_weights, loss_from_energy
+    from spectrax_gb300.vector_field import plan_for_params
+    p, bg, delta, _ = two_stream_setup(0.3, 1.0, 0.5, 1e-3, 9, 10, seed=1)
+    plan = plan_for_params(p, "divide")
+    adj = Dopri8Adjoint(plan, 0.05, 30, 5)
+    y0 = bg + 1e-3 * delta
+    w = window_weights(adj.ts, 0.3, 1.2)
+
+    def loss(y):
+        E, _ = adj.forward(torch.from_numpy(y).cuda())
+        return loss_from_energy(E.cpu().numpy(), w)
+
+    E, _ = adj.forward(torch.from_numpy(y0).cuda())
+    En = E.cpu().numpy()
+    dLdE = w / En
+    dLdE[-1] += 1.0
+    mu0, _ = adj.backward(torch.from_numpy(dLdE))
+    mu0 = mu0.cpu().numpy()
+    rng = np.random.default_rng(0)
+    for _ in range(2):
+        v = 1e-3 * (rng.standard_normal(len(y0)) + 1j * rng.standard_normal(len(y0)))
+        fd = (loss(y0 + FD_H * v) - loss(y0 - FD_H * v)) / (2 * FD_H)
+        ad = float(np.real(np.sum(mu0 * v)))
+        assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-12, (ad, fd)
+
+
+@pytest.mark.gpu
+def test_autograd_function_wiring():
+    import torch
+    from spectrax_gb300.adjoint import TwoStreamLoss
+    prob = _problem(nsteps=20)
+    k = torch.tensor(0.35, dtype=torch.float64, requires_grad=True)
+    nu = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    u = torch.tensor(0.5, dtype=torch.float64, requires_grad=True)
+    amp = torch.tensor(1e-3, dtype=torch.float64, requires_grad=True)
+    L = TwoStreamLoss.apply(k, nu, u, amp, prob)
+    L.backward()
+    _, g = prob.loss_and_grad(0.35, 1.0, 0.5, 1e-3)
+    assert abs(k.grad.item() - g["k"]) <= 1e-12 * abs(g["k"])
+    assert abs(amp.grad.item() - g["amp"]) <= 1e-12 * abs(g["amp"])
