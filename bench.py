@@ -189,6 +189,69 @@ def cpu_sample(p, y0, seconds=10.0, workers=None):
     return n / dt, n
 
 
+def run_extras(args):
+    """Secondary measurements of the same build: the batched damping-rate scan
+    against serial solves, and the adjoint gradient against one forward solve."""
+    import torch
+    out = {}
+    try:
+        from spectrax_gb300.batch import BatchSolver, autotune, landau_scan, serial_solve
+        insts = landau_scan(256, seed=0)
+        probs = [it["problem"] for it in insts]
+        y0s = [it["y0"] for it in insts]
+        ms = [it["masses"] for it in insts]
+        t1 = args.scan_t1
+        ts = np.linspace(0.0, t1, 41)
+        best = autotune(probs, y0s, t1_probe=0.2, masses=ms)
+        b = BatchSolver(probs, t1, rtol=1e-8, atol=1e-8, save_ts=ts, cluster=best["cluster"], tile=best["tile"],
+                        masses=ms)
+        y0 = b.pack(y0s)
+        b.run(y0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        yb = b.run(y0)
+        e1.record()
+        torch.cuda.synchronize()
+        tb = e0.elapsed_time(e1) * 1e-3
+        stats, ens = b.results()
+        fy, fst, fen, ts_serial = serial_solve(insts, t1, rtol=1e-8, atol=1e-8, save_ts=ts)
+        ys = b.unpack(yb)
+        err = max(float(np.linalg.norm(ys[i] - fy[i]) / np.linalg.norm(fy[i])) for i in range(len(insts)))
+        eerr = max(float(np.max(np.abs(ens[i][:, 0] - fen[i][:, 0]) / np.abs(fen[i][:, 0])))
+                   for i in range(len(insts)))
+        out["batch_scan"] = {
+            "instances": len(insts), "t1": t1, "batched_s": tb, "serial_s": ts_serial,
+            "speedup": ts_serial / tb, "rhs_evals": int(sum(s["rhs_evals"] for s in stats)),
+            "rhs_evals_per_s": sum(s["rhs_evals"] for s in stats) / tb,
+            "cluster": best["cluster"], "tile": best["tile"],
+            "max_rel_err_state_vs_serial": err, "max_rel_err_field_energy_vs_serial": eerr,
+            "note": "per-instance adaptive Dopri8 (rtol=atol=1e-8); serial = the same instances one by "
+                    "one through the graph-captured single-instance solver"}
+    except Exception as e:  # keep the main line even if an extra fails
+        out["batch_scan"] = {"error": repr(e)}
+    try:
+        from spectrax_gb300.adjoint import TwoStreamProblem
+        prob = TwoStreamProblem(Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0)
+        th = dict(k=0.2, nu=1.0, u=0.5, amp=1e-3)
+        prob.loss(**th)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prob.loss(**th)
+        torch.cuda.synchronize()
+        tf = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        L, g = prob.loss_and_grad(**th)
+        torch.cuda.synchronize()
+        tg = time.perf_counter() - t0
+        out["adjoint"] = {"workload": "two-stream Nx=65 Nn=128 Ns=3, 2000 fixed Dopri8 steps dt=0.05",
+                          "forward_s": tf, "loss_and_gradient_s": tg, "cost_ratio": tg / tf,
+                          "loss": L, "gradient": g, "checkpoints": "every ceil(sqrt(2000)) = 45 steps"}
+    except Exception as e:
+        out["adjoint"] = {"error": repr(e)}
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -288,17 +351,12 @@ def run_ours(args):
         torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_evals = 13 * args.steps
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_ms, e2e_s, float(evals), float(e2e_evals)], dtype=torch.float64, device="cuda")
-        mx = tt.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = tt.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        t_ms, e2e_s = float(mx[0]), float(mx[1])
-        evals_all, e2e_evals_all = float(sm[2]), float(sm[3])
-    else:
-        evals_all, e2e_evals_all = float(evals), float(e2e_evals)
+    from spectrax_gb300.distributed import reduce_timing
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t_ms, evals_all = reduce_timing(t_ms, float(evals), device=dev)          # max time, summed work
+    e2e_s, e2e_evals_all = reduce_timing(e2e_s, float(e2e_evals), device=dev)
+    acc_all = reduce_timing(0.0, float(acc), device=dev)[1]
+    extras = run_extras(args) if (world == 1 and args.extras) else None
     if rank != 0:
         return 0
     value = evals_all / (t_ms * 1e-3)
@@ -324,7 +382,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "step": "one Dopri8 step attempt (13 fused RHS stages + controller)",
                    "state_len": n, "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "accepted_steps_per_s": (acc * world) / (t_ms * 1e-3),
+        "accepted_steps_per_s": acc_all / (t_ms * 1e-3),
         "e2e": {"value": e2e_evals_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
         "gpu_launches": args.steps * 14,
@@ -342,6 +400,8 @@ def run_ours(args):
         line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{cpu_n} oracle RHS evaluations of the same state "
                                           f"(~{args.cpu_seconds:.0f} s, scipy.fft with all host threads)"}
+    if extras is not None:
+        line["extras"] = extras
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -352,10 +412,12 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--extras", type=int, default=1, help="also time the batched scan and the adjoint")
+    ap.add_argument("--scan-t1", type=float, default=4.0, help="horizon of the batched scan extra")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
