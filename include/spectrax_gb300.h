@@ -75,7 +75,13 @@ const char* spx_version(void);
  * spectrax/_initialization.py:114-154.
  */
 int spx_plan_create(const spx_problem* pb, spx_plan** out);
+/* Same, with the launch shape fixed: `tile` Hermite planes per CTA on the 1D1V
+ * path (1..16, 0 = automatic) and `threads` per CTA (multiple of 32 up to 256,
+ * 0 = 256).  Used by the autotuner. */
+int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx_plan** out);
 int spx_plan_destroy(spx_plan* plan);
+/* Launch shape chosen for a plan (any pointer may be NULL); path 0 = fused 1D1V, 1 = general. */
+int spx_plan_info(const spx_plan* plan, int32_t* tile, int32_t* ntiles, int32_t* threads, int32_t* path);
 
 /* Number of complex128 entries of the flat state (N_C + N_F). */
 int64_t spx_state_len(const spx_problem* pb);

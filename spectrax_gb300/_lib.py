@@ -88,7 +88,10 @@ _PROTOS = {
     "spx_last_error": (C.c_char_p, []),
     "spx_version": (C.c_char_p, []),
     "spx_plan_create": (C.c_int, [C.POINTER(spx_problem), C.POINTER(_VP)]),
+    "spx_plan_create_ex": (C.c_int, [C.POINTER(spx_problem), C.c_int32, C.c_int32, C.POINTER(_VP)]),
     "spx_plan_destroy": (C.c_int, [_VP]),
+    "spx_plan_info": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32)]),
     "spx_state_len": (C.c_int64, [C.POINTER(spx_problem)]),
     "spx_rhs_workspace_bytes": (C.c_size_t, [_VP]),
     "spx_rhs": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP]),

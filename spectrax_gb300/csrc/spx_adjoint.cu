@@ -216,7 +216,7 @@ int spx_rk_step_store(const spx_plan* pl, const void* y, double h, void* Ystages
   if (static_cast<const void*>(Yb) != y)
     SPX_CUDA(cudaMemcpyAsync(Yb, y, sizeof(double2) * len, cudaMemcpyDeviceToDevice, st));
   for (int stage = 0; stage < rk::S; ++stage)
-    k_rk_stage_1v<<<P.pb.Ns * P.ntiles + 1, NTHREADS, pl->smem_1v, st>>>(
+    k_rk_stage_1v<<<P.pb.Ns * P.ntiles + 1, pl->threads, pl->smem_1v, st>>>(
         pl->d_plan, pl->d_tab, static_cast<const double2*>(y), Yb, static_cast<double2*>(Kstages),
         static_cast<double2*>(ynext), h, stage);
   SPX_CUDA(cudaGetLastError());

@@ -97,6 +97,17 @@ template <bool INV> struct Dft<2, INV> {
     v[0] = cadd(a, b); v[1] = csub(a, b);
   }
 };
+// X1,2 = x0 - (x1+x2)/2 -+ i (sqrt3/2)(x1-x2) (forward; the inverse swaps the signs)
+template <bool INV> struct Dft<3, INV> {
+  __device__ __forceinline__ static void run(double2* v) {
+    const double c = INV ? -0.86602540378443864676 : 0.86602540378443864676;
+    const double2 t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+    const double2 m = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
+    v[0] = cadd(v[0], t1);
+    v[1] = make_double2(fma(c, t2.y, m.x), fma(-c, t2.x, m.y));
+    v[2] = make_double2(fma(-c, t2.y, m.x), fma(c, t2.x, m.y));
+  }
+};
 template <bool INV> struct Dft<4, INV> {
   __device__ __forceinline__ static void run(double2* v) {
     double2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
@@ -129,11 +140,19 @@ template <bool INV> struct Dft<8, INV> {
   }
 };
 
-// One Stockham stage with an even radix R in registers.
+// Largest pair index q of butterfly j whose inputs (first decimation-in-time
+// stage) or outputs (last decimation-in-frequency stage) can be non-zero /
+// are needed, when only standard indices <= cut or >= n - cut matter.
+__device__ __forceinline__ int pair_limit(int j, int M, int h, int cut) {
+  const int q = (cut + j) / M;
+  return q < h ? q : h;
+}
+
+// ---- decimation in time (Stockham): gather stride M, twiddle, DFT, scatter
+// to (j/Ns)*Ns*R + k + r*Ns.
 template <int R, bool INV>
-__device__ __forceinline__ void stage_even(const double2* __restrict__ in, double2* __restrict__ out,
-                                           int n, int Ns, const double2* __restrict__ tw,
-                                           const Lines& L) {
+__device__ __forceinline__ void stage_reg_dit(const double2* __restrict__ in, double2* __restrict__ out,
+                                              int n, int Ns, const double2* __restrict__ tw, const Lines& L) {
   const int M = n / R;
   const int ntask = L.nl * M;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
@@ -155,13 +174,45 @@ __device__ __forceinline__ void stage_even(const double2* __restrict__ in, doubl
   }
 }
 
-// One Stockham stage with an odd radix R (any R >= 3), two phases.
-// Phase 1, in place on `in`: apply twiddles and replace the pair (x_q, x_{R-q})
-// by (x_q + x_{R-q}, x_q - x_{R-q}).  Phase 2: one task per output pair (k, R-k).
-template <bool INV>
+// ---- decimation in frequency: the transpose of the stage above (gather from
+// the DIT output positions, DFT, twiddle the outputs, scatter with stride M).
+template <int R, bool INV>
+__device__ __forceinline__ void stage_reg_dif(const double2* __restrict__ in, double2* __restrict__ out,
+                                              int n, int Ns, const double2* __restrict__ tw, const Lines& L) {
+  const int M = n / R;
+  const int ntask = L.nl * M;
+  for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+    const int l = t / M, j = t - l * M;
+    const int b = L.base(l);
+    const int k = j % Ns;
+    const int idx = (j / Ns) * Ns * R + k;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[b + (idx + r * Ns) * L.es];
+    Dft<R, INV>::run(v);
+    if (Ns > 1 && k > 0) {
+      const double2* w = tw + k * (R - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = twiddle<INV>(v[r], w[r - 1]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[b + (j + r * M) * L.es] = v[r];
+  }
+}
+
+// Odd radix R (any R >= 3), two phases.  Phase 1, in place on `in`: replace
+// each pair (x_q, x_{R-q}) by (x_q + x_{R-q}, x_q - x_{R-q}) (with the
+// decimation-in-time twiddles applied first).  Phase 2: one task per output
+// pair (kk, R-kk): X = x_0 + sum_q a_q cos -+ i sum_q b_q sin.
+// DIF = false: gather stride M, scatter to the DIT positions; `pcut` >= 0 on
+//              the first stage skips input pairs that are zero.
+// DIF = true : gather from the DIT positions, twiddle the outputs, scatter
+//              with stride M; `pcut` >= 0 on the last stage skips output pairs
+//              that are not needed.
+template <bool INV, bool DIF>
 __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __restrict__ out, int n,
                                           int R, int Ns, const double2* __restrict__ tw,
-                                          const double2* __restrict__ cs, const Lines& L) {
+                                          const double2* __restrict__ cs, const Lines& L, int pcut) {
   const int M = n / R;
   const int h = (R - 1) >> 1;
   {
@@ -170,11 +221,20 @@ __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __r
       const int q = t % h + 1;
       const int lj = t / h;
       const int l = lj / M, j = lj - l * M;
+      if (!DIF && pcut >= 0 && q > pair_limit(j, M, h, pcut)) continue;
       const int b = L.base(l);
-      const int i1 = b + (j + q * M) * L.es, i2 = b + (j + (R - q) * M) * L.es;
-      double2 x1 = in[i1], x2 = in[i2];
       const int k = j % Ns;
-      if (Ns > 1 && k > 0) {
+      int i1, i2;
+      if (!DIF) {
+        i1 = b + (j + q * M) * L.es;
+        i2 = b + (j + (R - q) * M) * L.es;
+      } else {
+        const int idx = (j / Ns) * Ns * R + k;
+        i1 = b + (idx + q * Ns) * L.es;
+        i2 = b + (idx + (R - q) * Ns) * L.es;
+      }
+      double2 x1 = in[i1], x2 = in[i2];
+      if (!DIF && Ns > 1 && k > 0) {
         const double2* w = tw + k * (R - 1);
         x1 = twiddle<INV>(x1, w[q - 1]);
         x2 = twiddle<INV>(x2, w[R - q - 1]);
@@ -185,47 +245,83 @@ __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __r
   }
   __syncthreads();
   {
-    const int ntask = L.nl * M * (h + 1);
+    // task list: per butterfly j the output pairs kk = 0 .. kmax(j)
+    const bool prune_out = DIF && pcut >= 0;
+    int per_line = M * (h + 1);
+    if (prune_out) {
+      per_line = 0;
+      for (int j = 0; j < M; ++j) per_line += pair_limit(j, M, h, pcut) + 1;
+    }
+    const int ntask = L.nl * per_line;
     for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
-      const int kk = t % (h + 1);
-      const int lj = t / (h + 1);
-      const int l = lj / M, j = lj - l * M;
+      const int l = t / per_line;
+      int r = t - l * per_line;
+      int j, kk;
+      if (!prune_out) {
+        j = r / (h + 1);
+        kk = r - j * (h + 1);
+      } else {
+        j = 0;
+        int c = pair_limit(0, M, h, pcut) + 1;
+        while (r >= c) { r -= c; ++j; c = pair_limit(j, M, h, pcut) + 1; }
+        kk = r;
+      }
       const int b = L.base(l);
-      double2 A = in[b + j * L.es];
+      const int k = j % Ns;
+      const int idx = (j / Ns) * Ns * R + k;
+      const int qmax = (!DIF && pcut >= 0) ? pair_limit(j, M, h, pcut) : h;
+      const int s0 = DIF ? Ns : M;                    // input stride between q's
+      const int i0 = DIF ? idx : j;                   // input position of q = 0
+      double2 A = in[b + i0 * L.es];
       double2 B = make_double2(0.0, 0.0);
       int ang = 0;   // (q * kk) mod R
-      for (int q = 1; q <= h; ++q) {
+      for (int q = 1; q <= qmax; ++q) {
         ang += kk;
         if (ang >= R) ang -= R;
         const double2 cq = cs[ang];
-        const double2 aq = in[b + (j + q * M) * L.es];
-        const double2 bq = in[b + (j + (R - q) * M) * L.es];
+        const double2 aq = in[b + (i0 + q * s0) * L.es];
+        const double2 bq = in[b + (i0 + (R - q) * s0) * L.es];
         A = crfma(cq.x, aq, A);
         B = crfma(cq.y, bq, B);
       }
-      const int k = j % Ns;
-      const int idx = (j / Ns) * Ns * R + k;
-      // forward: X_k = A - iB, X_{R-k} = A + iB ; inverse: signs swapped
+      // forward: X_kk = A - iB, X_{R-kk} = A + iB ; inverse: signs swapped
       const double2 iB = INV ? make_double2(-B.y, B.x) : make_double2(B.y, -B.x);
-      out[b + (idx + kk * Ns) * L.es] = cadd(A, iB);
-      if (kk > 0) out[b + (idx + (R - kk) * Ns) * L.es] = csub(A, iB);
+      double2 X1 = cadd(A, iB), X2 = csub(A, iB);
+      if (!DIF) {
+        out[b + (idx + kk * Ns) * L.es] = X1;
+        if (kk > 0) out[b + (idx + (R - kk) * Ns) * L.es] = X2;
+      } else {
+        if (Ns > 1 && k > 0 && kk > 0) {
+          const double2* w = tw + k * (R - 1);
+          X1 = twiddle<INV>(X1, w[kk - 1]);
+          X2 = twiddle<INV>(X2, w[R - kk - 1]);
+        }
+        out[b + (j + kk * M) * L.es] = X1;
+        if (kk > 0) out[b + (j + (R - kk) * M) * L.es] = X2;
+      }
     }
   }
 }
 
-// Transform all lines along one axis.  Returns the buffer holding the result
-// (either a or b); both buffers share the line layout.
-template <bool INV>
-__device__ double2* fft_axis(double2* a, double2* b, const AxisPlan& ap, const double2* tab,
-                             const Lines& L) {
-  for (int st = 0; st < ap.nst; ++st) {
+// Transform all lines along one axis.  DIF = false runs the stages in order
+// (decimation in time), DIF = true runs their transposes in reverse order
+// (decimation in frequency).  pcut >= 0 prunes the first DIT stage's zero
+// inputs or the last DIF stage's unneeded outputs (standard indices beyond
+// +-pcut).  Returns the buffer holding the result (a or b).
+template <bool INV, bool DIF>
+__device__ double2* fft_axis_t(double2* a, double2* b, const AxisPlan& ap, const double2* tab,
+                               const Lines& L, int pcut) {
+  for (int i = 0; i < ap.nst; ++i) {
+    const int st = DIF ? ap.nst - 1 - i : i;
     const int R = ap.radix[st], Ns = ap.span[st];
     const double2* tw = ap.tw[st] >= 0 ? tab + ap.tw[st] : nullptr;
+    const int pc = (st == 0) ? pcut : -1;
     switch (R) {
-      case 2: stage_even<2, INV>(a, b, ap.n, Ns, tw, L); break;
-      case 4: stage_even<4, INV>(a, b, ap.n, Ns, tw, L); break;
-      case 8: stage_even<8, INV>(a, b, ap.n, Ns, tw, L); break;
-      default: stage_odd<INV>(a, b, ap.n, R, Ns, tw, tab + ap.cs[st], L); break;
+      case 2: DIF ? stage_reg_dif<2, INV>(a, b, ap.n, Ns, tw, L) : stage_reg_dit<2, INV>(a, b, ap.n, Ns, tw, L); break;
+      case 3: DIF ? stage_reg_dif<3, INV>(a, b, ap.n, Ns, tw, L) : stage_reg_dit<3, INV>(a, b, ap.n, Ns, tw, L); break;
+      case 4: DIF ? stage_reg_dif<4, INV>(a, b, ap.n, Ns, tw, L) : stage_reg_dit<4, INV>(a, b, ap.n, Ns, tw, L); break;
+      case 8: DIF ? stage_reg_dif<8, INV>(a, b, ap.n, Ns, tw, L) : stage_reg_dit<8, INV>(a, b, ap.n, Ns, tw, L); break;
+      default: stage_odd<INV, DIF>(a, b, ap.n, R, Ns, tw, tab + ap.cs[st], L, pc); break;
     }
     __syncthreads();
     double2* t = a; a = b; b = t;
@@ -233,26 +329,33 @@ __device__ double2* fft_axis(double2* a, double2* b, const AxisPlan& ap, const d
   return a;
 }
 
+// Unpruned decimation-in-time transform (kept for callers without a mask).
+template <bool INV>
+__device__ __forceinline__ double2* fft_axis(double2* a, double2* b, const AxisPlan& ap, const double2* tab,
+                                             const Lines& L) {
+  return fft_axis_t<INV, false>(a, b, ap, tab, L, -1);
+}
+
 // 3-D transform of `np` contiguous planes of shape (Ny, Nx, Nz) (element
 // (y*Nx + x)*Nz + z of plane p at p*Ny*Nx*Nz) held in buffer a; b is the
-// ping-pong partner.  Returns the buffer holding the result.
-template <bool INV>
-__device__ double2* fft_planes(double2* a, double2* b, const DevPlan& P, const double2* tab,
-                               int np) {
+// ping-pong partner.  DIF = false: masked input (zero beyond each axis' cut),
+// DIF = true: only the masked outputs are needed.  Returns the result buffer.
+template <bool INV, bool DIF>
+__device__ double2* fft_planes_t(double2* a, double2* b, const DevPlan& P, const double2* tab, int np) {
   const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
   if (Nz > 1) {   // z-lines, l = (p*Ny + y)*Nx + x, base = l*Nz
     Lines L{np * Ny * Nx, 1, 1, Nz, 0};
-    double2* r = fft_axis<INV>(a, b, P.ax[2], tab, L);
+    double2* r = fft_axis_t<INV, DIF>(a, b, P.ax[2], tab, L, P.ax[2].cut);
     if (r != a) { b = a; a = r; }
   }
   if (Nx > 1) {   // x-lines, l = (p*Ny + y)*Nz + z, base = (l/Nz)*Nx*Nz + l%Nz
     Lines L{np * Ny * Nz, Nz, Nz, Nx * Nz, 1};
-    double2* r = fft_axis<INV>(a, b, P.ax[1], tab, L);
+    double2* r = fft_axis_t<INV, DIF>(a, b, P.ax[1], tab, L, P.ax[1].cut);
     if (r != a) { b = a; a = r; }
   }
   if (Ny > 1) {   // y-lines, l = p*Nx*Nz + x*Nz + z, base = p*plane + l%(Nx*Nz)
     Lines L{np * Nx * Nz, Nx * Nz, Nx * Nz, P.plane, 1};
-    double2* r = fft_axis<INV>(a, b, P.ax[0], tab, L);
+    double2* r = fft_axis_t<INV, DIF>(a, b, P.ax[0], tab, L, P.ax[0].cut);
     if (r != a) { b = a; a = r; }
   }
   return a;

@@ -447,10 +447,10 @@ static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;
   for (int stage = 0; stage < rk::S; ++stage) {
     if (P.path == 0) {
-      k_d8_stage_1v<<<s->grid_stage, NTHREADS, s->plan->smem_1v, st>>>(s->args, stage);
+      k_d8_stage_1v<<<s->grid_stage, s->plan->threads, s->plan->smem_1v, st>>>(s->args, stage);
     } else {
-      k_d8_real<<<s->grid_real, NTHREADS, s->plan->smem_gen, st>>>(s->args, stage);
-      k_d8_stage_gen<<<s->grid_stage, NTHREADS, s->plan->smem_gen, st>>>(s->args, stage);
+      k_d8_real<<<s->grid_real, s->plan->threads, s->plan->smem_gen, st>>>(s->args, stage);
+      k_d8_stage_gen<<<s->grid_stage, s->plan->threads, s->plan->smem_gen, st>>>(s->args, stage);
     }
   }
   k_d8_save<<<s->plan->nsm, NTHREADS, 0, st>>>(s->args);

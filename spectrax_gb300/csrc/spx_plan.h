@@ -16,13 +16,14 @@ struct spx_plan {
   size_t smem_1v = 0;           // dynamic smem of the fused 1D1V kernel
   size_t smem_gen = 0;          // dynamic smem of the general kernels
   size_t ws_bytes = 0;          // scratch of spx_rhs
+  int threads = 256;            // CTA width of the right-hand-side kernels (<= 256)
 };
 
 namespace spx {
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 // Fill `pl` (everything but the device pointers) from a problem; returns SPX_OK or an error code.
-int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl);
+int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile = 0);
 // Launch helpers used by several entry points.
 int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, cudaStream_t st);
 // Opt-in shared memory per block of the current device (0 on failure).

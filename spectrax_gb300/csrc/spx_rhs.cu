@@ -98,7 +98,7 @@ static int build_axis(int n, int cut, double L, std::vector<double2>& tab, AxisP
   return SPX_OK;
 }
 
-int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl) {
+int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
   if (!pb) { set_error("null problem"); return SPX_E_ARG; }
   const spx_problem& p = *pb;
   if (p.Nx < 1 || p.Ny < 1 || p.Nz < 1 || p.Nn < 1 || p.Nm < 1 || p.Np < 1 || p.Ns < 1) {
@@ -134,7 +134,7 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl) {
     P.path = 0;
     const int N = p.Nx;
     const long long planes = (long long)p.Ns * p.Nn;
-    int T = (int)((planes + pl->nsm - 1) / pl->nsm);
+    int T = tile > 0 ? tile : (int)((planes + pl->nsm - 1) / pl->nsm);
     T = std::max(1, std::min(T, 16));
     // shared memory of the widest user (the JVP): 2*(2T+2)*N double2 + table
     while (T > 1 && pl->smem_tab + 2 * (size_t)(2 * T + 2) * N * sizeof(double2) > smem_max) --T;
@@ -371,11 +371,11 @@ int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, c
   const DevPlan& P = pl->host;
   if (P.path == 0) {
     const int grid = P.pb.Ns * P.ntiles + 1;
-    k_rhs1v<<<grid, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, y, dy);
+    k_rhs1v<<<grid, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, y, dy);
   } else {
     const int nplanes = P.pb.Ns * P.nh;
-    k_gen_real<<<nplanes + 3 * P.pb.Ns + 3, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws);
-    k_gen_nl<<<nplanes + 1, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws, dy);
+    k_gen_real<<<nplanes + 3 * P.pb.Ns + 3, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws);
+    k_gen_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws, dy);
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
@@ -398,16 +398,23 @@ int64_t spx_state_len(const spx_problem* pb) {
   return (int64_t)pb->Ns * pb->Nn * pb->Nm * pb->Np * plane + 6 * plane;
 }
 
-int spx_plan_create(const spx_problem* pb, spx_plan** out) {
+int spx_plan_create(const spx_problem* pb, spx_plan** out) { return spx_plan_create_ex(pb, 0, 0, out); }
+
+int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx_plan** out) {
   if (!out) { set_error("null output pointer"); return SPX_E_ARG; }
   *out = nullptr;
+  if (tile < 0 || tile > 16 || !(threads == 0 || (threads >= 32 && threads <= 256 && threads % 32 == 0))) {
+    set_error("spx_plan_create_ex: tile must be 0..16 and threads 0 or a multiple of 32 in 32..256");
+    return SPX_E_ARG;
+  }
   int dev = 0;
   SPX_CUDA(cudaGetDevice(&dev));
   int nsm = 0;
   SPX_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   spx_plan* pl = new spx_plan();
   pl->device = dev;
-  int rc = build_plan_host(pb, nsm, pl);
+  pl->threads = threads > 0 ? threads : NTHREADS;
+  int rc = build_plan_host(pb, nsm, pl, tile);
   if (rc != SPX_OK) { delete pl; return rc; }
   rc = set_attrs();
   if (rc != SPX_OK) { delete pl; return rc; }
@@ -433,6 +440,15 @@ int spx_plan_destroy(spx_plan* pl) {
 }
 
 size_t spx_rhs_workspace_bytes(const spx_plan* pl) { return pl ? pl->ws_bytes : 0; }
+
+int spx_plan_info(const spx_plan* pl, int32_t* tile, int32_t* ntiles, int32_t* threads, int32_t* path) {
+  if (!pl) { set_error("spx_plan_info: null plan"); return SPX_E_ARG; }
+  if (tile) *tile = pl->host.tile;
+  if (ntiles) *ntiles = pl->host.ntiles;
+  if (threads) *threads = pl->threads;
+  if (path) *path = pl->host.path;
+  return SPX_OK;
+}
 
 int spx_rhs(const spx_plan* pl, const void* y, void* dy, void* ws, size_t ws_bytes, void* stream) {
   if (!pl || !y || !dy) { set_error("spx_rhs: null argument"); return SPX_E_ARG; }
@@ -470,12 +486,12 @@ int spx_jvp(const spx_plan* pl, const void* y, const void* v, void* Jv, void* ws
   double2* out = static_cast<double2*>(Jv);
   double2* w = static_cast<double2*>(ws);
   if (P.path == 0) {
-    k_jvp1v<<<P.pb.Ns * P.ntiles + 1, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, yy, vv, out);
+    k_jvp1v<<<P.pb.Ns * P.ntiles + 1, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, yy, vv, out);
   } else {
     const int nplanes = P.pb.Ns * P.nh;
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
-    k_jvp_real<<<2 * nreal, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, vv, w);
-    k_jvp_nl<<<nplanes + 1, NTHREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w, out);
+    k_jvp_real<<<2 * nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, vv, w);
+    k_jvp_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w, out);
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
@@ -492,10 +508,10 @@ int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   double2* part = static_cast<double2*>(ws);
-  k_vjp1v<<<P.pb.Ns * P.ntiles, NTHREADS, pl->smem_1v, st>>>(
+  k_vjp1v<<<P.pb.Ns * P.ntiles, pl->threads, pl->smem_1v, st>>>(
       pl->d_plan, pl->d_tab, static_cast<const double2*>(y), static_cast<const double2*>(wv),
       static_cast<double2*>(g), part);
-  k_vjp1v_fields<<<1, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(wv),
+  k_vjp1v_fields<<<1, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(wv),
                                                    static_cast<double2*>(g), part);
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;

@@ -89,7 +89,7 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
     sA[l * N + std_index(c, N)] = v;
   }
   __syncthreads();
-  double2* r = fft_axis<true>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0});
+  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
   double2* o = (r == sA) ? sB : sA;
   // real-space products into the lines right after the G lines
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
@@ -99,7 +99,7 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
     r[ng * N + i] = pr;
   }
   __syncthreads();
-  double2* f = fft_axis<false>(r + ng * N, o + ng * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0});
+  double2* f = fft_axis_t<false, true>(r + ng * N, o + ng * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
   const double ua = u0 / a0;
   const double Dd = P.pb.D;
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
@@ -217,7 +217,7 @@ __device__ inline void general_to_real(const DevPlan& P, const double2* __restri
     sA[d] = v;
   }
   __syncthreads();
-  double2* r = fft_planes<true>(sA, sB, P, tab, 1);
+  double2* r = fft_planes_t<true, false>(sA, sB, P, tab, 1);
   for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) out[pt] = r[pt];
 }
 
@@ -339,7 +339,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     sA[pt] = acc;
   }
   __syncthreads();
-  double2* f = fft_planes<false>(sA, sB, P, tab, 1);
+  double2* f = fft_planes_t<false, true>(sA, sB, P, tab, 1);
 
   const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
   const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
@@ -462,10 +462,11 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
   }
   __syncthreads();
   // both transforms have the same number of stages, so both results land in `r`
-  double2* r = fft_axis<true>(sA, sB, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0});
+  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
   double2* o = (r == sA) ? sB : sA;
   {
-    double2* r2 = fft_axis<false>(sA + (nt + 1) * N, sB + (nt + 1) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0});
+    double2* r2 = fft_axis_t<false, false>(sA + (nt + 1) * N, sB + (nt + 1) * N, P.ax[1], tab,
+                                           Lines{nt, 1, 1, N, 0}, cut);
     (void)r2;
   }
   // partial field sum R_s(x) for this tile (fixed order over planes), then Q = G . W in place
@@ -484,7 +485,7 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
     r[(1 + nt) * N + i] = cmul(r[x], r[(1 + nt) * N + i]);
   }
   __syncthreads();
-  double2* q = fft_axis<true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0});
+  double2* q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
   const double ua = u0 / a0;
   const double Dd = P.pb.D;
   const double iO = 1.0 / P.pb.Omega_cs[0];
@@ -538,7 +539,7 @@ __device__ inline void vjp1v_fields(const DevPlan& P, const double2* __restrict_
     sA[s * N + x] = acc;
   }
   __syncthreads();
-  double2* r = fft_axis<true>(sA, sB, P.ax[1], tab, Lines{Ns, 1, 1, N, 0});
+  double2* r = fft_axis_t<true, true>(sA, sB, P.ax[1], tab, Lines{Ns, 1, 1, N, 0}, cut);
   const double2* Wf = w + P.nc;
   double2* gF = g + P.nc;
   for (int c = threadIdx.x; c < N; c += blockDim.x) {

@@ -53,24 +53,36 @@ class Ops:
         self.flops += mult * (2 * fma + addmul)
 
 
-def fft_line_ops(n: int) -> Ops:
-    """FP64 work of one length-n line through the Stockham engine."""
+def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit") -> Ops:
+    """FP64 work of one length-n line through the Stockham engine.
+
+    cut (the 2/3-mask cutoff) prunes the first decimation-in-time stage (masked
+    input, mode "dit") or the last decimation-in-frequency stage (masked output,
+    mode "dif") when that stage has an odd radix >= 5."""
     o = Ops()
     if n == 1:
         return o
     Ns = 1
-    for R in factorize(n):
+    for si, R in enumerate(factorize(n)):
         M = n // R
         tw_tasks = (M - M // Ns) if Ns > 1 else 0
-        if R % 2 == 0:
+        if R % 2 == 0 or R == 3:
             o.add(fma=2 * (R - 1), addmul=2 * (R - 1), mult=tw_tasks)   # twiddle cmuls
-            dft = {2: 4, 4: 16, 8: 56}[R]
+            dft = {2: 4, 3: 12, 4: 16, 8: 56}[R]
             o.add(addmul=dft, mult=M)
         else:
             h = (R - 1) // 2
+            prune = cut is not None and si == 0
+            qm = [min(h, (cut + j) // M) if prune else h for j in range(M)]
             o.add(fma=4, addmul=4, mult=tw_tasks * h)                   # two twiddles per pair
-            o.add(addmul=4, mult=M * h)                                 # sum / difference
-            o.add(fma=4 * h, addmul=4, mult=M * (h + 1))                # symmetric direct DFT
+            if mode == "dit":
+                o.add(addmul=4, mult=sum(qm))                           # pair sums / differences
+                for q in qm:                                            # all outputs, q <= qmax terms
+                    o.add(fma=4 * q, addmul=4, mult=h + 1)
+            else:
+                o.add(addmul=4, mult=M * h)
+                for q in qm:                                            # only outputs kk <= qmax
+                    o.add(fma=4 * h, addmul=4, mult=q + 1)
         Ns *= R
     return o
 
@@ -81,24 +93,26 @@ def rhs_ops(shape, tile=None, ntiles=None) -> Ops:
     o = Ops()
     plane = Nx * Ny * Nz
     if Ny == 1 and Nz == 1 and Nm == 1 and Np == 1:
-        f = fft_line_ops(Nx)
+        cut = Nx // 3
+        fi, ff = fft_line_ops(Nx, cut, "dit"), fft_line_ops(Nx, cut, "dif")
         ntiles = ntiles or 1
         lines_inv = Ns * (Nn + ntiles)          # C_{n-1} per plane + one G per tile
         lines_fwd = Ns * Nn
-        o.instr += f.instr * (lines_inv + lines_fwd)
-        o.flops += f.flops * (lines_inv + lines_fwd)
+        o.instr += fi.instr * lines_inv + ff.instr * lines_fwd
+        o.flops += fi.flops * lines_inv + ff.flops * lines_fwd
         o.add(fma=2, addmul=2, mult=Ns * Nn * Nx)            # G * C
         o.add(fma=6, addmul=4, mult=Ns * Nn * Nx)            # streaming, damping, NL add
         o.add(fma=4, addmul=2, mult=Ns * Nx)                 # G combination
         o.add(fma=8 * Ns + 6, addmul=24, mult=Nx)            # Maxwell + current
         return o
-    fy, fx, fz = fft_line_ops(Ny), fft_line_ops(Nx), fft_line_ops(Nz)
-    per_plane = Ops(instr=fy.instr * Nx * Nz + fx.instr * Ny * Nz + fz.instr * Ny * Nx,
-                    flops=fy.flops * Nx * Nz + fx.flops * Ny * Nz + fz.flops * Ny * Nx)
+    def plane(mode):
+        fy, fx, fz = (fft_line_ops(N, N // 3, mode) for N in (Ny, Nx, Nz))
+        return Ops(instr=fy.instr * Nx * Nz + fx.instr * Ny * Nz + fz.instr * Ny * Nx,
+                   flops=fy.flops * Nx * Nz + fx.flops * Ny * Nz + fz.flops * Ny * Nx)
+    pi, pf = plane("dit"), plane("dif")
     nplanes = Ns * Nn * Nm * Np
-    ntr = 2 * nplanes + 3 * Ns + 3
-    o.instr += per_plane.instr * ntr
-    o.flops += per_plane.flops * ntr
+    o.instr += pi.instr * (nplanes + 3 * Ns + 3) + pf.instr * nplanes
+    o.flops += pi.flops * (nplanes + 3 * Ns + 3) + pf.flops * nplanes
     o.add(fma=30, addmul=12, mult=nplanes * plane)           # real-space bracket (interior planes)
     o.add(fma=12, addmul=8, mult=nplanes * plane)            # streaming x/y/z, damping, NL add
     o.add(fma=8 * Ns + 6, addmul=24, mult=plane)

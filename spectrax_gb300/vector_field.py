@@ -29,17 +29,21 @@ def _stream_ptr(stream=None):
 class Plan:
     """Owns one ``spx_plan`` (device tables) plus a cached workspace."""
 
-    def __init__(self, problem: _lib.spx_problem, device=None):
+    def __init__(self, problem: _lib.spx_problem, device=None, tile=0, threads=0):
         L = _lib.lib()
         self.problem = problem
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         with torch.cuda.device(self.device):
             h = C.c_void_p()
-            _lib.check(L.spx_plan_create(C.byref(problem), C.byref(h)), "spx_plan_create")
+            _lib.check(L.spx_plan_create_ex(C.byref(problem), int(tile), int(threads), C.byref(h)),
+                       "spx_plan_create_ex")
         self.handle = h
         self.state_len = int(L.spx_state_len(C.byref(problem)))
         self.ws_bytes = int(L.spx_rhs_workspace_bytes(h))
         self._ws = None
+        t, nt, th, path = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        _lib.check(L.spx_plan_info(h, C.byref(t), C.byref(nt), C.byref(th), C.byref(path)), "spx_plan_info")
+        self.tile, self.ntiles, self.threads, self.path = t.value, nt.value, th.value, path.value
 
     @property
     def shape(self):
@@ -117,19 +121,64 @@ class Plan:
             self.handle = None
 
 
-def get_plan(problem: _lib.spx_problem, device=None) -> Plan:
+def get_plan(problem: _lib.spx_problem, device=None, tile=0, threads=0) -> Plan:
     dev = torch.cuda.current_device() if device is None else device
-    key = (bytes(problem), dev)
+    key = (bytes(problem), dev, int(tile), int(threads))
     with _cache_lock:
         pl = _plan_cache.get(key)
         if pl is None:
-            pl = Plan(problem, dev)
+            pl = Plan(problem, dev, tile, threads)
             _plan_cache[key] = pl
         return pl
 
 
-def plan_for_params(params, mask_mode=None, device=None) -> Plan:
-    return get_plan(problem_from_params(params, mask_mode or get_mask_mode()), device)
+_tuned: dict = {}
+
+
+def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False):
+    """Pick (tile, threads) for a problem by timing the right-hand side over a
+    candidate grid; returns the tuned Plan (cached per problem)."""
+    dev = torch.cuda.current_device() if device is None else device
+    key = (bytes(problem), dev)
+    if key in _tuned:
+        return _tuned[key]
+    base = get_plan(problem, dev)
+    if base.path != 0:
+        cands = [(0, t) for t in (128, 256)]
+    else:
+        Nn = problem.Nn
+        tiles = sorted({t for t in (1, 2, 3, 4, 5, 6, 8, 12, 16) if t <= max(1, Nn)} | {base.tile})
+        cands = [(t, th) for t in tiles for th in (128, 256)]
+    y = torch.randn(base.state_len, dtype=torch.complex128, device=base.device) * 1e-3
+    best, table = None, []
+    for t, th in cands:
+        try:
+            pl = get_plan(problem, dev, t, th)
+        except _lib.SpectraxError:
+            continue
+        dy = torch.empty_like(y)
+        for _ in range(3):
+            pl.rhs_into(y, dy)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            pl.rhs_into(y, dy)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        table.append((pl.tile, th, ms))
+        if verbose:
+            print(f"autotune tile={pl.tile} threads={th}: {ms * 1e3:.1f} us", flush=True)
+        if best is None or ms < best[2]:
+            best = (pl, th, ms)
+    best[0].tuning = table
+    _tuned[key] = best[0]
+    return best[0]
+
+
+def plan_for_params(params, mask_mode=None, device=None, tuned=False) -> Plan:
+    pb = problem_from_params(params, mask_mode or get_mask_mode())
+    return autotune(pb, device) if tuned else get_plan(pb, device)
 
 
 def _as_cuda_state(y, dev):
