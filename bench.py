@@ -307,7 +307,7 @@ def run_ours(args):
     from spectrax_gb300.vector_field import plan_for_params
 
     p, y0 = two_stream_params(seed=rank)
-    plan = plan_for_params(p, "divide")
+    plan = plan_for_params(p, "divide", tuned=True)      # autotuned tile / CTA width
     n = plan.state_len
     solver = Dopri8Solver(plan, 0.0, 1e9, 0.01, ts=None, adaptive=True, rtol=RTOL, atol=ATOL,
                           max_steps=1 << 40, save_states=False, masses=[1.0, 1.0, 1836.0])
@@ -381,6 +381,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "step": "one Dopri8 step attempt (13 fused RHS stages + controller)",
                    "state_len": n, "l2": "flushed (256 MB write) before every timed step",
+                   "tile": plan.tile, "threads": plan.threads,
                    "parallelism": "replicas" if world > 1 else "single"},
         "accepted_steps_per_s": acc_all / (t_ms * 1e-3),
         "e2e": {"value": e2e_evals_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,

@@ -245,59 +245,77 @@ __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __r
   }
   __syncthreads();
   {
-    // task list: per butterfly j the output pairs kk = 0 .. kmax(j)
+    // task list: per butterfly j the output pairs kk = 0 .. kmax(j), two pairs
+    // (kk, kk + 1) per task so that a_q / b_q loads are shared and each thread
+    // runs eight independent FMA chains.
     const bool prune_out = DIF && pcut >= 0;
-    int per_line = M * (h + 1);
+    int per_line = M * ((h + 2) >> 1);
     if (prune_out) {
       per_line = 0;
-      for (int j = 0; j < M; ++j) per_line += pair_limit(j, M, h, pcut) + 1;
+      for (int j = 0; j < M; ++j) per_line += (pair_limit(j, M, h, pcut) + 2) >> 1;
     }
     const int ntask = L.nl * per_line;
     for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
       const int l = t / per_line;
       int r = t - l * per_line;
-      int j, kk;
+      int j, kmax;
       if (!prune_out) {
-        j = r / (h + 1);
-        kk = r - j * (h + 1);
+        const int pj = (h + 2) >> 1;
+        j = r / pj;
+        r -= j * pj;
+        kmax = h;
       } else {
         j = 0;
-        int c = pair_limit(0, M, h, pcut) + 1;
-        while (r >= c) { r -= c; ++j; c = pair_limit(j, M, h, pcut) + 1; }
-        kk = r;
+        kmax = pair_limit(0, M, h, pcut);
+        int c = (kmax + 2) >> 1;
+        while (r >= c) { r -= c; ++j; kmax = pair_limit(j, M, h, pcut); c = (kmax + 2) >> 1; }
       }
+      const int kk0 = 2 * r;
+      const bool two = kk0 + 1 <= kmax;
+      const int kk1 = two ? kk0 + 1 : kk0;
       const int b = L.base(l);
       const int k = j % Ns;
       const int idx = (j / Ns) * Ns * R + k;
       const int qmax = (!DIF && pcut >= 0) ? pair_limit(j, M, h, pcut) : h;
       const int s0 = DIF ? Ns : M;                    // input stride between q's
       const int i0 = DIF ? idx : j;                   // input position of q = 0
-      double2 A = in[b + i0 * L.es];
-      double2 B = make_double2(0.0, 0.0);
-      int ang = 0;   // (q * kk) mod R
+      const double2 x0 = in[b + i0 * L.es];
+      double2 A0 = x0, A1 = x0;
+      double2 B0 = make_double2(0.0, 0.0), B1 = make_double2(0.0, 0.0);
+      int ang0 = 0, ang1 = 0;   // (q * kk) mod R
       for (int q = 1; q <= qmax; ++q) {
-        ang += kk;
-        if (ang >= R) ang -= R;
-        const double2 cq = cs[ang];
+        ang0 += kk0;
+        if (ang0 >= R) ang0 -= R;
+        ang1 += kk1;
+        if (ang1 >= R) ang1 -= R;
         const double2 aq = in[b + (i0 + q * s0) * L.es];
         const double2 bq = in[b + (i0 + (R - q) * s0) * L.es];
-        A = crfma(cq.x, aq, A);
-        B = crfma(cq.y, bq, B);
+        const double2 c0 = cs[ang0], c1 = cs[ang1];
+        A0 = crfma(c0.x, aq, A0);
+        B0 = crfma(c0.y, bq, B0);
+        A1 = crfma(c1.x, aq, A1);
+        B1 = crfma(c1.y, bq, B1);
       }
-      // forward: X_kk = A - iB, X_{R-kk} = A + iB ; inverse: signs swapped
-      const double2 iB = INV ? make_double2(-B.y, B.x) : make_double2(B.y, -B.x);
-      double2 X1 = cadd(A, iB), X2 = csub(A, iB);
-      if (!DIF) {
-        out[b + (idx + kk * Ns) * L.es] = X1;
-        if (kk > 0) out[b + (idx + (R - kk) * Ns) * L.es] = X2;
-      } else {
-        if (Ns > 1 && k > 0 && kk > 0) {
-          const double2* w = tw + k * (R - 1);
-          X1 = twiddle<INV>(X1, w[kk - 1]);
-          X2 = twiddle<INV>(X2, w[R - kk - 1]);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (u == 1 && !two) break;
+        const int kk = u ? kk1 : kk0;
+        const double2 A = u ? A1 : A0, B = u ? B1 : B0;
+        // forward: X_kk = A - iB, X_{R-kk} = A + iB ; inverse: signs swapped
+        const double2 iB = INV ? make_double2(-B.y, B.x) : make_double2(B.y, -B.x);
+        double2 X1 = cadd(A, iB), X2 = csub(A, iB);
+        if (!DIF) {
+          out[b + (idx + kk * Ns) * L.es] = X1;
+          if (kk > 0) out[b + (idx + (R - kk) * Ns) * L.es] = X2;
+        } else {
+          if (Ns > 1 && k > 0 && kk > 0) {
+            const double2* w = tw + k * (R - 1);
+            X1 = twiddle<INV>(X1, w[kk - 1]);
+            X2 = twiddle<INV>(X2, w[R - kk - 1]);
+          }
+          out[b + (j + kk * M) * L.es] = X1;
+          if (kk > 0) out[b + (j + (R - kk) * M) * L.es] = X2;
         }
-        out[b + (j + kk * M) * L.es] = X1;
-        if (kk > 0) out[b + (j + (R - kk) * M) * L.es] = X2;
       }
     }
   }

@@ -49,6 +49,14 @@ struct D8Args {
 __constant__ double cCoef[14][13];
 __constant__ int cMask[14];
 
+// Programmatic dependent launch: wait until the previous launch in the stream
+// has completed and its writes are visible, then let the next launch start its
+// own prologue.  Both are no-ops when the launch has no programmatic dependency.
+__device__ __forceinline__ void pdl_wait_and_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 struct Attempt {
   double h, t_stop;
   int landed, go;
@@ -75,9 +83,9 @@ struct EpiStage {
   double h;
   __device__ __forceinline__ void operator()(size_t e, double2 v) const {
     K[(size_t)stage * len + e] = v;
-    double2 acc = Y[e];
     const int row = stage;   // coefficients a(stage+1, j)
     const int mask = cMask[row];
+    double2 acc = Y[e];
     for (int j = 0; j < stage; ++j)
       if (mask & (1 << j)) acc = crfma(h * cCoef[row][j], K[(size_t)j * len + e], acc);
     acc = crfma(h * cCoef[row][stage], v, acc);
@@ -218,17 +226,21 @@ __device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, doub
 }
 
 // ------------------------------------------------------------------ stage kernels
-__global__ void __launch_bounds__(NTHREADS) k_d8_stage_1v(D8Args a, int stage) {
+template <bool LAST>
+__global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
   __shared__ double red[NTHREADS / 32];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
+  // prologue independent of the previous launch; then wait for it (PDL)
+  load_plan(P, stab, a.plan, a.tab);
+  pdl_wait_and_release();
   if (threadIdx.x == 0) {
     s = *a.st;
     if (stage == 0 && blockIdx.x == 0) a.st->save_pending = 0;
   }
-  load_plan(P, stab, a.plan, a.tab);   // contains __syncthreads
+  __syncthreads();
   const Attempt at = attempt_params(s, a.save_ts);
   if (!at.go) {
     if (stage == rk::S - 1 && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING) {
@@ -247,7 +259,7 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_stage_1v(D8Args a, int stage) {
   const int sp = b / P.ntiles, tile = b % P.ntiles;
   const int n0 = tile * P.tile;
   const int nt = min(P.tile, P.pb.Nn - n0);
-  if (stage < rk::S - 1) {
+  if constexpr (!LAST) {
     EpiStage epi{Y, a.K, a.S[(stage + 1) & 1], a.len, stage, at.h};
     if (stage == 0 && s.k1_valid) {
       for_each_owned_1v(P, b, [&](size_t e) { epi(e, a.K[e]); });
@@ -269,8 +281,10 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
   __shared__ D8Dev s;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
-  if (threadIdx.x == 0) s = *a.st;
   load_plan(P, stab, a.plan, a.tab);
+  pdl_wait_and_release();
+  if (threadIdx.x == 0) s = *a.st;
+  __syncthreads();
   const Attempt at = attempt_params(s, a.save_ts);
   if (!at.go || (stage == 0 && s.k1_valid)) return;
   const double2* in = (stage == 0) ? a.Y[s.cur] : a.S[stage & 1];
@@ -279,17 +293,20 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
   general_to_real(P, stab, in, blockIdx.x, a.ws + (size_t)blockIdx.x * P.plane, sA, sB);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_d8_stage_gen(D8Args a, int stage) {
+template <bool LAST>
+__global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
   __shared__ double red[NTHREADS / 32];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, a.plan, a.tab);
+  pdl_wait_and_release();
   if (threadIdx.x == 0) {
     s = *a.st;
     if (stage == 0 && blockIdx.x == 0) a.st->save_pending = 0;
   }
-  load_plan(P, stab, a.plan, a.tab);
+  __syncthreads();
   const Attempt at = attempt_params(s, a.save_ts);
   if (!at.go) {
     if (stage == rk::S - 1 && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING) {
@@ -304,7 +321,7 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_stage_gen(D8Args a, int stage) 
   double2* sB = sA + P.plane;
   const int b = blockIdx.x;
   const double2* GB = a.ws + (size_t)nplanes * P.plane;
-  if (stage < rk::S - 1) {
+  if constexpr (!LAST) {
     EpiStage epi{Y, a.K, a.S[(stage + 1) & 1], a.len, stage, at.h};
     if (stage == 0 && s.k1_valid) {
       for_each_owned_gen(P, b, [&](size_t e) { epi(e, a.K[e]); });
@@ -326,6 +343,7 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_stage_gen(D8Args a, int stage) 
 __global__ void __launch_bounds__(NTHREADS) k_d8_save(D8Args a) {
   __shared__ D8Dev s;
   __shared__ double red[NTHREADS / 32];
+  pdl_wait_and_release();
   if (threadIdx.x == 0) s = *a.st;
   __syncthreads();
   if (!s.save_pending) return;
@@ -433,27 +451,54 @@ static int d8_attrs() {
   if (done) return SPX_OK;
   const int optin = smem_optin();
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_real));
   SPX_CUDA(cudaFuncSetAttribute(k_d8_real, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen<false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_gen<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen<true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_gen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   done = true;
   return SPX_OK;
+}
+
+// Launch with a programmatic dependency on the previous kernel in the stream, so
+// its prologue overlaps the tail of that kernel.
+template <class... Args>
+static void launch_pdl(void (*k)(Args...), int grid, int threads, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
 }
 
 static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;
   for (int stage = 0; stage < rk::S; ++stage) {
     if (P.path == 0) {
-      k_d8_stage_1v<<<s->grid_stage, s->plan->threads, s->plan->smem_1v, st>>>(s->args, stage);
+      if (stage < rk::S - 1)
+        launch_pdl(k_d8_stage_1v<false>, s->grid_stage, s->plan->threads, s->plan->smem_1v, st, s->args, stage);
+      else
+        launch_pdl(k_d8_stage_1v<true>, s->grid_stage, s->plan->threads, s->plan->smem_1v, st, s->args, stage);
     } else {
-      k_d8_real<<<s->grid_real, s->plan->threads, s->plan->smem_gen, st>>>(s->args, stage);
-      k_d8_stage_gen<<<s->grid_stage, s->plan->threads, s->plan->smem_gen, st>>>(s->args, stage);
+      launch_pdl(k_d8_real, s->grid_real, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
+      if (stage < rk::S - 1)
+        launch_pdl(k_d8_stage_gen<false>, s->grid_stage, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
+      else
+        launch_pdl(k_d8_stage_gen<true>, s->grid_stage, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
     }
   }
-  k_d8_save<<<s->plan->nsm, NTHREADS, 0, st>>>(s->args);
+  launch_pdl(k_d8_save, s->plan->nsm, (int)NTHREADS, (size_t)0, st, s->args);
 }
 
 static int d8_free(spx_dopri8* s) {

@@ -135,6 +135,137 @@ __device__ __forceinline__ void rhs1v_tile(const DevPlan& P, const double2* __re
 }
 
 // ------------------------------------------------------------------------
+// Fused 1D1V tile, gather-first variant.  The stage input is read through a
+// source functor `src(e)` (a plain vector, or y + h sum a_j K_j for a Runge-
+// Kutta stage) with all of an element's loads in flight, once per element,
+// into a shared-memory copy U of the tile's unmasked planes n0-1 .. n0+nt;
+// the FFT lines and the linear terms then read U, so the only global reads
+// are in this gather.  U: (nt+2)*N, sA/sB: (nt+1)*N double2 each.
+// ------------------------------------------------------------------------
+struct SrcPlain {
+  const double2* y;
+  __device__ __forceinline__ double2 operator()(size_t e) const { return y[e]; }
+};
+
+template <class Src, class Epi>
+__device__ void rhs1v_tile_g(const DevPlan& P, const double2* __restrict__ tab, const Src& src,
+                             int s, int n0, int nt, double2* U, double2* sA, double2* sB,
+                             double* scoef, Epi& epi) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  const size_t sbase = (size_t)s * Nn * N;
+  const double a0 = P.pb.alpha_s[3 * s];
+  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
+  const int nu = nt + 2;          // planes n0-1 .. n0+nt
+  const int nl = nt + 1;          // FFT lines: G, then C_{n-1} for the nt planes
+  if (threadIdx.x < nt) {
+    const int n = n0 + threadIdx.x;
+    double* c = scoef + 4 * threadIdx.x;
+    c[0] = sqrt((double)(n + 1) * 0.5);
+    c[1] = sqrt((double)n * 0.5);
+    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
+    c[3] = P.pb.nu * colc(Nn, n);
+  }
+  // gather: U lines, and the masked field combination G straight into FFT line 0
+  for (int i = threadIdx.x; i < (nu + 1) * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    if (l < nu) {
+      const int n = n0 - 1 + l;
+      U[i] = (n >= 0 && n < Nn) ? src(sbase + (size_t)n * N + c) : make_double2(0.0, 0.0);
+    } else {
+      double2 v = make_double2(0.0, 0.0);
+      if (kept(c, N, cut)) {
+        const size_t f0 = (size_t)P.nc + c;
+        v = src(f0);
+        v = crfma(u1, src(f0 + 5 * N), v);
+        v = crfma(-u2, src(f0 + 4 * N), v);
+      }
+      sA[std_index(c, N)] = v;
+    }
+  }
+  __syncthreads();
+  // FFT line l >= 1 holds the masked C_{n-1}, n = n0 + l - 1, i.e. U line l - 1
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int l = i / N + 1, c = i - (l - 1) * N;
+    sA[l * N + std_index(c, N)] = kept(c, N, cut) ? U[(l - 1) * N + c] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
+  double2* o = (r == sA) ? sB : sA;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int x = i % N;
+    r[N + i] = cmul(r[x], r[N + i]);
+  }
+  __syncthreads();
+  double2* f = fft_axis_t<false, true>(r + N, o + N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
+  const double ua = u0 / a0;
+  const double Dd = P.pb.D;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    const int n = n0 + l;
+    const double* cf = scoef + 4 * l;
+    const double2 kt = ktab(P, tab, 1, c);
+    const double w = kt.x * a0;
+    const double2 Cm = U[l * N + c], C0 = U[(l + 1) * N + c], Cp = U[(l + 2) * N + c];
+    double2 t = cscale(ua, C0);
+    t = crfma(cf[0], Cp, t);
+    t = crfma(cf[1], Cm, t);
+    double d = cf[3];
+    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
+    double re = fma(w, t.y, -d * C0.x);
+    double im = fma(-w, t.x, -d * C0.y);
+    if (n >= 1 && kept(c, N, cut)) {
+      const double2 nl2 = f[l * N + std_index(c, N)];
+      re = fma(cf[2], nl2.x, re);
+      im = fma(cf[2], nl2.y, im);
+    }
+    epi(sbase + (size_t)n * N + c, make_double2(re, im));
+  }
+}
+
+// Maxwell + current through a source functor (field CTA of the gather-first path).
+template <class Src, class Epi>
+__device__ void maxwell_src(const DevPlan& P, const double2* __restrict__ tab, const Src& src, Epi& epi) {
+  const spx_problem& pb = P.pb;
+  const int Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const size_t pl = (size_t)P.plane;
+  const double rs2 = 0.70710678118654752440;
+  const double iO = 1.0 / pb.Omega_cs[0];
+  for (int pt = threadIdx.x; pt < (int)pl; pt += blockDim.x) {
+    const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
+    const double Kx = ktab(P, tab, 1, cx).x, Ky = ktab(P, tab, 0, cy).x, Kz = ktab(P, tab, 2, cz).x;
+    double2 J0 = make_double2(0, 0), J1 = make_double2(0, 0), J2 = make_double2(0, 0);
+    for (int s = 0; s < pb.Ns; ++s) {
+      const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
+      const double pre = pb.qs[s] * a0 * a1 * a2;
+      const size_t b0 = (size_t)s * P.nh * pl + pt;
+      const double2 C000 = src(b0);
+      const double2 C100 = pb.Nn > 1 ? src(b0 + pl) : make_double2(0, 0);
+      const double2 C010 = pb.Nm > 1 ? src(b0 + (size_t)pb.Nn * pl) : make_double2(0, 0);
+      const double2 C001 = pb.Np > 1 ? src(b0 + (size_t)pb.Nn * pb.Nm * pl) : make_double2(0, 0);
+      J0 = crfma(pre, crfma(pb.u_s[3 * s], C000, cscale(a0 * rs2, C100)), J0);
+      J1 = crfma(pre, crfma(pb.u_s[3 * s + 1], C000, cscale(a1 * rs2, C010)), J1);
+      J2 = crfma(pre, crfma(pb.u_s[3 * s + 2], C000, cscale(a2 * rs2, C001)), J2);
+    }
+    const size_t f0 = (size_t)P.nc + pt;
+    const double2 Ex = src(f0), Ey = src(f0 + pl), Ez = src(f0 + 2 * pl);
+    const double2 Bx = src(f0 + 3 * pl), By = src(f0 + 4 * pl), Bz = src(f0 + 5 * pl);
+    const double2 kbx = csub(cscale(Ky, Bz), cscale(Kz, By));
+    const double2 kby = csub(cscale(Kz, Bx), cscale(Kx, Bz));
+    const double2 kbz = csub(cscale(Kx, By), cscale(Ky, Bx));
+    const double2 kex = csub(cscale(Ky, Ez), cscale(Kz, Ey));
+    const double2 key = csub(cscale(Kz, Ex), cscale(Kx, Ez));
+    const double2 kez = csub(cscale(Kx, Ey), cscale(Ky, Ex));
+    epi(f0, make_double2(fma(-J0.x, iO, -kbx.y), fma(-J0.y, iO, kbx.x)));
+    epi(f0 + pl, make_double2(fma(-J1.x, iO, -kby.y), fma(-J1.y, iO, kby.x)));
+    epi(f0 + 2 * pl, make_double2(fma(-J2.x, iO, -kbz.y), fma(-J2.y, iO, kbz.x)));
+    epi(f0 + 3 * pl, make_double2(kex.y, -kex.x));
+    epi(f0 + 4 * pl, make_double2(key.y, -key.x));
+    epi(f0 + 5 * pl, make_double2(kez.y, -kez.x));
+  }
+}
+
+// ------------------------------------------------------------------------
 // Maxwell + current for Fourier points [p0, p1) of the field planes.
 // ------------------------------------------------------------------------
 template <class Epi, class LD = LdPlain>
