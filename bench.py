@@ -307,7 +307,8 @@ def run_ours(args):
     from spectrax_gb300.vector_field import plan_for_params
 
     p, y0 = two_stream_params(seed=rank)
-    plan = plan_for_params(p, "divide", tuned=True)      # autotuned tile / CTA width
+    # tile / CTA width autotuned on Dopri8 attempts of this very state
+    plan = plan_for_params(p, "divide", tuned=True, tune_for="dopri8", sample=torch.from_numpy(y0))
     n = plan.state_len
     solver = Dopri8Solver(plan, 0.0, 1e9, 0.01, ts=None, adaptive=True, rtol=RTOL, atol=ATOL,
                           max_steps=1 << 40, save_states=False, masses=[1.0, 1.0, 1836.0])
@@ -363,34 +364,31 @@ def run_ours(args):
     ms_per_step = t_ms / args.steps
     hbm_peak, hbm_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, _lib.lib())
-    stage_ms = ms_per_step / 13.0
-    bytes_launch = perf.dopri8_vectors_per_step() * n * 16 / 13.0
-    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    Ns_, Nn_ = SHAPE[6], SHAPE[3]
-    T = max(1, min(16, -(-Ns_ * Nn_ // nsm)))
-    ntiles = -(-Nn_ // T)
-    ops = perf.rhs_ops(SHAPE, T, ntiles)
-    # per-stage FP64 work: one RHS + the fused Runge-Kutta combination (~2 FMA per read vector)
-    flops_stage = ops.flops + 4.0 * (perf.dopri8_vectors_per_step() / 13.0) * n
-    achieved_gbs = bytes_launch / (stage_ms * 1e-3) / 1e9
-    achieved_tf = flops_stage / (stage_ms * 1e-3) / 1e12
+    launch_ms = ms_per_step / 14.0
+    # algorithmic bytes of an average launch of the step (13 stages, finish; save is empty)
+    bytes_launch = perf.dopri8_vectors_per_step() * n * 16 / 14.0
+    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile))
+    # FP64 work of a step: 13 RHS + the Runge-Kutta combinations (4 flops per complex FMA)
+    flops_step = 13.0 * ops.flops + 4.0 * perf.dopri8_combination_fmas_per_entry() * n
+    achieved_gbs = bytes_launch / (launch_ms * 1e-3) / 1e9
+    achieved_tf = flops_step / (ms_per_step * 1e-3) / 1e12
     traffic = profile_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "step": "one Dopri8 step attempt (13 fused RHS stages + controller)",
+        "config": {"workload": WORKLOAD, "step": "one Dopri8 step attempt (13 fused RHS stages, finish + controller, save)",
                    "state_len": n, "l2": "flushed (256 MB write) before every timed step",
                    "tile": plan.tile, "threads": plan.threads,
                    "parallelism": "replicas" if world > 1 else "single"},
         "accepted_steps_per_s": acc_all / (t_ms * 1e-3),
         "e2e": {"value": e2e_evals_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": n * 16},
-        "gpu_launches": args.steps * 14,
+        "gpu_launches": args.steps * 15,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                      "peak_source": hbm_src,
-                     "kernel": "k_d8_stage_1v (duration = step time / 13)"},
+                     "kernel": "k_d8_stage_1v + k_d8_finish (duration = step time / 14)"},
         "fp64": {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
                  "frac": achieved_tf / fp64_peak, "peak_source": "live FMA probe (spx_probe_fp64)",
                  "note": "the binding ceiling of this path on GB300"},

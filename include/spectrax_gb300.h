@@ -165,6 +165,10 @@ typedef struct spx_dopri8_opts {
   int32_t save_states; /* 1: keep every saved state (nsave * state_len complex128) */
   const double* masses; /* host array of Ns species masses for the kinetic energy (NULL: ones);
                            spectrax/_diagnostics.py:44-68 uses (1, mi_me) for two species */
+  int32_t hermitian;  /* 1: at reset, test y0 for exact Hermitian symmetry (C(-k) == conj C(k)
+                           bit for bit, every plane) on the fused 1D1V path with odd Nx; when it
+                           holds, evaluate stages with packed real transforms (half the FFTs).
+                           The symmetry is then kept exactly by every stage.  0: never. */
 } spx_dopri8_opts;
 
 typedef struct spx_dopri8 spx_dopri8;   /* opaque: stage buffers + CUDA graph */
@@ -174,6 +178,8 @@ typedef struct spx_dopri8_stats {
   double t, dt;
   int64_t accepted, rejected, rhs_evals;
   int32_t status, saved;
+  int32_t hermitian;  /* 1 if the packed real-transform stages are in use */
+  int32_t pad;
 } spx_dopri8_stats;
 
 /*

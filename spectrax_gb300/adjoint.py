@@ -34,33 +34,7 @@ from .dopri8 import Dopri8Solver
 from .params import initialize_simulation_parameters
 from .vector_field import Plan, _stream_ptr, plan_for_params
 
-# Prince-Dormand RK8(7)13M weights (the same published rationals as the device tableau)
-_A = {
-    1: {0: 1 / 18}, 2: {0: 1 / 48, 1: 1 / 16}, 3: {0: 1 / 32, 2: 3 / 32},
-    4: {0: 5 / 16, 2: -75 / 64, 3: 75 / 64}, 5: {0: 3 / 80, 3: 3 / 16, 4: 3 / 20},
-    6: {0: 29443841 / 614563906, 3: 77736538 / 692538347, 4: -28693883 / 1125000000,
-        5: 23124283 / 1800000000},
-    7: {0: 16016141 / 946692911, 3: 61564180 / 158732637, 4: 22789713 / 633445777,
-        5: 545815736 / 2771057229, 6: -180193667 / 1043307555},
-    8: {0: 39632708 / 573591083, 3: -433636366 / 683701615, 4: -421739975 / 2616292301,
-        5: 100302831 / 723423059, 6: 790204164 / 839813087, 7: 800635310 / 3783071287},
-    9: {0: 246121993 / 1340847787, 3: -37695042795 / 15268766246, 4: -309121744 / 1061227803,
-        5: -12992083 / 490766935, 6: 6005943493 / 2108947869, 7: 393006217 / 1396673457,
-        8: 123872331 / 1001029789},
-    10: {0: -1028468189 / 846180014, 3: 8478235783 / 508512852, 4: 1311729495 / 1432422823,
-         5: -10304129995 / 1701304382, 6: -48777925059 / 3047939560, 7: 15336726248 / 1032824649,
-         8: -45442868181 / 3398467696, 9: 3065993473 / 597172653},
-    11: {0: 185892177 / 718116043, 3: -3185094517 / 667107341, 4: -477755414 / 1098053517,
-         5: -703635378 / 230739211, 6: 5731566787 / 1027545527, 7: 5232866602 / 850066563,
-         8: -4093664535 / 808688257, 9: 3962137247 / 1805957418, 10: 65686358 / 487910083},
-    12: {0: 403863854 / 491063109, 3: -5068492393 / 434740067, 4: -411421997 / 543043805,
-         5: 652783627 / 914296604, 6: 11173962825 / 925320556, 7: -13158990841 / 6184727034,
-         8: 3936647629 / 1978049680, 9: -160528059 / 685178525, 10: 248638103 / 1413531060},
-}
-_B = [14005451 / 335480064, 0, 0, 0, 0, -59238493 / 1068277825, 181606767 / 758867731,
-      561292985 / 797845732, -1041891430 / 1371343529, 760417239 / 1151165299,
-      118820643 / 751138087, -528747749 / 2220607170, 1 / 4]
-S = 13
+from .tableau import A as _A, B as _B, S
 
 
 def _ptr(t: torch.Tensor):
@@ -94,8 +68,9 @@ class Dopri8Adjoint:
 
     # ------------------------------------------------------------------ forward
     def forward(self, y0: torch.Tensor):
+        # general (complex-transform) stages, the same kernels as the recomputation
         s = Dopri8Solver(self.plan, 0.0, self.ts[-1], self.dt, ts=self.ts, adaptive=False,
-                         save_states=False, masses=self.masses, max_steps=self.N + 10)
+                         save_states=False, masses=self.masses, max_steps=self.N + 10, hermitian=False)
         s.reset(y0)
         ckpts = [y0.clone()]
         done = 0

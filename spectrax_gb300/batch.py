@@ -202,10 +202,11 @@ def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses
 
 
 # ----------------------------------------------------------------- serial baseline
-def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None):
+def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermitian=False):
     """Solve the instances one after another with the single-instance device
     Dopri8 (plain GPU right-hand side per stage).  Returns (final states, stats,
-    energies, seconds)."""
+    energies, seconds).  hermitian=False keeps the general complex-transform
+    stages, the same arithmetic as the batched kernel."""
     from .dopri8 import Dopri8Solver
     finals, stats, ens = [], [], []
     torch.cuda.synchronize()
@@ -213,7 +214,7 @@ def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None):
     for it in insts:
         plan = get_plan(it["problem"])
         s = Dopri8Solver(plan, 0.0, t1, dt0, ts=save_ts, adaptive=True, rtol=rtol, atol=atol,
-                         save_states=False, masses=it.get("masses"))
+                         save_states=False, masses=it.get("masses"), hermitian=hermitian)
         s.reset(torch.from_numpy(it["y0"]))
         s.run()
         finals.append(s.state())

@@ -34,6 +34,12 @@ struct AxisPlan {
   int kofs;              // offset of the per-axis k table: (k_c / L, k_c) pairs, n entries
 };
 
+// Shared-memory lines (of N double2) after the table on the fused 1D1V path:
+// two JVP line buffers of 2T+2 lines, or the gathered field CTA's 2*Ns+6 lines.
+__host__ __device__ __forceinline__ int lines_1v(int T, int Ns) {
+  return (4 * (T + 1) > 2 * Ns + 6) ? 4 * (T + 1) : 2 * Ns + 6;
+}
+
 // Everything a kernel needs about one problem; lives in device memory next to
 // the double2 table it indexes.
 struct DevPlan {

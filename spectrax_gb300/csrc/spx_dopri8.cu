@@ -1,14 +1,19 @@
 // spx_dopri8.cu — device Prince-Dormand 8(7) solver for one large instance.
 //
-// One step attempt = 13 stage launches + 1 save launch, captured once as a CUDA
-// graph and replayed.  Every stage kernel is the fused right-hand side with a
-// Runge-Kutta epilogue: the value f_i(e) of each output entry is stored as the
-// stage vector K_i(e) and immediately combined into the next stage input
-// y + h*sum_j a(i+1, j) K_j(e), so no separate combination pass touches memory.
-// The last stage writes y_new and the scaled error; its last CTA to finish
-// (atomic ticket, no spin-wait) reduces the per-CTA partial sums in a fixed
-// order and runs the step-size controller on the device.  The host only
-// replays graphs and polls the status word.
+// One step attempt is a fixed launch sequence captured once as a CUDA graph and
+// replayed; the host only replays graphs and polls the status word.
+//
+// Fused 1D1V path (13 stage launches + finish + save): stage i gathers its input
+// y + h*sum_j a(i, j) K_j straight from y and the stored K vectors, with all of
+// an entry's loads in flight, into a shared-memory copy of the tile's planes,
+// evaluates the right-hand side from there and stores only K_i.  The finish
+// kernel streams y_new and the scaled error over the state; its last CTA to
+// arrive (atomic ticket, no spin-wait) reduces the per-CTA sums in a fixed order
+// and runs the step-size controller on the device.
+//
+// General path (13 x (real-space + stage) + save): each stage epilogue stores
+// K_i and writes the next stage input; the last stage writes y_new and the
+// error and runs the same ticket/controller tail.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -26,7 +31,7 @@ struct D8Dev {
   int status, adaptive, cur, k1_valid;
   int isave, nsave, save_pending, save_lo, save_hi, saved;
   unsigned int arrive;
-  int pad;
+  int herm;           // 1: the state is exactly Hermitian, stages use packed real transforms
 };
 
 struct D8Args {
@@ -44,6 +49,11 @@ struct D8Args {
   const double* masses;
   long long len;
 };
+
+// Element i (0 or 1) of a two-pointer kernel argument, by select: indexing the
+// argument array with a runtime index would copy the argument block to local memory.
+template <class T>
+__device__ __forceinline__ T* pick(T* const (&p)[2], int i) { return i ? p[1] : p[0]; }
 
 // a(i+1, j) rows for i = 0..11, then b (row 12) and e (row 13); nonzero masks
 __constant__ double cCoef[14][13];
@@ -141,15 +151,9 @@ __device__ double block_sum(double v, double* red) {
   return r;   // valid in thread 0
 }
 
-// Last CTA of the last stage: reduce partials, accept/reject, advance the clock.
-__device__ void finalize_step(const D8Args& a, const Attempt& at, int nblocks) {
+// Thread 0 of the last CTA of an attempt: accept/reject, advance the clock.
+__device__ void finalize_step(const D8Args& a, const Attempt& at, double sum, int nonf) {
   D8Dev* st = a.st;
-  double sum = 0.0;
-  int nonf = 0;
-  for (int b = 0; b < nblocks; ++b) {
-    sum += __ldcg(a.part + 2 * b);
-    nonf |= (__ldcg(a.part + 2 * b + 1) != 0.0);
-  }
   const double en = sqrt(sum / (double)a.len);
   bool accept;
   double dt_next;
@@ -207,9 +211,12 @@ __device__ void for_each_owned_gen(const DevPlan& P, int b, F&& f) {
   for (size_t i = threadIdx.x; i < n; i += blockDim.x) f(base + i);
 }
 
-// Common tail of the last stage: per-CTA reduction and the ticket.
+// Common tail of an attempt: per-CTA partial sums, then an atomic ticket; the
+// last CTA to arrive (no spin-wait) reduces all partials with every thread in a
+// fixed order and runs the controller.
 template <class EL>
 __device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, double* red) {
+  __shared__ int last;
   const double s1 = block_sum(el.sq, red);
   __syncthreads();
   const double s2 = block_sum((double)el.nonfinite, red);
@@ -218,19 +225,69 @@ __device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, doub
     a.part[2 * blockIdx.x + 1] = s2;
     __threadfence();
     const unsigned int ticket = atomicAdd(&a.st->arrive, 1u);
-    if (ticket == gridDim.x - 1) {
-      __threadfence();
-      finalize_step(a, at, gridDim.x);
-    }
+    last = (ticket == gridDim.x - 1);
   }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double sum = 0.0, nf = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    sum += __ldcg(a.part + 2 * b);
+    nf += __ldcg(a.part + 2 * b + 1);
+  }
+  sum = block_sum(sum, red);
+  __syncthreads();
+  nf = block_sum(nf, red);
+  if (threadIdx.x == 0) finalize_step(a, at, sum, nf != 0.0);
 }
 
 // ------------------------------------------------------------------ stage kernels
-template <bool LAST>
+// Term lists of the stage inputs: stage i reads K_j for the j < i with
+// a(i, j) != 0, in ascending j (at most 10 terms for this tableau).
+constexpr int MAX_TERMS = 10;
+__constant__ int cTermN[13];
+__constant__ int cTermJ[13][MAX_TERMS];
+
+// Stage input y + h sum_j a(stage, j) K_j of one entry, loads issued in rounds
+// ahead of their multiply-adds; the sum runs over y, then j ascending.
+// The K_j offsets come from constant memory indexed by the launch's stage, so
+// they stay in uniform registers; c = h*a(stage, j) per term is in shared memory.
+struct SrcStage {
+  const double2* __restrict__ Y;
+  const double2* __restrict__ K;
+  long long len;
+  int stage;
+  const double* c;
+  __device__ __forceinline__ double2 operator()(size_t e) const {
+    const int nterm = cTermN[stage];
+    double2 acc = Y[e];
+    // two rounds of up to 5 loads in flight: 10 at once would not fit the
+    // register budget of the stage kernel next to its address arithmetic
+#pragma unroll 1
+    for (int r = 0; r < nterm; r += 5) {
+      double2 k[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j)
+        if (r + j < nterm) k[j] = K[(size_t)cTermJ[stage][r + j] * len + e];
+#pragma unroll
+      for (int j = 0; j < 5; ++j)
+        if (r + j < nterm) acc = crfma(c[r + j], k[j], acc);
+    }
+    return acc;
+  }
+};
+
+struct EpiK {
+  double2* __restrict__ K;
+  __device__ __forceinline__ void operator()(size_t e, double2 v) const { K[e] = v; }
+};
+
+// One stage of the fused 1D1V path: gather the stage input into shared memory,
+// evaluate the right-hand side, store K_stage.  Nothing else is written, so the
+// next stage and the finish kernel read only y and the K vectors.
 __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
-  __shared__ double red[NTHREADS / 32];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   // prologue independent of the previous launch; then wait for it (PDL)
@@ -242,38 +299,85 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
   }
   __syncthreads();
   const Attempt at = attempt_params(s, a.save_ts);
-  if (!at.go) {
-    if (stage == rk::S - 1 && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING) {
-      a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
-    }
-    return;
-  }
-  const double2* Y = a.Y[s.cur];
-  const double2* in = (stage == 0) ? Y : a.S[stage & 1];
+  if (!at.go) return;                      // the finish kernel records why
+  if (stage == 0 && s.k1_valid) return;    // K_0 = f(y) kept from the rejected attempt
+  __shared__ double tc[MAX_TERMS];
+  if (threadIdx.x < cTermN[stage]) tc[threadIdx.x] = at.h * cCoef[stage - 1][cTermJ[stage][threadIdx.x]];
+  __syncthreads();
+  const SrcStage src{pick(a.Y, s.cur), a.K, a.len, stage, tc};
+  EpiK epi{a.K + (size_t)stage * a.len};
   const int nblk = P.pb.Ns * P.ntiles;
   const int N = P.ax[1].n;
+  const int T = P.tile;
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + (size_t)(P.tile + 1) * N;
-  double* scoef = reinterpret_cast<double*>(sB + (size_t)(P.tile + 1) * N);
+  double2* sB = sA + (size_t)(T + 1) * N;
+  double2* U = sB + (size_t)(T + 1) * N;
+  double* scoef = reinterpret_cast<double*>(sA + (size_t)lines_1v(T, P.pb.Ns) * N);
   const int b = blockIdx.x;
-  const int sp = b / P.ntiles, tile = b % P.ntiles;
-  const int n0 = tile * P.tile;
-  const int nt = min(P.tile, P.pb.Nn - n0);
-  if constexpr (!LAST) {
-    EpiStage epi{Y, a.K, a.S[(stage + 1) & 1], a.len, stage, at.h};
-    if (stage == 0 && s.k1_valid) {
-      for_each_owned_1v(P, b, [&](size_t e) { epi(e, a.K[e]); });
-    } else if (b == nblk) {
-      maxwell_range(P, stab, in, 0, P.plane, epi);
-    } else if (nt > 0) {
-      rhs1v_tile(P, stab, in, sp, n0, nt, sA, sB, scoef, epi);
-    }
+  if (b == nblk) {
+    maxwell1v_g(P, stab, src, sA, epi);
   } else {
-    EpiLast el{Y, a.K, a.Y[s.cur ^ 1], a.len, at.h, s.rtol, s.atol, s.adaptive, 0.0, 0};
-    if (b == nblk) maxwell_range(P, stab, in, 0, P.plane, el);
-    else if (nt > 0) rhs1v_tile(P, stab, in, sp, n0, nt, sA, sB, scoef, el);
-    last_stage_tail(a, at, el, red);
+    const int sp = b / P.ntiles, tile = b % P.ntiles;
+    const int n0 = tile * T;
+    const int nt = min(T, P.pb.Nn - n0);
+    if (nt > 0) {
+      if (s.herm) rhs1v_tile_h(P, stab, src, sp, n0, nt, U, sA, sB, scoef, epi);
+      else rhs1v_tile_g(P, stab, src, sp, n0, nt, U, sA, sB, scoef, epi);
+    }
   }
+}
+
+// End of an attempt on the fused 1D1V path: y_new = y + h sum b_j K_j and the
+// error h sum e_j K_j, streamed over the whole state with every load in flight,
+// then the per-CTA error sums and the controller (last CTA).
+__global__ void __launch_bounds__(NTHREADS) k_d8_finish(D8Args a) {
+  __shared__ D8Dev s;
+  __shared__ double red[NTHREADS / 32];
+  pdl_wait_and_release();
+  if (threadIdx.x == 0) s = *a.st;
+  __syncthreads();
+  const Attempt at = attempt_params(s, a.save_ts);
+  if (!at.go) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING)
+      a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
+    return;
+  }
+  const double2* __restrict__ Y = pick(a.Y, s.cur);
+  const double2* __restrict__ K = a.K;
+  double2* __restrict__ Yn = pick(a.Y, s.cur ^ 1);
+  __shared__ double cb[13], ce[13];
+  if (threadIdx.x < 13) {
+    cb[threadIdx.x] = at.h * cCoef[12][threadIdx.x];
+    ce[threadIdx.x] = at.h * cCoef[13][threadIdx.x];
+  }
+  __syncthreads();
+  const int mb = cMask[12], me = cMask[13];
+  struct { double sq; int nonfinite; } el{0.0, 0};
+  const long long len = a.len;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len;
+       e += (long long)gridDim.x * blockDim.x) {
+    double2 k[13];
+#pragma unroll
+    for (int j = 0; j < 13; ++j)
+      if ((mb | me) & (1 << j)) k[j] = K[(size_t)j * len + e];
+    const double2 y0 = Y[e];
+    double2 yn = y0;
+    double2 er = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int j = 0; j < 13; ++j) {
+      if (mb & (1 << j)) yn = crfma(cb[j], k[j], yn);
+      if (me & (1 << j)) er = crfma(ce[j], k[j], er);
+    }
+    Yn[e] = yn;
+    if (!(isfinite(yn.x) && isfinite(yn.y))) el.nonfinite = 1;
+    if (s.adaptive) {
+      const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
+      const double sc = fma(s.rtol, sqrt(fmax(m0, m1)), s.atol);
+      const double rx = er.x / sc, ry = er.y / sc;
+      el.sq = fma(rx, rx, fma(ry, ry, el.sq));
+    }
+  }
+  last_stage_tail(a, at, el, red);
 }
 
 __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
@@ -287,7 +391,7 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
   __syncthreads();
   const Attempt at = attempt_params(s, a.save_ts);
   if (!at.go || (stage == 0 && s.k1_valid)) return;
-  const double2* in = (stage == 0) ? a.Y[s.cur] : a.S[stage & 1];
+  const double2* in = (stage == 0) ? pick(a.Y, s.cur) : pick(a.S, stage & 1);
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
   double2* sB = sA + P.plane;
   general_to_real(P, stab, in, blockIdx.x, a.ws + (size_t)blockIdx.x * P.plane, sA, sB);
@@ -314,15 +418,15 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stag
     }
     return;
   }
-  const double2* Y = a.Y[s.cur];
-  const double2* in = (stage == 0) ? Y : a.S[stage & 1];
+  const double2* Y = pick(a.Y, s.cur);
+  const double2* in = (stage == 0) ? Y : pick(a.S, stage & 1);
   const int nplanes = P.pb.Ns * P.nh;
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
   double2* sB = sA + P.plane;
   const int b = blockIdx.x;
   const double2* GB = a.ws + (size_t)nplanes * P.plane;
   if constexpr (!LAST) {
-    EpiStage epi{Y, a.K, a.S[(stage + 1) & 1], a.len, stage, at.h};
+    EpiStage epi{Y, a.K, pick(a.S, (stage + 1) & 1), a.len, stage, at.h};
     if (stage == 0 && s.k1_valid) {
       for_each_owned_gen(P, b, [&](size_t e) { epi(e, a.K[e]); });
     } else if (b == nplanes) {
@@ -331,11 +435,28 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stag
       general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, epi);
     }
   } else {
-    EpiLast el{Y, a.K, a.Y[s.cur ^ 1], a.len, at.h, s.rtol, s.atol, s.adaptive, 0.0, 0};
+    EpiLast el{Y, a.K, pick(a.Y, s.cur ^ 1), a.len, at.h, s.rtol, s.atol, s.adaptive, 0.0, 0};
     if (b == nplanes) maxwell_range(P, stab, in, 0, P.plane, el);
     else general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, el);
     last_stage_tail(a, at, el, red);
   }
+}
+
+// Exact Hermitian test of a fused-1D1V state (odd Nx): every line of Nx entries
+// (Hermite planes and field components) must satisfy y(N-1-c) == conj y(c).
+// Any violation clears *flag (set to 1 by the caller).
+__global__ void __launch_bounds__(NTHREADS) k_d8_herm_check(const double2* __restrict__ y, long long nlines,
+                                                           int N, int* flag) {
+  const long long total = nlines * N;
+  int bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long l = i / N;
+    const int c = (int)(i - l * N);
+    const double2 a = y[i], b = y[l * N + (N - 1 - c)];
+    if (!(a.x == b.x && a.y == -b.y)) bad = 1;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicAnd(flag, 0);
 }
 
 // Save: copy the state for pending save indices and compute the energies of
@@ -347,7 +468,7 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_save(D8Args a) {
   if (threadIdx.x == 0) s = *a.st;
   __syncthreads();
   if (!s.save_pending) return;
-  const double2* Y = a.Y[s.cur];
+  const double2* Y = pick(a.Y, s.cur);
   if (a.saved) {
     for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
       double2* dst = a.saved + (size_t)idx * a.len;
@@ -410,13 +531,14 @@ struct spx_dopri8 {
   D8Dev init{};
   void* block = nullptr;
   int nsave = 0;
-  int grid_stage = 0, grid_real = 0;
+  int grid_stage = 0, grid_real = 0, grid_finish = 0;
   int attempts_per_graph = 8;
   cudaStream_t cap = nullptr;
   cudaGraph_t graph = nullptr, graph1 = nullptr;
   cudaGraphExec_t exec = nullptr, exec1 = nullptr;   // `attempts_per_graph` attempts / one attempt
   int* h_status = nullptr;   // pinned
   std::vector<double> ts;
+  bool herm_allowed = false;  // requested, fused 1D1V path, odd Nx, antisymmetric k table
 };
 
 static bool g_d8_consts = false;
@@ -440,8 +562,20 @@ static int upload_consts() {
     if (c[12][j] != 0.0) m[12] |= 1 << j;
     if (c[13][j] != 0.0) m[13] |= 1 << j;
   }
+  int tn[13], tj[13][MAX_TERMS];
+  std::memset(tj, 0, sizeof(tj));
+  for (int i = 0; i < 13; ++i) {
+    tn[i] = 0;
+    for (int j = 0; j < i; ++j)
+      if (c[i - 1][j] != 0.0) {
+        if (tn[i] == MAX_TERMS) { set_error("tableau has more stage terms than supported"); return SPX_E_UNSUPPORTED; }
+        tj[i][tn[i]++] = j;
+      }
+  }
   SPX_CUDA(cudaMemcpyToSymbol(cCoef, c, sizeof(c)));
   SPX_CUDA(cudaMemcpyToSymbol(cMask, m, sizeof(m)));
+  SPX_CUDA(cudaMemcpyToSymbol(cTermN, tn, sizeof(tn)));
+  SPX_CUDA(cudaMemcpyToSymbol(cTermJ, tj, sizeof(tj)));
   g_d8_consts = true;
   return SPX_OK;
 }
@@ -451,10 +585,8 @@ static int d8_attrs() {
   if (done) return SPX_OK;
   const int optin = smem_optin();
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<false>));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_real));
   SPX_CUDA(cudaFuncSetAttribute(k_d8_real, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen<false>));
@@ -486,10 +618,7 @@ static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;
   for (int stage = 0; stage < rk::S; ++stage) {
     if (P.path == 0) {
-      if (stage < rk::S - 1)
-        launch_pdl(k_d8_stage_1v<false>, s->grid_stage, s->plan->threads, s->plan->smem_1v, st, s->args, stage);
-      else
-        launch_pdl(k_d8_stage_1v<true>, s->grid_stage, s->plan->threads, s->plan->smem_1v, st, s->args, stage);
+      launch_pdl(k_d8_stage_1v, s->grid_stage, s->plan->threads, s->plan->smem_1v, st, s->args, stage);
     } else {
       launch_pdl(k_d8_real, s->grid_real, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
       if (stage < rk::S - 1)
@@ -498,6 +627,7 @@ static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
         launch_pdl(k_d8_stage_gen<true>, s->grid_stage, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
     }
   }
+  if (P.path == 0) launch_pdl(k_d8_finish, s->grid_finish, (int)NTHREADS, (size_t)0, st, s->args);
   launch_pdl(k_d8_save, s->plan->nsm, (int)NTHREADS, (size_t)0, st, s->args);
 }
 
@@ -539,12 +669,14 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   s->nsave = o->nsave;
   s->grid_stage = (P.path == 0) ? P.pb.Ns * P.ntiles + 1 : P.pb.Ns * P.nh + 1;
   s->grid_real = (P.path == 0) ? 0 : P.pb.Ns * P.nh + 3 * Ns + 3;
+  s->grid_finish = (int)std::min<long long>(plan->nsm, (len + NTHREADS - 1) / NTHREADS);
+  const int nparts = std::max(s->grid_stage, s->grid_finish);
   // one allocation: st | part | save_ts | masses | energies | Y0 Y1 S0 S1 | K[13] | ws | saved
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t vec = al((size_t)len * sizeof(double2));
   size_t off = 0;
   const size_t o_st = off; off += al(sizeof(D8Dev));
-  const size_t o_part = off; off += al(2 * (size_t)s->grid_stage * sizeof(double));
+  const size_t o_part = off; off += al(2 * (size_t)nparts * sizeof(double));
   const size_t o_ts = off; off += al(std::max(1, o->nsave) * sizeof(double));
   const size_t o_m = off; off += al(SPX_MAX_SPECIES * sizeof(double));
   const size_t o_en = off; off += al(std::max(1, o->nsave) * (size_t)(2 + Ns) * sizeof(double));
@@ -581,6 +713,14 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   I.t = o->t0; I.t0 = o->t0; I.t1 = o->t1; I.dt = o->dt0;
   I.rtol = o->rtol; I.atol = o->atol; I.adaptive = o->adaptive ? 1 : 0;
   I.max_steps = o->max_steps; I.nsave = o->nsave; I.status = SPX_ST_RUNNING;
+  if (o->hermitian && P.path == 0 && (P.ax[1].n & 1)) {
+    // the streaming and Maxwell terms keep the symmetry only if k(N-1-c) == -k(c) exactly
+    const int N = P.ax[1].n;
+    bool anti = true;
+    for (int c = 0; c < N; ++c)
+      if (!(plan->tab[P.ax[1].kofs + c].x == -plan->tab[P.ax[1].kofs + N - 1 - c].x)) anti = false;
+    s->herm_allowed = anti;
+  }
   e = cudaMallocHost(&s->h_status, sizeof(int) * 4);
   if (e == cudaSuccess && o->nsave > 0)
     e = cudaMemcpy(b + o_ts, o->save_ts, o->nsave * sizeof(double), cudaMemcpyHostToDevice);
@@ -617,8 +757,15 @@ int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
   while (hi < s->nsave && s->ts[hi] <= I.t0) ++hi;
   if (hi > 0) { I.save_pending = 1; I.save_lo = 0; I.save_hi = hi; I.isave = hi; }
   if (I.t0 >= I.t1) I.status = SPX_ST_DONE;
+  I.herm = s->herm_allowed ? 1 : 0;
   SPX_CUDA(cudaMemcpyAsync(s->args.st, &I, sizeof(I), cudaMemcpyHostToDevice, st));
   SPX_CUDA(cudaMemcpyAsync(s->args.Y[0], y0, (size_t)s->args.len * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  if (s->herm_allowed) {
+    const int N = s->plan->host.ax[1].n;
+    const long long nlines = s->args.len / N;
+    const int grid = (int)std::min<long long>(4LL * s->plan->nsm, (s->args.len + NTHREADS - 1) / NTHREADS);
+    k_d8_herm_check<<<grid, NTHREADS, 0, st>>>(s->args.Y[0], nlines, N, &s->args.st->herm);
+  }
   if (hi > 0) k_d8_save<<<s->plan->nsm, NTHREADS, 0, st>>>(s->args);
   SPX_CUDA(cudaGetLastError());
   // the init struct lives on the host stack: make the copy complete before returning
@@ -678,6 +825,7 @@ int spx_dopri8_stats_get(spx_dopri8* s, spx_dopri8_stats* out, void* stream) {
   out->t = d.t; out->dt = d.dt;
   out->accepted = d.accepted; out->rejected = d.rejected; out->rhs_evals = d.evals;
   out->status = d.status; out->saved = d.saved;
+  out->hermitian = d.herm; out->pad = 0;
   return SPX_OK;
 }
 

@@ -136,13 +136,13 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
     const long long planes = (long long)p.Ns * p.Nn;
     int T = tile > 0 ? tile : (int)((planes + pl->nsm - 1) / pl->nsm);
     T = std::max(1, std::min(T, 16));
-    // shared memory of the widest user (the JVP): 2*(2T+2)*N double2 + table
-    while (T > 1 && pl->smem_tab + 2 * (size_t)(2 * T + 2) * N * sizeof(double2) > smem_max) --T;
+    // shared memory of the widest user: lines_1v(T, Ns)*N double2 + table
+    while (T > 1 && pl->smem_tab + (size_t)lines_1v(T, p.Ns) * N * sizeof(double2) > smem_max) --T;
     int ntiles = (p.Nn + T - 1) / T;
     T = (p.Nn + ntiles - 1) / ntiles;   // even out the tiles
     P.tile = T;
     P.ntiles = ntiles;
-    pl->smem_1v = pl->smem_tab + 2 * (size_t)(2 * T + 2) * N * sizeof(double2) + 16 * 4 * sizeof(double);
+    pl->smem_1v = pl->smem_tab + (size_t)lines_1v(T, p.Ns) * N * sizeof(double2) + 16 * 4 * sizeof(double);
     // the VJP keeps one partial field line per (species, tile)
     pl->ws_bytes = (size_t)p.Ns * ntiles * N * sizeof(double2);
   } else {

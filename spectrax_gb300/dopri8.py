@@ -33,7 +33,8 @@ def species_masses(params):
 
 class Dopri8Solver:
     def __init__(self, plan: Plan, t0: float, t1: float, dt0: float, ts=None, adaptive=True,
-                 rtol=1e-10, atol=1e-12, max_steps=1_000_000, save_states=True, masses=None):
+                 rtol=1e-10, atol=1e-12, max_steps=1_000_000, save_states=True, masses=None,
+                 hermitian=True):
         L = _lib.lib()
         self.plan = plan
         self.ts = np.ascontiguousarray(np.asarray([] if ts is None else ts, np.float64))
@@ -48,6 +49,9 @@ class Dopri8Solver:
         o.max_steps = int(max_steps)
         o.save_states = 1 if save_states else 0
         o.masses = self._masses.ctypes.data_as(C.POINTER(C.c_double))
+        # detect an exactly Hermitian y0 at reset (odd Nx, fused 1D1V path) and use
+        # packed real transforms for it
+        o.hermitian = 1 if hermitian else 0
         self.save_states = bool(save_states)
         h = C.c_void_p()
         with torch.cuda.device(plan.device):
@@ -81,7 +85,8 @@ class Dopri8Solver:
         s = _lib.spx_dopri8_stats()
         _lib.check(_lib.lib().spx_dopri8_stats_get(self.handle, C.byref(s), _stream_ptr(stream)), "stats")
         return dict(t=s.t, dt=s.dt, accepted=s.accepted, rejected=s.rejected, rhs_evals=s.rhs_evals,
-                    status=s.status, status_name=_lib.STATUS_NAMES.get(s.status, "?"), saved=s.saved)
+                    status=s.status, status_name=_lib.STATUS_NAMES.get(s.status, "?"), saved=s.saved,
+                    hermitian=bool(s.hermitian))
 
     def _copy(self, what, out):
         _lib.check(_lib.lib().spx_dopri8_copy(self.handle, what, C.c_void_p(out.data_ptr()),

@@ -10,20 +10,24 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
-# RK8(7)13M: per stage i (0-based) the number of earlier stage vectors the
-# fused epilogue reads to form the next stage input (nonzero a(i+1, j), j < i),
-# and for the last stage the number of stage vectors read for y_new and the error.
-_NEXT_INPUT_READS = [0, 1, 1, 2, 2, 3, 4, 5, 6, 7, 8, 9]
-_LAST_STAGE_READS = 8
-
-
 def dopri8_vectors_per_step() -> int:
-    """State-sized vectors read + written by one 13-stage step of the fused stepper."""
-    total = 3                              # stage 0: read y, write K0 and the next input
-    for m in _NEXT_INPUT_READS[1:]:
-        total += 4 + m                     # read input and y, write K_i and next input
-    total += 2 + _LAST_STAGE_READS + 1     # last stage: input, y, K_j, write y_new
+    """State-sized vectors read + written by one step attempt of the fused 1D1V stepper.
+
+    Stage i reads y and the K_j with a(i, j) != 0 (its input is formed while
+    gathering) and writes K_i; the finish kernel reads y and the K_j with
+    b_j != 0 or e_j != 0 and writes y_new."""
+    from .tableau import A, B, E
+    total = 0
+    for i in range(13):
+        total += 1 + len(A.get(i, {})) + 1
+    total += 1 + sum(1 for b, e in zip(B, E) if b != 0 or e != 0) + 1
     return total
+
+
+def dopri8_combination_fmas_per_entry() -> int:
+    """Complex multiply-adds per state entry and step for the stage inputs, y_new and the error."""
+    from .tableau import A, B, E
+    return sum(len(r) for r in A.values()) + sum(1 for b in B if b) + sum(1 for e in E if e)
 
 
 def factorize(n: int):

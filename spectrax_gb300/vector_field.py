@@ -135,11 +135,19 @@ def get_plan(problem: _lib.spx_problem, device=None, tile=0, threads=0) -> Plan:
 _tuned: dict = {}
 
 
-def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False):
-    """Pick (tile, threads) for a problem by timing the right-hand side over a
-    candidate grid; returns the tuned Plan (cached per problem)."""
+def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False, target="rhs", sample=None):
+    """Pick (tile, threads) for a problem by timing over a candidate grid; returns
+    the tuned Plan (cached per problem and target).
+
+    target "rhs" times the plain right-hand side; "dopri8" times fixed-step
+    Dopri8 attempts (13 gather-first stage kernels + finish), whose kernels
+    balance shared memory and latency differently.  `sample` is the state to
+    time with (an exactly Hermitian one selects the packed-transform stages);
+    default: small random values."""
+    if target not in ("rhs", "dopri8"):
+        raise ValueError("target must be 'rhs' or 'dopri8'")
     dev = torch.cuda.current_device() if device is None else device
-    key = (bytes(problem), dev)
+    key = (bytes(problem), dev, target, sample is not None)
     if key in _tuned:
         return _tuned[key]
     base = get_plan(problem, dev)
@@ -149,21 +157,34 @@ def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False):
         Nn = problem.Nn
         tiles = sorted({t for t in (1, 2, 3, 4, 5, 6, 8, 12, 16) if t <= max(1, Nn)} | {base.tile})
         cands = [(t, th) for t in tiles for th in (128, 256)]
-    y = torch.randn(base.state_len, dtype=torch.complex128, device=base.device) * 1e-3
+    if sample is not None:
+        y = torch.as_tensor(sample).to(base.device, torch.complex128).contiguous()
+        base.check_state(y, "sample")
+    else:
+        y = torch.randn(base.state_len, dtype=torch.complex128, device=base.device) * 1e-3
     best, table = None, []
     for t, th in cands:
         try:
             pl = get_plan(problem, dev, t, th)
         except _lib.SpectraxError:
             continue
-        dy = torch.empty_like(y)
-        for _ in range(3):
-            pl.rhs_into(y, dy)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            pl.rhs_into(y, dy)
-        e1.record()
+        if target == "rhs":
+            dy = torch.empty_like(y)
+            for _ in range(3):
+                pl.rhs_into(y, dy)
+            e0.record()
+            for _ in range(reps):
+                pl.rhs_into(y, dy)
+            e1.record()
+        else:
+            from .dopri8 import Dopri8Solver
+            sv = Dopri8Solver(pl, 0.0, 1e30, 1e-6, adaptive=False, max_steps=1 << 40, save_states=False)
+            sv.reset(y)
+            sv.enqueue(3)
+            e0.record()
+            sv.enqueue(reps)
+            e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         table.append((pl.tile, th, ms))
@@ -176,9 +197,9 @@ def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False):
     return best[0]
 
 
-def plan_for_params(params, mask_mode=None, device=None, tuned=False) -> Plan:
+def plan_for_params(params, mask_mode=None, device=None, tuned=False, tune_for="rhs", sample=None) -> Plan:
     pb = problem_from_params(params, mask_mode or get_mask_mode())
-    return autotune(pb, device) if tuned else get_plan(pb, device)
+    return autotune(pb, device, target=tune_for, sample=sample) if tuned else get_plan(pb, device)
 
 
 def _as_cuda_state(y, dev):
