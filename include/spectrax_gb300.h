@@ -38,7 +38,8 @@ enum {
   SPX_ST_DONE = 1,
   SPX_ST_MAX_STEPS = 2,
   SPX_ST_DT_UNDERFLOW = 3,
-  SPX_ST_NONFINITE = 4
+  SPX_ST_NONFINITE = 4,
+  SPX_ST_WAIT_TIMEOUT = 5   /* a bounded device-side wait for staged data gave up (solve stopped) */
 };
 
 /*

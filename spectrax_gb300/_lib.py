@@ -16,7 +16,7 @@ MAX_SPECIES = 8
 MAX_AXIS = 256
 
 SPX_OK, SPX_E_ARG, SPX_E_CUDA, SPX_E_WORKSPACE, SPX_E_UNSUPPORTED = 0, -1, -2, -3, -4
-STATUS_NAMES = {0: "RUNNING", 1: "DONE", 2: "MAX_STEPS", 3: "DT_UNDERFLOW", 4: "NONFINITE"}
+STATUS_NAMES = {0: "RUNNING", 1: "DONE", 2: "MAX_STEPS", 3: "DT_UNDERFLOW", 4: "NONFINITE", 5: "WAIT_TIMEOUT"}
 
 
 class SpectraxLibraryError(RuntimeError):

@@ -3,17 +3,18 @@
 // One step attempt is a fixed launch sequence captured once as a CUDA graph and
 // replayed; the host only replays graphs and polls the status word.
 //
-// Fused 1D1V path (13 stage launches + finish + save): stage i gathers its input
-// y + h*sum_j a(i, j) K_j straight from y and the stored K vectors, with all of
-// an entry's loads in flight, into a shared-memory copy of the tile's planes,
-// evaluates the right-hand side from there and stores only K_i.  The finish
-// kernel streams y_new and the scaled error over the state; its last CTA to
-// arrive (atomic ticket, no spin-wait) reduces the per-CTA sums in a fixed order
-// and runs the step-size controller on the device.
+// Fused 1D1V path (13 stage launches + save): stage i stages its input planes
+// (the tile's Hermite planes n0-1 .. n0+nt of S_i and the field lines G needs)
+// into shared memory with bulk copies, and on a second barrier the operands of
+// its epilogue (y and the K_j of its own planes), which land while the
+// transforms run.  The epilogue stores K_i and the next input
+// S_{i+1} = y + h sum_j a(i+1, j) K_j; the last stage forms y_new and the
+// scaled error instead, and its last CTA to arrive (atomic ticket, no
+// spin-wait) reduces the per-CTA sums in a fixed order and runs the step-size
+// controller on the device.
 //
-// General path (13 x (real-space + stage) + save): each stage epilogue stores
-// K_i and writes the next stage input; the last stage writes y_new and the
-// error and runs the same ticket/controller tail.
+// General path (13 x (real-space + stage) + save): the same epilogues with
+// global operands.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -22,6 +23,7 @@
 #include "spx_plan.h"
 #include "spx_rhs.cuh"
 #include "spx_tableau.cuh"
+#include "spx_tma.cuh"
 
 namespace spx {
 
@@ -48,6 +50,7 @@ struct D8Args {
   double* energies;
   const double* masses;
   long long len;
+  int npf;            // fused 1D1V path: epilogue operands staged in shared memory (y first)
 };
 
 // Element i (0 or 1) of a two-pointer kernel argument, by select: indexing the
@@ -242,52 +245,173 @@ __device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, doub
 }
 
 // ------------------------------------------------------------------ stage kernels
-// Term lists of the stage inputs: stage i reads K_j for the j < i with
-// a(i, j) != 0, in ascending j (at most 10 terms for this tableau).
+// Epilogue term lists: stage i < 12 forms the next input y + h sum_j a(i+1, j)
+// K_j over j < i with a(i+1, j) != 0 (then + h a(i+1, i) K_i); the last stage
+// forms y_new and the error over j < 12 with b_j != 0 or e_j != 0.  Ascending j.
 constexpr int MAX_TERMS = 10;
-__constant__ int cTermN[13];
-__constant__ int cTermJ[13][MAX_TERMS];
+__constant__ int cEpiN[13];
+__constant__ int cEpiJ[13][MAX_TERMS];
 
-// Stage input y + h sum_j a(stage, j) K_j of one entry, loads issued in rounds
-// ahead of their multiply-adds; the sum runs over y, then j ascending.
-// The K_j offsets come from constant memory indexed by the launch's stage, so
-// they stay in uniform registers; c = h*a(stage, j) per term is in shared memory.
-struct SrcStage {
+// Coefficients of the current launch's epilogue, in shared memory.
+struct EpiTerms {
+  int n;                       // number of K_j terms (j < stage)
+  int j[MAX_TERMS];
+  double c[MAX_TERMS];         // h a(stage+1, j)  or  h b_j
+  double e[MAX_TERMS];         // last stage: h e_j
+  double cself, eself;         // the current stage's own weights
+};
+
+__device__ void fill_terms(EpiTerms& T, int stage, double h) {
+  const bool last = stage == rk::S - 1;
+  const int row = last ? 12 : stage;
+  T.n = cEpiN[stage];
+  for (int t = 0; t < T.n; ++t) {
+    const int j = cEpiJ[stage][t];
+    T.j[t] = j;
+    T.c[t] = h * cCoef[row][j];
+    T.e[t] = last ? h * cCoef[13][j] : 0.0;
+  }
+  T.cself = h * cCoef[row][stage];
+  T.eself = last ? h * cCoef[13][stage] : 0.0;
+}
+
+// Epilogue of stages 0..11: store K_i and the next stage input.  The first
+// `npf` operands (y, then K_j in list order) of the CTA's own entries are
+// staged in shared memory `pf` (own entries each, local index il); the rest
+// are read from global memory, up to five loads in flight.
+struct EpiNext {
+  double2* __restrict__ Ki;
+  double2* __restrict__ Snext;
   const double2* __restrict__ Y;
   const double2* __restrict__ K;
   long long len;
-  int stage;
-  const double* c;
-  __device__ __forceinline__ double2 operator()(size_t e) const {
-    const int nterm = cTermN[stage];
-    double2 acc = Y[e];
-    // two rounds of up to 5 loads in flight: 10 at once would not fit the
-    // register budget of the stage kernel next to its address arithmetic
+  const EpiTerms* T;
+  const double2* pf;
+  int own, npf;
+  uint64_t* bar;               // completes when pf is filled (nullptr: nothing staged)
+  __device__ bool prepare() const {
+    if (!bar) return true;
+    const bool ok = mbar_wait_bounded(bar, 0);
+    return !__syncthreads_or(!ok);
+  }
+  __device__ __forceinline__ double2 operand(int q, size_t e, int il) const {
+    // q = 0: y, q >= 1: K_{j[q-1]}
+    if (q < npf) return pf[(size_t)q * own + il];
+    return q == 0 ? Y[e] : K[(size_t)T->j[q - 1] * len + e];
+  }
+  __device__ __forceinline__ void operator()(size_t e, int il, double2 v) const {
+    Ki[e] = v;
+    const int n = T->n;
+    double2 acc;
+    if (npf > n) {                       // every operand staged
+      acc = pf[il];
 #pragma unroll 1
-    for (int r = 0; r < nterm; r += 5) {
-      double2 k[5];
+      for (int t = 0; t < n; ++t) acc = crfma(T->c[t], pf[(size_t)(1 + t) * own + il], acc);
+    } else {
+      acc = operand(0, e, il);
+#pragma unroll 1
+      for (int r = 0; r < n; r += 5) {
+        double2 k[5];
 #pragma unroll
-      for (int j = 0; j < 5; ++j)
-        if (r + j < nterm) k[j] = K[(size_t)cTermJ[stage][r + j] * len + e];
+        for (int u = 0; u < 5; ++u)
+          if (r + u < n) k[u] = operand(1 + r + u, e, il);
 #pragma unroll
-      for (int j = 0; j < 5; ++j)
-        if (r + j < nterm) acc = crfma(c[r + j], k[j], acc);
+        for (int u = 0; u < 5; ++u)
+          if (r + u < n) acc = crfma(T->c[r + u], k[u], acc);
+      }
     }
-    return acc;
+    Snext[e] = crfma(T->cself, v, acc);
   }
 };
 
-struct EpiK {
-  double2* __restrict__ K;
-  __device__ __forceinline__ void operator()(size_t e, double2 v) const { K[e] = v; }
+// Epilogue of the last stage: y_new, scaled error, non-finite flag; operands
+// staged as in EpiNext.
+struct EpiFinal {
+  double2* __restrict__ Ki;
+  double2* __restrict__ Ynew;
+  const double2* __restrict__ Y;
+  const double2* __restrict__ K;
+  long long len;
+  const EpiTerms* T;
+  const double2* pf;
+  int own, npf;
+  uint64_t* bar;
+  double rtol, atol;
+  int adaptive;
+  double sq;
+  int nonfinite;
+  __device__ bool prepare() const {
+    if (!bar) return true;
+    const bool ok = mbar_wait_bounded(bar, 0);
+    return !__syncthreads_or(!ok);
+  }
+  __device__ __forceinline__ double2 operand(int q, size_t e, int il) const {
+    if (q < npf) return pf[(size_t)q * own + il];
+    return q == 0 ? Y[e] : K[(size_t)T->j[q - 1] * len + e];
+  }
+  __device__ __forceinline__ void operator()(size_t e, int il, double2 v) {
+    Ki[e] = v;
+    const double2 y0 = operand(0, e, il);
+    double2 yn = y0;
+    double2 er = make_double2(0.0, 0.0);
+    const int n = T->n;
+    if (npf > n) {                       // every operand staged
+#pragma unroll 1
+      for (int t = 0; t < n; ++t) {
+        const double2 k = pf[(size_t)(1 + t) * own + il];
+        yn = crfma(T->c[t], k, yn);
+        er = crfma(T->e[t], k, er);
+      }
+    } else {
+#pragma unroll 1
+      for (int r = 0; r < n; r += 5) {
+        double2 k[5];
+#pragma unroll
+        for (int u = 0; u < 5; ++u)
+          if (r + u < n) k[u] = operand(1 + r + u, e, il);
+#pragma unroll
+        for (int u = 0; u < 5; ++u)
+          if (r + u < n) {
+            yn = crfma(T->c[r + u], k[u], yn);
+            er = crfma(T->e[r + u], k[u], er);
+          }
+      }
+    }
+    yn = crfma(T->cself, v, yn);
+    er = crfma(T->eself, v, er);
+    Ynew[e] = yn;
+    if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
+    if (adaptive) {
+      const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
+      const double sc = fma(rtol, sqrt(fmax(m0, m1)), atol);
+      const double rx = er.x / sc, ry = er.y / sc;
+      sq = fma(rx, rx, fma(ry, ry, sq));
+    }
+  }
 };
 
-// One stage of the fused 1D1V path: gather the stage input into shared memory,
-// evaluate the right-hand side, store K_stage.  Nothing else is written, so the
-// next stage and the finish kernel read only y and the K vectors.
+// Shared-memory layout of the fused 1D1V stage kernel after the table (double2
+// units, all 16-byte aligned):
+//   sA, sB : (T+1)*N each   U : (T+2)*N   F3 : 3*N   (the field CTA reuses
+//   sA.. as its (2*Ns+12)*N gather + output area)   scoef : 64 doubles
+//   pf     : npf * T * N   (y and K_j of the CTA's own planes)
+__host__ __device__ __forceinline__ int d8_lines_1v(int T, int Ns) {
+  const int a = 2 * (T + 1) + (T + 2) + 3, b = 2 * Ns + 12;
+  return a > b ? a : b;
+}
+
+// One stage of the fused 1D1V path.  Thread 0 stages the tile's input planes
+// n0-1 .. n0+nt and the three field lines that G needs with bulk copies, plus
+// the epilogue's own-plane operands on a second barrier, so the latter arrive
+// while the transforms run.  The last stage (LAST) forms y_new and the error
+// and runs the controller in its last CTA.
+template <bool LAST>
 __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
+  __shared__ double red[NTHREADS / 32];
+  __shared__ EpiTerms terms;
+  __shared__ __align__(8) uint64_t bars[2];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   // prologue independent of the previous launch; then wait for it (PDL)
@@ -299,85 +423,115 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
   }
   __syncthreads();
   const Attempt at = attempt_params(s, a.save_ts);
-  if (!at.go) return;                      // the finish kernel records why
-  if (stage == 0 && s.k1_valid) return;    // K_0 = f(y) kept from the rejected attempt
-  __shared__ double tc[MAX_TERMS];
-  if (threadIdx.x < cTermN[stage]) tc[threadIdx.x] = at.h * cCoef[stage - 1][cTermJ[stage][threadIdx.x]];
-  __syncthreads();
-  const SrcStage src{pick(a.Y, s.cur), a.K, a.len, stage, tc};
-  EpiK epi{a.K + (size_t)stage * a.len};
-  const int nblk = P.pb.Ns * P.ntiles;
-  const int N = P.ax[1].n;
-  const int T = P.tile;
-  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + (size_t)(T + 1) * N;
-  double2* U = sB + (size_t)(T + 1) * N;
-  double* scoef = reinterpret_cast<double*>(sA + (size_t)lines_1v(T, P.pb.Ns) * N);
-  const int b = blockIdx.x;
-  if (b == nblk) {
-    maxwell1v_g(P, stab, src, sA, epi);
-  } else {
-    const int sp = b / P.ntiles, tile = b % P.ntiles;
-    const int n0 = tile * T;
-    const int nt = min(T, P.pb.Nn - n0);
-    if (nt > 0) {
-      if (s.herm) rhs1v_tile_h(P, stab, src, sp, n0, nt, U, sA, sB, scoef, epi);
-      else rhs1v_tile_g(P, stab, src, sp, n0, nt, U, sA, sB, scoef, epi);
-    }
-  }
-}
-
-// End of an attempt on the fused 1D1V path: y_new = y + h sum b_j K_j and the
-// error h sum e_j K_j, streamed over the whole state with every load in flight,
-// then the per-CTA error sums and the controller (last CTA).
-__global__ void __launch_bounds__(NTHREADS) k_d8_finish(D8Args a) {
-  __shared__ D8Dev s;
-  __shared__ double red[NTHREADS / 32];
-  pdl_wait_and_release();
-  if (threadIdx.x == 0) s = *a.st;
-  __syncthreads();
-  const Attempt at = attempt_params(s, a.save_ts);
   if (!at.go) {
-    if (blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING)
+    if (LAST && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING)
       a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
     return;
   }
-  const double2* __restrict__ Y = pick(a.Y, s.cur);
-  const double2* __restrict__ K = a.K;
-  double2* __restrict__ Yn = pick(a.Y, s.cur ^ 1);
-  __shared__ double cb[13], ce[13];
-  if (threadIdx.x < 13) {
-    cb[threadIdx.x] = at.h * cCoef[12][threadIdx.x];
-    ce[threadIdx.x] = at.h * cCoef[13][threadIdx.x];
+  if (threadIdx.x == 0) fill_terms(terms, stage, at.h);
+  const long long len = a.len;
+  const double2* Y = pick(a.Y, s.cur);
+  const double2* in = (stage == 0) ? Y : pick(a.S, stage & 1);
+  double2* Ki = a.K + (size_t)stage * len;
+  const int nblk = P.pb.Ns * P.ntiles;
+  const int N = P.ax[1].n, T = P.tile, Nn = P.pb.Nn;
+  const int b = blockIdx.x;
+  if (!LAST && stage == 0 && s.k1_valid) {
+    // rejected attempt: K_0 = f(y) is kept; rebuild the next input y + h a(1,0) K_0
+    __syncthreads();
+    double2* Sn = pick(a.S, 1);
+    auto one = [&](size_t e) { Sn[e] = crfma(terms.cself, Ki[e], Y[e]); };
+    if (b == nblk) {
+      for (int i = threadIdx.x; i < 6 * N; i += blockDim.x) one((size_t)P.nc + i);
+    } else {
+      const int sp = b / P.ntiles, n0 = (b % P.ntiles) * T, nt = min(T, Nn - n0);
+      const size_t base = ((size_t)sp * Nn + n0) * N;
+      for (int i = threadIdx.x; i < nt * N; i += blockDim.x) one(base + i);
+    }
+    return;
+  }
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double* scoef = reinterpret_cast<double*>(sA + (size_t)d8_lines_1v(T, P.pb.Ns) * N);
+  double2* pf = reinterpret_cast<double2*>(scoef + 64);
+  if (b == nblk) {
+    // field CTA: plain gather (one CTA, small) and global epilogue operands
+    __syncthreads();
+    if constexpr (!LAST) {
+      EpiNext epi{Ki, pick(a.S, (stage + 1) & 1), Y, a.K, len, &terms, nullptr, 0, 0, nullptr};
+      maxwell1v_g(P, stab, SrcPlain{in}, sA, epi);
+    } else {
+      EpiFinal el{Ki, pick(a.Y, s.cur ^ 1), Y, a.K, len, &terms, nullptr, 0, 0, nullptr,
+                  s.rtol, s.atol, s.adaptive, 0.0, 0};
+      maxwell1v_g(P, stab, SrcPlain{in}, sA, el);
+      last_stage_tail(a, at, el, red);
+    }
+    return;
+  }
+  const int sp = b / P.ntiles, n0 = (b % P.ntiles) * T, nt = min(T, Nn - n0);
+  if (nt <= 0) {
+    if constexpr (LAST) {
+      struct { double sq; int nonfinite; } none{0.0, 0};
+      __syncthreads();
+      last_stage_tail(a, at, none, red);
+    }
+    return;
+  }
+  double2* sB = sA + (size_t)(T + 1) * N;
+  double2* U = sB + (size_t)(T + 1) * N;
+  double2* F3 = U + (size_t)(T + 2) * N;
+  const size_t sbase = (size_t)sp * Nn * N;
+  const int own = nt * N;
+  const int npf = min(a.npf, 1 + cEpiN[stage]);
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
   }
   __syncthreads();
-  const int mb = cMask[12], me = cMask[13];
-  struct { double sq; int nonfinite; } el{0.0, 0};
-  const long long len = a.len;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len;
-       e += (long long)gridDim.x * blockDim.x) {
-    double2 k[13];
-#pragma unroll
-    for (int j = 0; j < 13; ++j)
-      if ((mb | me) & (1 << j)) k[j] = K[(size_t)j * len + e];
-    const double2 y0 = Y[e];
-    double2 yn = y0;
-    double2 er = make_double2(0.0, 0.0);
-#pragma unroll
-    for (int j = 0; j < 13; ++j) {
-      if (mb & (1 << j)) yn = crfma(cb[j], k[j], yn);
-      if (me & (1 << j)) er = crfma(ce[j], k[j], er);
-    }
-    Yn[e] = yn;
-    if (!(isfinite(yn.x) && isfinite(yn.y))) el.nonfinite = 1;
-    if (s.adaptive) {
-      const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
-      const double sc = fma(s.rtol, sqrt(fmax(m0, m1)), s.atol);
-      const double rx = er.x / sc, ry = er.y / sc;
-      el.sq = fma(rx, rx, fma(ry, ry, el.sq));
-    }
+  if (threadIdx.x == 0) {
+    const int lo = max(n0 - 1, 0), hi = min(n0 + nt, Nn - 1);     // staged planes, inclusive
+    const uint32_t bu = (uint32_t)((hi - lo + 1) * N * sizeof(double2));
+    const uint32_t bf = (uint32_t)(N * sizeof(double2));
+    mbar_arm(&bars[0], bu + 3 * bf);
+    bulk_g2s(U + (size_t)(lo - (n0 - 1)) * N, in + sbase + (size_t)lo * N, bu, &bars[0]);
+    const double2* F = in + P.nc;
+    bulk_g2s(F3, F, bf, &bars[0]);                    // E_x
+    bulk_g2s(F3 + N, F + 5 * (size_t)N, bf, &bars[0]); // B_z
+    bulk_g2s(F3 + 2 * N, F + 4 * (size_t)N, bf, &bars[0]); // B_y
+    const uint32_t bo = (uint32_t)(own * sizeof(double2));
+    mbar_arm(&bars[1], (uint32_t)npf * bo);
+    const size_t o0 = sbase + (size_t)n0 * N;
+    bulk_g2s(pf, Y + o0, bo, &bars[1]);
+    for (int q = 1; q < npf; ++q)
+      bulk_g2s(pf + (size_t)q * own, a.K + (size_t)terms.j[q - 1] * len + o0, bo, &bars[1]);
   }
-  last_stage_tail(a, at, el, red);
+  // planes outside [0, Nn) read as zero (disjoint from the staged ones)
+  if (n0 == 0)
+    for (int i = threadIdx.x; i < N; i += blockDim.x) U[i] = make_double2(0.0, 0.0);
+  if (n0 + nt == Nn)
+    for (int i = threadIdx.x; i < N; i += blockDim.x) U[(size_t)(nt + 1) * N + i] = make_double2(0.0, 0.0);
+  const bool ok = mbar_wait_bounded(&bars[0], 0);
+  if (__syncthreads_or(!ok)) {
+    // the staged input never arrived: stop the solve, give the copies a last chance
+    if (threadIdx.x == 0) {
+      atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
+      mbar_wait_bounded(&bars[1], 0);
+    }
+    return;
+  }
+  if constexpr (!LAST) {
+    EpiNext epi{Ki, pick(a.S, (stage + 1) & 1), Y, a.K, len, &terms, pf, own, npf, &bars[1]};
+    if (s.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
+    else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
+  } else {
+    EpiFinal el{Ki, pick(a.Y, s.cur ^ 1), Y, a.K, len, &terms, pf, own, npf, &bars[1],
+                s.rtol, s.atol, s.adaptive, 0.0, 0};
+    if (s.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
+    else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
+    last_stage_tail(a, at, el, red);
+  }
+  // a failed prepare() returns from the tile early: record it once
+  if (threadIdx.x == 0 && !mbar_try_wait(&bars[1], 0)) atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
 }
 
 __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
@@ -531,7 +685,8 @@ struct spx_dopri8 {
   D8Dev init{};
   void* block = nullptr;
   int nsave = 0;
-  int grid_stage = 0, grid_real = 0, grid_finish = 0;
+  int grid_stage = 0, grid_real = 0;
+  size_t smem_stage = 0;      // dynamic shared memory of the stage kernels
   int attempts_per_graph = 8;
   cudaStream_t cap = nullptr;
   cudaGraph_t graph = nullptr, graph1 = nullptr;
@@ -566,16 +721,17 @@ static int upload_consts() {
   std::memset(tj, 0, sizeof(tj));
   for (int i = 0; i < 13; ++i) {
     tn[i] = 0;
-    for (int j = 0; j < i; ++j)
-      if (c[i - 1][j] != 0.0) {
-        if (tn[i] == MAX_TERMS) { set_error("tableau has more stage terms than supported"); return SPX_E_UNSUPPORTED; }
-        tj[i][tn[i]++] = j;
-      }
+    for (int j = 0; j < i; ++j) {
+      const bool use = (i < 12) ? (c[i][j] != 0.0) : (c[12][j] != 0.0 || c[13][j] != 0.0);
+      if (!use) continue;
+      if (tn[i] == MAX_TERMS) { set_error("tableau has more stage terms than supported"); return SPX_E_UNSUPPORTED; }
+      tj[i][tn[i]++] = j;
+    }
   }
   SPX_CUDA(cudaMemcpyToSymbol(cCoef, c, sizeof(c)));
   SPX_CUDA(cudaMemcpyToSymbol(cMask, m, sizeof(m)));
-  SPX_CUDA(cudaMemcpyToSymbol(cTermN, tn, sizeof(tn)));
-  SPX_CUDA(cudaMemcpyToSymbol(cTermJ, tj, sizeof(tj)));
+  SPX_CUDA(cudaMemcpyToSymbol(cEpiN, tn, sizeof(tn)));
+  SPX_CUDA(cudaMemcpyToSymbol(cEpiJ, tj, sizeof(tj)));
   g_d8_consts = true;
   return SPX_OK;
 }
@@ -585,8 +741,10 @@ static int d8_attrs() {
   if (done) return SPX_OK;
   const int optin = smem_optin();
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_real));
   SPX_CUDA(cudaFuncSetAttribute(k_d8_real, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen<false>));
@@ -618,16 +776,18 @@ static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;
   for (int stage = 0; stage < rk::S; ++stage) {
     if (P.path == 0) {
-      launch_pdl(k_d8_stage_1v, s->grid_stage, s->plan->threads, s->plan->smem_1v, st, s->args, stage);
+      if (stage < rk::S - 1)
+        launch_pdl(k_d8_stage_1v<false>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
+      else
+        launch_pdl(k_d8_stage_1v<true>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
     } else {
       launch_pdl(k_d8_real, s->grid_real, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
       if (stage < rk::S - 1)
-        launch_pdl(k_d8_stage_gen<false>, s->grid_stage, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
+        launch_pdl(k_d8_stage_gen<false>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
       else
-        launch_pdl(k_d8_stage_gen<true>, s->grid_stage, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
+        launch_pdl(k_d8_stage_gen<true>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
     }
   }
-  if (P.path == 0) launch_pdl(k_d8_finish, s->grid_finish, (int)NTHREADS, (size_t)0, st, s->args);
   launch_pdl(k_d8_save, s->plan->nsm, (int)NTHREADS, (size_t)0, st, s->args);
 }
 
@@ -669,8 +829,27 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   s->nsave = o->nsave;
   s->grid_stage = (P.path == 0) ? P.pb.Ns * P.ntiles + 1 : P.pb.Ns * P.nh + 1;
   s->grid_real = (P.path == 0) ? 0 : P.pb.Ns * P.nh + 3 * Ns + 3;
-  s->grid_finish = (int)std::min<long long>(plan->nsm, (len + NTHREADS - 1) / NTHREADS);
-  const int nparts = std::max(s->grid_stage, s->grid_finish);
+  const int nparts = s->grid_stage;
+  int npf = 0;
+  if (P.path == 0) {
+    // stage kernel shared memory: table + line buffers + coefficients + staged
+    // epilogue operands; stage as many operands (y, then K_j) as keep two CTAs
+    // per SM resident, at least y.
+    const int T = P.tile, N = P.ax[1].n;
+    const size_t base = plan->smem_tab + (size_t)d8_lines_1v(T, Ns) * N * sizeof(double2) + 64 * sizeof(double);
+    const size_t per = (size_t)T * N * sizeof(double2);
+    cudaFuncAttributes fa;
+    cudaError_t ea = cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>);
+    if (ea != cudaSuccess) { delete s; return cuda_fail(ea, "cudaFuncGetAttributes"); }
+    const size_t two_per_sm = 228 * 1024 / 2 - 1024 - fa.sharedSizeBytes;
+    const size_t optin = (size_t)smem_optin() - fa.sharedSizeBytes;
+    const size_t budget = (base + per <= two_per_sm) ? two_per_sm : optin;
+    npf = (int)std::min<size_t>(1 + MAX_TERMS, budget > base ? (budget - base) / per : 0);
+    if (npf < 1) { delete s; set_error("Nx / tile too large for the Dopri8 stage kernel"); return SPX_E_UNSUPPORTED; }
+    s->smem_stage = base + (size_t)npf * per;
+  } else {
+    s->smem_stage = plan->smem_gen;
+  }
   // one allocation: st | part | save_ts | masses | energies | Y0 Y1 S0 S1 | K[13] | ws | saved
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t vec = al((size_t)len * sizeof(double2));
@@ -703,6 +882,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   A.ws = reinterpret_cast<double2*>(b + o_ws);
   A.saved = o->save_states ? reinterpret_cast<double2*>(b + o_sv) : nullptr;
   A.len = len;
+  A.npf = npf;
   s->ts.assign(o->save_ts, o->save_ts + o->nsave);
   double masses[SPX_MAX_SPECIES];
   for (int i = 0; i < SPX_MAX_SPECIES; ++i) masses[i] = 1.0;

@@ -135,212 +135,144 @@ __device__ __forceinline__ void rhs1v_tile(const DevPlan& P, const double2* __re
 }
 
 // ------------------------------------------------------------------------
-// Fused 1D1V tile, gather-first variant.  The stage input is read through a
-// source functor `src(e)` (a plain vector, or y + h sum a_j K_j for a Runge-
-// Kutta stage) with all of an element's loads in flight, once per element,
-// into a shared-memory copy U of the tile's unmasked planes n0-1 .. n0+nt;
-// the FFT lines and the linear terms then read U, so the only global reads
-// are in this gather.  U: (nt+2)*N, sA/sB: (nt+1)*N double2 each.
+// Fused 1D1V tile over a stage input already staged in shared memory:
+//   U  : planes n0-1 .. n0+nt of species s ((nt+2)*N, zero outside [0, Nn))
+//   F3 : the field lines E_x, B_z, B_y (3*N), centred order.
+// The epilogue functor gets (global index, index within the tile's own planes,
+// value); its prepare() runs on every thread before the first call and may
+// wait for staged operands (returning false abandons the epilogue).  HERM = false: complex transforms of G and the nt lines C_{n-1}.
+// HERM = true (exactly Hermitian state, odd Nx): C(-k) = conj C(k) on every
+// line, so G(x) and C_{n-1}(x) are real and two real lines share one complex
+// transform: the inverse FFT of X_a + i X_b gives x_a + i x_b, and the forward
+// FFT W of p_a + i p_b gives P_a(k) = (W(k) + conj W(-k)) / 2 and
+// P_b(k) = -i (W(k) - conj W(-k)) / 2 -- half the transforms.  Every output is
+// formed from k and -k by mirrored operations, so the result is again exactly
+// Hermitian and the property holds along a Runge-Kutta trajectory.
+// sA / sB: (nt+1)*N double2 each; scoef: 4*nt doubles.
 // ------------------------------------------------------------------------
+template <bool HERM, class Epi>
+__device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, int s, int n0, int nt,
+                             const double2* U, const double2* F3, double2* sA, double2* sB,
+                             double* scoef, Epi& epi) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  const size_t sbase = (size_t)s * Nn * N;
+  const double a0 = P.pb.alpha_s[3 * s];
+  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
+  if (threadIdx.x < nt) {
+    const int n = n0 + threadIdx.x;
+    double* c = scoef + 4 * threadIdx.x;
+    c[0] = sqrt((double)(n + 1) * 0.5);
+    c[1] = sqrt((double)n * 0.5);
+    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
+    c[3] = P.pb.nu * colc(Nn, n);
+  }
+  // G = E_x + u_y B_z - u_z B_y at centred index c (masked)
+  auto G = [&](int c) {
+    double2 v = F3[c];
+    v = crfma(u1, F3[N + c], v);
+    return crfma(-u2, F3[2 * N + c], v);
+  };
+  const double2 zero = make_double2(0.0, 0.0);
+  double2* f;                           // forward transforms of the products
+  if (!HERM) {
+    // FFT lines: 0 = G, l + 1 = C_{n0+l-1} = U line l (masked, transform order)
+    for (int i = threadIdx.x; i < (nt + 1) * N; i += blockDim.x) {
+      const int l = i / N, c = i - l * N;
+      double2 v = zero;
+      if (kept(c, N, cut)) v = (l == 0) ? G(c) : U[(l - 1) * N + c];
+      sA[l * N + std_index(c, N)] = v;
+    }
+    __syncthreads();
+    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
+    double2* o = (r == sA) ? sB : sA;
+    for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+      const int x = i % N;
+      r[N + i] = cmul(r[x], r[N + i]);
+    }
+    __syncthreads();
+    f = fft_axis_t<false, true>(r + N, o + N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
+  } else {
+    const int nreal = nt + 1;             // real lines: 0 = G, q + 1 = C_{n0+q-1} = U line q
+    const int nin = (nreal + 1) / 2;      // packed inverse transforms
+    const int nout = (nt + 1) / 2;        // packed forward transforms
+    for (int i = threadIdx.x; i < nin * N; i += blockDim.x) {
+      const int j = i / N, c = i - j * N;
+      double2 z = zero;
+      if (kept(c, N, cut)) {
+        const int la = 2 * j, lb = 2 * j + 1;
+        const double2 xa = la == 0 ? G(c) : U[(la - 1) * N + c];
+        const double2 xb = lb < nreal ? U[(lb - 1) * N + c] : zero;
+        z = make_double2(xa.x - xb.y, xa.y + xb.x);
+      }
+      sA[j * N + std_index(c, N)] = z;
+    }
+    __syncthreads();
+    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nin, 1, 1, N, 0}, cut);
+    double2* o = (r == sA) ? sB : sA;
+    // real-space products p_q = G * C_{n0+q-1}, packed in pairs into o
+    for (int i = threadIdx.x; i < nout * N; i += blockDim.x) {
+      const int j = i / N, x = i - j * N;
+      const double g = r[x].x;
+      const int qa = 2 * j, qb = 2 * j + 1;      // real lines qa + 1, qb + 1
+      const double2 za = r[((qa + 1) >> 1) * N + x];
+      const double ca = ((qa + 1) & 1) ? za.y : za.x;
+      double cb = 0.0;
+      if (qb < nt) {
+        const double2 zb = r[((qb + 1) >> 1) * N + x];
+        cb = ((qb + 1) & 1) ? zb.y : zb.x;
+      }
+      o[j * N + x] = make_double2(g * ca, g * cb);
+    }
+    __syncthreads();
+    f = fft_axis_t<false, true>(o, r, P.ax[1], tab, Lines{nout, 1, 1, N, 0}, cut);
+  }
+  // the epilogue's own staged operands (called by every thread; false: give up)
+  if (!epi.prepare()) return;
+  const double ua = u0 / a0;
+  const double Dd = P.pb.D;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    const int n = n0 + l;
+    const double* cf = scoef + 4 * l;
+    const double2 kt = ktab(P, tab, 1, c);
+    const double w = kt.x * a0;
+    const double2 Cm = U[l * N + c], C0 = U[(l + 1) * N + c], Cp = U[(l + 2) * N + c];
+    double2 t = cscale(ua, C0);
+    t = crfma(cf[0], Cp, t);
+    t = crfma(cf[1], Cm, t);
+    double d = cf[3];
+    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
+    double re = fma(w, t.y, -d * C0.x);
+    double im = fma(-w, t.x, -d * C0.y);
+    if (n >= 1 && kept(c, N, cut)) {
+      double2 nl2;
+      if (!HERM) {
+        nl2 = f[l * N + std_index(c, N)];
+      } else {
+        const double2* fl = f + (l >> 1) * N;
+        const double2 W = fl[std_index(c, N)], Wm = fl[std_index(N - 1 - c, N)];
+        if ((l & 1) == 0) nl2 = make_double2(0.5 * (W.x + Wm.x), 0.5 * (W.y - Wm.y));
+        else nl2 = make_double2(0.5 * (W.y + Wm.y), -0.5 * (W.x - Wm.x));
+      }
+      re = fma(cf[2], nl2.x, re);
+      im = fma(cf[2], nl2.y, im);
+    }
+    epi(sbase + (size_t)n * N + c, i, make_double2(re, im));
+  }
+}
+
 struct SrcPlain {
   const double2* y;
   __device__ __forceinline__ double2 operator()(size_t e) const { return y[e]; }
 };
 
-template <class Src, class Epi>
-__device__ void rhs1v_tile_g(const DevPlan& P, const double2* __restrict__ tab, const Src& src,
-                             int s, int n0, int nt, double2* U, double2* sA, double2* sB,
-                             double* scoef, Epi& epi) {
-  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
-  const size_t sbase = (size_t)s * Nn * N;
-  const double a0 = P.pb.alpha_s[3 * s];
-  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
-  const int nu = nt + 2;          // planes n0-1 .. n0+nt
-  const int nl = nt + 1;          // FFT lines: G, then C_{n-1} for the nt planes
-  if (threadIdx.x < nt) {
-    const int n = n0 + threadIdx.x;
-    double* c = scoef + 4 * threadIdx.x;
-    c[0] = sqrt((double)(n + 1) * 0.5);
-    c[1] = sqrt((double)n * 0.5);
-    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
-    c[3] = P.pb.nu * colc(Nn, n);
-  }
-  // gather: U lines (U line l < nt is also FFT line l + 1, the masked C_{n-1}
-  // of plane n = n0 + l), and the masked field combination G into FFT line 0
-  // (one source read in flight per thread: a read is up to 13 loads)
-#pragma unroll 1
-  for (int i = threadIdx.x; i < (nu + 1) * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
-    if (l < nu) {
-      const int n = n0 - 1 + l;
-      const double2 v = (n >= 0 && n < Nn) ? src(sbase + (size_t)n * N + c) : make_double2(0.0, 0.0);
-      U[i] = v;
-      if (l < nt) sA[(l + 1) * N + std_index(c, N)] = kept(c, N, cut) ? v : make_double2(0.0, 0.0);
-    } else {
-      double2 v = make_double2(0.0, 0.0);
-      if (kept(c, N, cut)) {
-        // G = E_x + u_y B_z - u_z B_y
-        const size_t f0 = (size_t)P.nc + c;
-#pragma unroll 1
-        for (int q = 0; q < 3; ++q) {
-          const double2 f = src(f0 + (q == 0 ? 0 : (q == 1 ? 5 : 4)) * (size_t)N);
-          v = q == 0 ? f : crfma(q == 1 ? u1 : -u2, f, v);
-        }
-      }
-      sA[std_index(c, N)] = v;
-    }
-  }
-  __syncthreads();
-  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
-  double2* o = (r == sA) ? sB : sA;
-  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-    const int x = i % N;
-    r[N + i] = cmul(r[x], r[N + i]);
-  }
-  __syncthreads();
-  double2* f = fft_axis_t<false, true>(r + N, o + N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
-  const double ua = u0 / a0;
-  const double Dd = P.pb.D;
-  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
-    const int n = n0 + l;
-    const double* cf = scoef + 4 * l;
-    const double2 kt = ktab(P, tab, 1, c);
-    const double w = kt.x * a0;
-    const double2 Cm = U[l * N + c], C0 = U[(l + 1) * N + c], Cp = U[(l + 2) * N + c];
-    double2 t = cscale(ua, C0);
-    t = crfma(cf[0], Cp, t);
-    t = crfma(cf[1], Cm, t);
-    double d = cf[3];
-    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
-    double re = fma(w, t.y, -d * C0.x);
-    double im = fma(-w, t.x, -d * C0.y);
-    if (n >= 1 && kept(c, N, cut)) {
-      const double2 nl2 = f[l * N + std_index(c, N)];
-      re = fma(cf[2], nl2.x, re);
-      im = fma(cf[2], nl2.y, im);
-    }
-    epi(sbase + (size_t)n * N + c, make_double2(re, im));
-  }
-}
-
-// ------------------------------------------------------------------------
-// Fused 1D1V tile for an exactly Hermitian state (odd Nx): C(-k) = conj C(k)
-// for every plane, so G(x) and the C_{n-1}(x) are real.  Two real lines share
-// one complex transform: the inverse FFT of X_a + i X_b gives x_a + i x_b, and
-// the forward FFT W of p_a + i p_b gives P_a(k) = (W(k) + conj W(-k)) / 2 and
-// P_b(k) = -i (W(k) - conj W(-k)) / 2.  Half the transforms of rhs1v_tile_g.
-// Every output is formed from k and -k by mirrored operations, so the result
-// is again exactly Hermitian and the property holds along a Runge-Kutta
-// trajectory.  Real lines: 0 = G, q + 1 = C_{n0+q-1} = U line q.
-// ------------------------------------------------------------------------
-template <class Src, class Epi>
-__device__ void rhs1v_tile_h(const DevPlan& P, const double2* __restrict__ tab, const Src& src,
-                             int s, int n0, int nt, double2* U, double2* sA, double2* sB,
-                             double* scoef, Epi& epi) {
-  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
-  const size_t sbase = (size_t)s * Nn * N;
-  const double a0 = P.pb.alpha_s[3 * s];
-  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
-  const int nu = nt + 2;
-  const int nreal = nt + 1;               // G and the nt lines C_{n-1}
-  const int nin = (nreal + 1) / 2;        // packed inverse transforms
-  const int nout = (nt + 1) / 2;          // packed forward transforms
-  if (threadIdx.x < nt) {
-    const int n = n0 + threadIdx.x;
-    double* c = scoef + 4 * threadIdx.x;
-    c[0] = sqrt((double)(n + 1) * 0.5);
-    c[1] = sqrt((double)n * 0.5);
-    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
-    c[3] = P.pb.nu * colc(Nn, n);
-  }
-  // gather: U lines, and the field combination G (centred order) into sB line 0
-#pragma unroll 1
-  for (int i = threadIdx.x; i < (nu + 1) * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
-    if (l < nu) {
-      const int n = n0 - 1 + l;
-      U[i] = (n >= 0 && n < Nn) ? src(sbase + (size_t)n * N + c) : make_double2(0.0, 0.0);
-    } else {
-      double2 v = make_double2(0.0, 0.0);
-      if (kept(c, N, cut)) {
-        const size_t f0 = (size_t)P.nc + c;
-#pragma unroll 1
-        for (int q = 0; q < 3; ++q) {
-          const double2 f = src(f0 + (q == 0 ? 0 : (q == 1 ? 5 : 4)) * (size_t)N);
-          v = q == 0 ? f : crfma(q == 1 ? u1 : -u2, f, v);
-        }
-      }
-      sB[c] = v;
-    }
-  }
-  __syncthreads();
-  // pack real lines (2j, 2j+1) as X_2j + i X_2j+1, masked, in transform order
-  for (int i = threadIdx.x; i < nin * N; i += blockDim.x) {
-    const int j = i / N, c = i - j * N;
-    double2 z = make_double2(0.0, 0.0);
-    if (kept(c, N, cut)) {
-      const int la = 2 * j, lb = 2 * j + 1;
-      const double2 xa = la == 0 ? sB[c] : U[(la - 1) * N + c];
-      const double2 xb = lb < nreal ? U[(lb - 1) * N + c] : make_double2(0.0, 0.0);
-      z = make_double2(xa.x - xb.y, xa.y + xb.x);
-    }
-    sA[j * N + std_index(c, N)] = z;
-  }
-  __syncthreads();
-  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nin, 1, 1, N, 0}, cut);
-  double2* o = (r == sA) ? sB : sA;
-  // real-space products p_q = G * C_{n0+q-1}, packed in pairs into o
-  for (int i = threadIdx.x; i < nout * N; i += blockDim.x) {
-    const int j = i / N, x = i - j * N;
-    const double g = r[x].x;
-    const int qa = 2 * j, qb = 2 * j + 1;      // real lines qa + 1, qb + 1
-    const double2 za = r[((qa + 1) >> 1) * N + x];
-    const double ca = ((qa + 1) & 1) ? za.y : za.x;
-    double cb = 0.0;
-    if (qb < nt) {
-      const double2 zb = r[((qb + 1) >> 1) * N + x];
-      cb = ((qb + 1) & 1) ? zb.y : zb.x;
-    }
-    o[j * N + x] = make_double2(g * ca, g * cb);
-  }
-  __syncthreads();
-  double2* f = fft_axis_t<false, true>(o, r, P.ax[1], tab, Lines{nout, 1, 1, N, 0}, cut);
-  const double ua = u0 / a0;
-  const double Dd = P.pb.D;
-  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
-    const int n = n0 + l;
-    const double* cf = scoef + 4 * l;
-    const double2 kt = ktab(P, tab, 1, c);
-    const double w = kt.x * a0;
-    const double2 Cm = U[l * N + c], C0 = U[(l + 1) * N + c], Cp = U[(l + 2) * N + c];
-    double2 t = cscale(ua, C0);
-    t = crfma(cf[0], Cp, t);
-    t = crfma(cf[1], Cm, t);
-    double d = cf[3];
-    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
-    double re = fma(w, t.y, -d * C0.x);
-    double im = fma(-w, t.x, -d * C0.y);
-    if (n >= 1 && kept(c, N, cut)) {
-      const double2* fl = f + (l >> 1) * N;
-      const double2 W = fl[std_index(c, N)], Wm = fl[std_index(N - 1 - c, N)];
-      double2 nl2;
-      if ((l & 1) == 0) nl2 = make_double2(0.5 * (W.x + Wm.x), 0.5 * (W.y - Wm.y));
-      else nl2 = make_double2(0.5 * (W.y + Wm.y), -0.5 * (W.x - Wm.x));
-      re = fma(cf[2], nl2.x, re);
-      im = fma(cf[2], nl2.y, im);
-    }
-    epi(sbase + (size_t)n * N + c, make_double2(re, im));
-  }
-}
-
-// Field CTA of the gather-first 1D1V path: C_{s,0}, C_{s,1} and the six field
-// lines are gathered through `src` into shared memory F ((2*Ns + 6)*N double2,
-// one source read in flight per thread), then Maxwell + current as in
-// maxwell_range with Ny = Nz = Nm = Np = 1.
+// Field CTA of the staged 1D1V path: C_{s,0}, C_{s,1} and the six field lines
+// are gathered through `src` into shared memory F ((2*Ns + 12)*N double2, one
+// source read in flight per thread), Maxwell + current as in maxwell_range
+// with Ny = Nz = Nm = Np = 1 go to the last 6*N entries of F, and one loop
+// hands them to the epilogue (global index, index within the six field lines,
+// value), so a heavy epilogue is instantiated once.
 template <class Src, class Epi>
 __device__ void maxwell1v_g(const DevPlan& P, const double2* __restrict__ tab, const Src& src,
                             double2* F, Epi& epi) {
@@ -361,6 +293,7 @@ __device__ void maxwell1v_g(const DevPlan& P, const double2* __restrict__ tab, c
   }
   __syncthreads();
   const double2* Fl = F + 2 * Ns * N;
+  double2* Fo = F + (2 * Ns + 6) * N;
   const double rs2 = 0.70710678118654752440;
   const double iO = 1.0 / pb.Omega_cs[0];
   const double2 zero = make_double2(0.0, 0.0);
@@ -384,14 +317,16 @@ __device__ void maxwell1v_g(const DevPlan& P, const double2* __restrict__ tab, c
     const double2 kex = csub(cscale(Ky, Ez), cscale(Kz, Ey));
     const double2 key = csub(cscale(Kz, Ex), cscale(Kx, Ez));
     const double2 kez = csub(cscale(Kx, Ey), cscale(Ky, Ex));
-    const size_t f0 = (size_t)P.nc + pt;
-    epi(f0, make_double2(fma(-J0.x, iO, -kbx.y), fma(-J0.y, iO, kbx.x)));
-    epi(f0 + N, make_double2(fma(-J1.x, iO, -kby.y), fma(-J1.y, iO, kby.x)));
-    epi(f0 + 2 * N, make_double2(fma(-J2.x, iO, -kbz.y), fma(-J2.y, iO, kbz.x)));
-    epi(f0 + 3 * N, make_double2(kex.y, -kex.x));
-    epi(f0 + 4 * N, make_double2(key.y, -key.x));
-    epi(f0 + 5 * N, make_double2(kez.y, -kez.x));
+    Fo[pt] = make_double2(fma(-J0.x, iO, -kbx.y), fma(-J0.y, iO, kbx.x));
+    Fo[N + pt] = make_double2(fma(-J1.x, iO, -kby.y), fma(-J1.y, iO, kby.x));
+    Fo[2 * N + pt] = make_double2(fma(-J2.x, iO, -kbz.y), fma(-J2.y, iO, kbz.x));
+    Fo[3 * N + pt] = make_double2(kex.y, -kex.x);
+    Fo[4 * N + pt] = make_double2(key.y, -key.x);
+    Fo[5 * N + pt] = make_double2(kez.y, -kez.x);
   }
+  __syncthreads();
+#pragma unroll 1
+  for (int i = threadIdx.x; i < 6 * N; i += blockDim.x) epi((size_t)P.nc + i, i, Fo[i]);
 }
 
 // ------------------------------------------------------------------------

@@ -13,14 +13,14 @@ from dataclasses import dataclass
 def dopri8_vectors_per_step() -> int:
     """State-sized vectors read + written by one step attempt of the fused 1D1V stepper.
 
-    Stage i reads y and the K_j with a(i, j) != 0 (its input is formed while
-    gathering) and writes K_i; the finish kernel reads y and the K_j with
-    b_j != 0 or e_j != 0 and writes y_new."""
+    Stage i < 12 reads its input S_i, y and the K_j (j < i) with a(i+1, j) != 0
+    and writes K_i and S_{i+1} (stage 0: S_0 = y); the last stage reads S_12, y
+    and the K_j (j < 12) with b_j != 0 or e_j != 0 and writes K_12 and y_new."""
     from .tableau import A, B, E
-    total = 0
-    for i in range(13):
-        total += 1 + len(A.get(i, {})) + 1
-    total += 1 + sum(1 for b, e in zip(B, E) if b != 0 or e != 0) + 1
+    total = 3                                                   # stage 0: y; K_0, S_1
+    for i in range(1, 12):
+        total += 4 + sum(1 for j in A.get(i + 1, {}) if j < i)
+    total += 4 + sum(1 for j in range(12) if B[j] != 0 or E[j] != 0)
     return total
 
 

@@ -140,7 +140,7 @@ def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False, tar
     the tuned Plan (cached per problem and target).
 
     target "rhs" times the plain right-hand side; "dopri8" times fixed-step
-    Dopri8 attempts (13 gather-first stage kernels + finish), whose kernels
+    Dopri8 attempts (13 staged stage kernels), whose kernels
     balance shared memory and latency differently.  `sample` is the state to
     time with (an exactly Hermitian one selects the packed-transform stages);
     default: small random values."""
