@@ -261,52 +261,96 @@ __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __r
       for (int j = 0; j < M; ++j) per_line += (pair_limit(j, M, h, pcut) + 2) >> 1;
     }
     const int ntask = L.nl * per_line;
-    for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
-      const int l = t / per_line;
-      int r = t - l * per_line;
-      int j, kmax;
-      if (!prune_out) {
-        const int pj = (h + 2) >> 1;
-        j = r / pj;
-        r -= j * pj;
-        kmax = h;
-      } else {
-        j = 0;
-        kmax = pair_limit(0, M, h, pcut);
-        int c = (kmax + 2) >> 1;
-        while (r >= c) { r -= c; ++j; kmax = pair_limit(j, M, h, pcut); c = (kmax + 2) >> 1; }
+    // Work goes out per warp: full warps take 32 tasks, one lane each; the
+    // remainder (rem < 32 tasks) shares one warp, each task's sum over q split
+    // over G lanes (G a power of two, G * rem <= 32) and reduced by shuffles, so
+    // that a nearly empty warp does not cost a full task loop.  FP64 issue is
+    // per warp instruction, whatever the number of active lanes.
+    const int nfw = ntask >> 5;
+    const int rem = ntask - (nfw << 5);
+    int G = 1;
+    if (rem > 0 && rem <= 16) {
+      G = 32 / rem;
+      while (G & (G - 1)) G &= G - 1;
+    }
+    const int units = nfw + (rem > 0 ? 1 : 0);
+    const int lane = threadIdx.x & 31;
+    for (int u = threadIdx.x >> 5; u < units; u += blockDim.x >> 5) {
+      const bool split = u == nfw;                     // the remainder warp
+      const int Gu = split ? G : 1;
+      const int t = split ? (nfw << 5) + lane / Gu : (u << 5) + lane;
+      const int g = split ? lane % Gu : 0;
+      const bool active = split ? (lane / Gu) < rem : true;
+      double2 A0 = make_double2(0.0, 0.0), A1 = A0, B0 = A0, B1 = A0;
+      int l = 0, j = 0, kk0 = 0, kk1 = 0;
+      bool two = false;
+      if (active) {
+        l = t / per_line;
+        int r = t - l * per_line;
+        int kmax;
+        if (!prune_out) {
+          const int pj = (h + 2) >> 1;
+          j = r / pj;
+          r -= j * pj;
+          kmax = h;
+        } else {
+          j = 0;
+          kmax = pair_limit(0, M, h, pcut);
+          int c = (kmax + 2) >> 1;
+          while (r >= c) { r -= c; ++j; kmax = pair_limit(j, M, h, pcut); c = (kmax + 2) >> 1; }
+        }
+        kk0 = 2 * r;
+        two = kk0 + 1 <= kmax;
+        kk1 = two ? kk0 + 1 : kk0;
+        const int b = L.base(l);
+        const int k = j % Ns;
+        const int idx = (j / Ns) * Ns * R + k;
+        const int qmax = (!DIF && pcut >= 0) ? pair_limit(j, M, h, pcut) : h;
+        const int s0 = DIF ? Ns : M;                    // input stride between q's
+        const int i0 = DIF ? idx : j;                   // input position of q = 0
+        int q0 = 1, q1 = qmax;
+        if (Gu > 1) {
+          const int seg = (qmax + Gu - 1) / Gu;
+          q0 = 1 + g * seg;
+          q1 = min(qmax, (g + 1) * seg);
+        }
+        if (g == 0) { A0 = in[b + i0 * L.es]; A1 = A0; }
+        int ang0 = ((q0 - 1) * kk0) % R, ang1 = ((q0 - 1) * kk1) % R;   // (q * kk) mod R
+        for (int q = q0; q <= q1; ++q) {
+          ang0 += kk0;
+          if (ang0 >= R) ang0 -= R;
+          ang1 += kk1;
+          if (ang1 >= R) ang1 -= R;
+          const double2 aq = in[b + (i0 + q * s0) * L.es];
+          const double2 bq = in[b + (i0 + (R - q) * s0) * L.es];
+          const double2 c0 = cs[ang0], c1 = cs[ang1];
+          A0 = crfma(c0.x, aq, A0);
+          B0 = crfma(c0.y, bq, B0);
+          A1 = crfma(c1.x, aq, A1);
+          B1 = crfma(c1.y, bq, B1);
+        }
       }
-      const int kk0 = 2 * r;
-      const bool two = kk0 + 1 <= kmax;
-      const int kk1 = two ? kk0 + 1 : kk0;
+      if (Gu > 1) {
+        for (int off = Gu >> 1; off > 0; off >>= 1) {
+          A0.x += __shfl_down_sync(0xffffffffu, A0.x, off);
+          A0.y += __shfl_down_sync(0xffffffffu, A0.y, off);
+          B0.x += __shfl_down_sync(0xffffffffu, B0.x, off);
+          B0.y += __shfl_down_sync(0xffffffffu, B0.y, off);
+          A1.x += __shfl_down_sync(0xffffffffu, A1.x, off);
+          A1.y += __shfl_down_sync(0xffffffffu, A1.y, off);
+          B1.x += __shfl_down_sync(0xffffffffu, B1.x, off);
+          B1.y += __shfl_down_sync(0xffffffffu, B1.y, off);
+        }
+      }
+      if (!active || g != 0) continue;
       const int b = L.base(l);
       const int k = j % Ns;
       const int idx = (j / Ns) * Ns * R + k;
-      const int qmax = (!DIF && pcut >= 0) ? pair_limit(j, M, h, pcut) : h;
-      const int s0 = DIF ? Ns : M;                    // input stride between q's
-      const int i0 = DIF ? idx : j;                   // input position of q = 0
-      const double2 x0 = in[b + i0 * L.es];
-      double2 A0 = x0, A1 = x0;
-      double2 B0 = make_double2(0.0, 0.0), B1 = make_double2(0.0, 0.0);
-      int ang0 = 0, ang1 = 0;   // (q * kk) mod R
-      for (int q = 1; q <= qmax; ++q) {
-        ang0 += kk0;
-        if (ang0 >= R) ang0 -= R;
-        ang1 += kk1;
-        if (ang1 >= R) ang1 -= R;
-        const double2 aq = in[b + (i0 + q * s0) * L.es];
-        const double2 bq = in[b + (i0 + (R - q) * s0) * L.es];
-        const double2 c0 = cs[ang0], c1 = cs[ang1];
-        A0 = crfma(c0.x, aq, A0);
-        B0 = crfma(c0.y, bq, B0);
-        A1 = crfma(c1.x, aq, A1);
-        B1 = crfma(c1.y, bq, B1);
-      }
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (u == 1 && !two) break;
-        const int kk = u ? kk1 : kk0;
-        const double2 A = u ? A1 : A0, B = u ? B1 : B0;
+      for (int uu = 0; uu < 2; ++uu) {
+        if (uu == 1 && !two) break;
+        const int kk = uu ? kk1 : kk0;
+        const double2 A = uu ? A1 : A0, B = uu ? B1 : B0;
         // forward: X_kk = A - iB, X_{R-kk} = A + iB ; inverse: signs swapped
         const double2 iB = INV ? make_double2(-B.y, B.x) : make_double2(B.y, -B.x);
         double2 X1 = cadd(A, iB), X2 = csub(A, iB);

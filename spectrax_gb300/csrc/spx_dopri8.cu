@@ -301,6 +301,19 @@ struct EpiNext {
   }
   __device__ __forceinline__ void operator()(size_t e, int il, double2 v) const {
     Ki[e] = v;
+    Snext[e] = next(e, il, v);
+  }
+  // exactly Hermitian operands: the mirrored entry e2 gets the conjugates
+  __device__ __forceinline__ void pair(size_t e, int il, size_t e2, int il2, double2 v, bool two) const {
+    const double2 sn = next(e, il, v);
+    Ki[e] = v;
+    Snext[e] = sn;
+    if (two) {
+      Ki[e2] = make_double2(v.x, -v.y);
+      Snext[e2] = make_double2(sn.x, -sn.y);
+    }
+  }
+  __device__ __forceinline__ double2 next(size_t e, int il, double2 v) const {
     const int n = T->n;
     double2 acc;
     if (npf > n) {                       // every operand staged
@@ -320,7 +333,7 @@ struct EpiNext {
           if (r + u < n) acc = crfma(T->c[r + u], k[u], acc);
       }
     }
-    Snext[e] = crfma(T->cself, v, acc);
+    return crfma(T->cself, v, acc);
   }
 };
 
@@ -340,6 +353,8 @@ struct EpiFinal {
   int adaptive;
   double sq;
   int nonfinite;
+  double2 last_yn;
+  double last_sq;
   __device__ bool prepare() const {
     if (!bar) return true;
     const bool ok = mbar_wait_bounded(bar, 0);
@@ -380,12 +395,25 @@ struct EpiFinal {
     yn = crfma(T->cself, v, yn);
     er = crfma(T->eself, v, er);
     Ynew[e] = yn;
+    last_yn = yn;
     if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
     if (adaptive) {
+      // |err / (atol + rtol max(|y0|, |y1|))|^2 with one division per entry
       const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
-      const double sc = fma(rtol, sqrt(fmax(m0, m1)), atol);
-      const double rx = er.x / sc, ry = er.y / sc;
-      sq = fma(rx, rx, fma(ry, ry, sq));
+      const double inv = 1.0 / fma(rtol, sqrt(fmax(m0, m1)), atol);
+      const double rx = er.x * inv, ry = er.y * inv;
+      last_sq = fma(rx, rx, ry * ry);
+      sq += last_sq;
+    }
+  }
+  // exactly Hermitian operands: the mirrored entry has the conjugate y_new and
+  // the same error contribution
+  __device__ __forceinline__ void pair(size_t e, int il, size_t e2, int il2, double2 v, bool two) {
+    (*this)(e, il, v);
+    if (two) {
+      Ki[e2] = make_double2(v.x, -v.y);
+      Ynew[e2] = make_double2(last_yn.x, -last_yn.y);
+      if (adaptive) sq += last_sq;
     }
   }
 };
@@ -461,7 +489,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
       maxwell1v_g(P, stab, SrcPlain{in}, sA, epi);
     } else {
       EpiFinal el{Ki, pick(a.Y, s.cur ^ 1), Y, a.K, len, &terms, nullptr, 0, 0, nullptr,
-                  s.rtol, s.atol, s.adaptive, 0.0, 0};
+                  s.rtol, s.atol, s.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
       maxwell1v_g(P, stab, SrcPlain{in}, sA, el);
       last_stage_tail(a, at, el, red);
     }
@@ -525,7 +553,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
     else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
   } else {
     EpiFinal el{Ki, pick(a.Y, s.cur ^ 1), Y, a.K, len, &terms, pf, own, npf, &bars[1],
-                s.rtol, s.atol, s.adaptive, 0.0, 0};
+                s.rtol, s.atol, s.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
     if (s.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
     else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
     last_stage_tail(a, at, el, red);

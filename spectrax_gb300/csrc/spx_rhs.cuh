@@ -145,9 +145,12 @@ __device__ __forceinline__ void rhs1v_tile(const DevPlan& P, const double2* __re
 // line, so G(x) and C_{n-1}(x) are real and two real lines share one complex
 // transform: the inverse FFT of X_a + i X_b gives x_a + i x_b, and the forward
 // FFT W of p_a + i p_b gives P_a(k) = (W(k) + conj W(-k)) / 2 and
-// P_b(k) = -i (W(k) - conj W(-k)) / 2 -- half the transforms.  Every output is
-// formed from k and -k by mirrored operations, so the result is again exactly
-// Hermitian and the property holds along a Runge-Kutta trajectory.
+// P_b(k) = -i (W(k) - conj W(-k)) / 2 -- half the transforms.  Only the k <= 0
+// half of each output plane is evaluated: the epilogue's
+// pair(e, il, e2, il2, v, two) stores v at e and, when two, conj(v) at the
+// mirrored entry e2 (its own operands being exactly Hermitian, everything it
+// derives from them is too), so the property holds along a Runge-Kutta
+// trajectory.
 // sA / sB: (nt+1)*N double2 each; scoef: 4*nt doubles.
 // ------------------------------------------------------------------------
 template <bool HERM, class Epi>
@@ -231,8 +234,11 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
   if (!epi.prepare()) return;
   const double ua = u0 / a0;
   const double Dd = P.pb.D;
-  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
+  // HERM: only the k <= 0 half (c <= centre) is evaluated; the epilogue's
+  // pair() also writes the conjugates at the mirrored entries
+  const int Nc = HERM ? (N + 1) / 2 : N;
+  for (int i = threadIdx.x; i < nt * Nc; i += blockDim.x) {
+    const int l = i / Nc, c = i - l * Nc;
     const int n = n0 + l;
     const double* cf = scoef + 4 * l;
     const double2 kt = ktab(P, tab, 1, c);
@@ -258,7 +264,13 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
       re = fma(cf[2], nl2.x, re);
       im = fma(cf[2], nl2.y, im);
     }
-    epi(sbase + (size_t)n * N + c, i, make_double2(re, im));
+    const size_t e = sbase + (size_t)n * N + c;
+    if constexpr (!HERM) {
+      epi(e, l * N + c, make_double2(re, im));
+    } else {
+      const int c2 = N - 1 - c;
+      epi.pair(e, l * N + c, sbase + (size_t)n * N + c2, l * N + c2, make_double2(re, im), c2 != c);
+    }
   }
 }
 
