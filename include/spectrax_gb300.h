@@ -233,12 +233,16 @@ typedef struct spx_batch_opts {
   int32_t cluster;       /* CTAs per instance, 1..8 */
   int32_t tile;          /* Hermite planes per tile (0: 8) */
   const double* masses;  /* host, n x SPX_MAX_SPECIES species masses (NULL: ones) */
+  int32_t hermitian;     /* 1: an instance with odd Nx whose initial state is exactly Hermitian
+                            (C(-k) == conj C(k) on every line) uses packed real transforms */
 } spx_batch_opts;
 
 typedef struct spx_batch_stats {
   double t, dt;
   int64_t accepted, rejected, rhs_evals;
   int32_t status, saved;
+  int32_t hermitian;     /* 1 if the instance ran with packed real transforms */
+  int32_t pad;
 } spx_batch_stats;
 
 typedef struct spx_batch spx_batch;

@@ -74,6 +74,7 @@ class spx_batch_opts(C.Structure):
         ("save_ts", C.POINTER(C.c_double)),
         ("cluster", C.c_int32), ("tile", C.c_int32),
         ("masses", C.POINTER(C.c_double)),
+        ("hermitian", C.c_int32),
     ]
 
 
@@ -82,6 +83,7 @@ class spx_batch_stats(C.Structure):
         ("t", C.c_double), ("dt", C.c_double),
         ("accepted", C.c_int64), ("rejected", C.c_int64), ("rhs_evals", C.c_int64),
         ("status", C.c_int32), ("saved", C.c_int32),
+        ("hermitian", C.c_int32), ("pad", C.c_int32),
     ]
 
 

@@ -64,7 +64,7 @@ def landau_scan(n=256, seed=0, amplitude=0.01, mask_mode="divide"):
 # ----------------------------------------------------------------- solver
 class BatchSolver:
     def __init__(self, problems, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, adaptive=True,
-                 max_steps=10_000_000, cluster=2, tile=8, masses=None, device=None):
+                 max_steps=10_000_000, cluster=2, tile=8, masses=None, device=None, hermitian=True):
         L = _lib.lib()
         self.n = len(problems)
         self.problems = list(problems)
@@ -85,6 +85,8 @@ class BatchSolver:
         o.cluster = int(cluster)
         o.tile = int(tile)
         o.masses = self._masses.ctypes.data_as(C.POINTER(C.c_double))
+        # instances with odd Nx and an exactly Hermitian y0 use packed real transforms
+        o.hermitian = 1 if hermitian else 0
         self.cluster, self.tile = int(cluster), int(tile)
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         h = C.c_void_p()
@@ -122,7 +124,7 @@ class BatchSolver:
                                                 _stream_ptr()), "spx_batch_results")
         torch.cuda.current_stream().synchronize()
         stats = [dict(t=s.t, dt=s.dt, accepted=s.accepted, rejected=s.rejected, rhs_evals=s.rhs_evals,
-                      status=s.status, saved=s.saved) for s in st]
+                      status=s.status, saved=s.saved, hermitian=bool(s.hermitian)) for s in st]
         energies = []
         for i in range(self.n):
             w = 2 + self.problems[i].Ns

@@ -8,7 +8,10 @@
 // the scaled error of a step is reduced through distributed shared memory and
 // every CTA runs the same controller on the same numbers, so no extra
 // broadcast is needed.  Stage data written by one CTA and read by another in
-// the same launch is loaded with ld.global.cg (L2-coherent).
+// the same launch is loaded with ld.global.cg (L2-coherent).  A tile's input
+// planes are staged in shared memory before its transforms; an instance whose
+// initial state is exactly Hermitian (odd Nx) runs the packed real-transform
+// tiles, which keep that symmetry exactly.
 //
 // Instances may differ in Nx, Nn, Ns, L, nu, alpha, u (spectrax's Landau scan:
 // Examples/1D_Landau_damping_dr_curve.py:149-175 loops over k serially).
@@ -42,6 +45,8 @@ struct BInst {
   double t, dt;          // results
   long long accepted, rejected, evals;
   int status, saved;
+  int herm_ok;           // odd Nx with an antisymmetric wavenumber table, and requested
+  int herm;              // result: y0 was exactly Hermitian, packed real transforms used
 };
 
 struct BArgs {
@@ -60,63 +65,143 @@ struct BArgs {
   const int* order;
   unsigned int* next;
   int tab_max;
-  int lines_max;          // double2 entries of each of the two line buffers
+  int work_max;           // double2 entries of the per-tile work area (line buffers, staged planes)
 };
 
 struct Ctl {
   double t, dt;
   long long acc, rej, evals;
-  int cur, k1_valid, isave, status, saved, pad;
+  int cur, k1_valid, isave, status, saved, herm;
 };
 
-struct EpiStageB {
+// Epilogue term list of one stage (see the single-instance solver): stage i < 12
+// forms y + h sum_j a(i+1, j) K_j over j < i with a(i+1, j) != 0, then
+// + h a(i+1, i) K_i; the last stage forms y_new and the error over j < 12 with
+// b_j != 0 or e_j != 0.  Ascending j.
+struct BTerms {
+  int n;
+  int j[12];
+  double c[12], e[12];
+  double cself, eself;
+};
+
+__device__ void fill_bterms(BTerms& T, int stage, double h) {
+  const bool last = stage == rk::S - 1;
+  const int row = last ? 12 : stage;
+  const int mask = last ? (bMask[12] | bMask[13]) : bMask[row];
+  T.n = 0;
+  for (int j = 0; j < stage; ++j)
+    if (mask & (1 << j)) {
+      T.j[T.n] = j;
+      T.c[T.n] = h * bCoef[row][j];
+      T.e[T.n] = last ? h * bCoef[13][j] : 0.0;
+      ++T.n;
+    }
+  T.cself = h * bCoef[row][stage];
+  T.eself = last ? h * bCoef[13][stage] : 0.0;
+}
+
+// Source of a tile's stage input written earlier in this launch (L2-coherent loads).
+struct SrcCG {
+  const double2* y;
+  __device__ __forceinline__ double2 operator()(size_t e) const { return __ldcg(y + e); }
+};
+
+// Stages 0..11: store K_i and the next stage input; operands from global memory
+// (written earlier in this launch: ld.global.cg), up to five loads in flight.
+struct EpiNextB {
+  double2* __restrict__ Ki;
+  double2* __restrict__ Snext;
   const double2* Y;
-  double2* K;
-  double2* Snext;
+  const double2* K;
   long long len;
-  int stage;
-  double h;
-  __device__ __forceinline__ void operator()(size_t e, double2 v) const {
-    K[(size_t)stage * len + e] = v;
+  const BTerms* T;
+  __device__ bool prepare() const { return true; }
+  __device__ __forceinline__ double2 next(size_t e, double2 v) const {
     double2 acc = __ldcg(Y + e);
-    const int mask = bMask[stage];
-    for (int j = 0; j < stage; ++j)
-      if (mask & (1 << j)) acc = crfma(h * bCoef[stage][j], __ldcg(K + (size_t)j * len + e), acc);
-    acc = crfma(h * bCoef[stage][stage], v, acc);
-    Snext[e] = acc;
+    const int n = T->n;
+#pragma unroll 1
+    for (int r = 0; r < n; r += 5) {
+      double2 k[5];
+#pragma unroll
+      for (int u = 0; u < 5; ++u)
+        if (r + u < n) k[u] = __ldcg(K + (size_t)T->j[r + u] * len + e);
+#pragma unroll
+      for (int u = 0; u < 5; ++u)
+        if (r + u < n) acc = crfma(T->c[r + u], k[u], acc);
+    }
+    return crfma(T->cself, v, acc);
+  }
+  __device__ __forceinline__ void operator()(size_t e, int, double2 v) const {
+    Ki[e] = v;
+    Snext[e] = next(e, v);
+  }
+  __device__ __forceinline__ void pair(size_t e, int, size_t e2, int, double2 v, bool two) const {
+    const double2 sn = next(e, v);
+    Ki[e] = v;
+    Snext[e] = sn;
+    if (two) {
+      Ki[e2] = make_double2(v.x, -v.y);
+      Snext[e2] = make_double2(sn.x, -sn.y);
+    }
   }
 };
 
-struct EpiLastB {
+// Last stage: y_new, scaled error, non-finite flag.
+struct EpiFinalB {
+  double2* __restrict__ Ki;
+  double2* __restrict__ Ynew;
   const double2* Y;
   const double2* K;
-  double2* Ynew;
   long long len;
-  double h, rtol, atol;
+  const BTerms* T;
+  double rtol, atol;
   int adaptive;
   double sq;
   int nonfinite;
-  __device__ __forceinline__ void operator()(size_t e, double2 v) {
+  __device__ bool prepare() const { return true; }
+  __device__ __forceinline__ double finish(size_t e, double2 v, double2& yn) {
     const double2 y0 = __ldcg(Y + e);
-    double2 yn = y0, er = make_double2(0.0, 0.0);
-    const int mb = bMask[12], me = bMask[13];
-    for (int j = 0; j < 12; ++j) {
-      const bool ub = mb & (1 << j), ue = me & (1 << j);
-      if (ub || ue) {
-        const double2 kj = __ldcg(K + (size_t)j * len + e);
-        if (ub) yn = crfma(h * bCoef[12][j], kj, yn);
-        if (ue) er = crfma(h * bCoef[13][j], kj, er);
-      }
+    yn = y0;
+    double2 er = make_double2(0.0, 0.0);
+    const int n = T->n;
+#pragma unroll 1
+    for (int r = 0; r < n; r += 5) {
+      double2 k[5];
+#pragma unroll
+      for (int u = 0; u < 5; ++u)
+        if (r + u < n) k[u] = __ldcg(K + (size_t)T->j[r + u] * len + e);
+#pragma unroll
+      for (int u = 0; u < 5; ++u)
+        if (r + u < n) {
+          yn = crfma(T->c[r + u], k[u], yn);
+          er = crfma(T->e[r + u], k[u], er);
+        }
     }
-    yn = crfma(h * bCoef[12][12], v, yn);
-    er = crfma(h * bCoef[13][12], v, er);
-    Ynew[e] = yn;
+    yn = crfma(T->cself, v, yn);
+    er = crfma(T->eself, v, er);
     if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
-    if (adaptive) {
-      const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
-      const double sc = fma(rtol, sqrt(fmax(m0, m1)), atol);
-      const double rx = er.x / sc, ry = er.y / sc;
-      sq = fma(rx, rx, fma(ry, ry, sq));
+    if (!adaptive) return 0.0;
+    const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
+    const double inv = 1.0 / fma(rtol, sqrt(fmax(m0, m1)), atol);
+    const double rx = er.x * inv, ry = er.y * inv;
+    return fma(rx, rx, ry * ry);
+  }
+  __device__ __forceinline__ void operator()(size_t e, int, double2 v) {
+    double2 yn;
+    sq += finish(e, v, yn);
+    Ki[e] = v;
+    Ynew[e] = yn;
+  }
+  __device__ __forceinline__ void pair(size_t e, int, size_t e2, int, double2 v, bool two) {
+    double2 yn;
+    const double c = finish(e, v, yn);
+    sq += two ? c + c : c;
+    Ki[e] = v;
+    Ynew[e] = yn;
+    if (two) {
+      Ki[e2] = make_double2(v.x, -v.y);
+      Ynew[e2] = make_double2(yn.x, -yn.y);
     }
   }
 };
@@ -176,11 +261,12 @@ __global__ void __launch_bounds__(NTHREADS) k_batch(BArgs a) {
   __shared__ int s_inst;
   __shared__ double s_part[2];
   __shared__ double red[NTHREADS / 32];
+  __shared__ BTerms terms;
+  __shared__ int s_bad;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
-  double2* sA = stab + (a.tab_max + 15) / 16 * 16;
-  double2* sB = sA + a.lines_max;
-  double* scoef = reinterpret_cast<double*>(sB + a.lines_max);
+  double2* sA = stab + (a.tab_max + 15) / 16 * 16;        // per-tile work area (work_max entries)
+  double* scoef = reinterpret_cast<double*>(sA + a.work_max);
 
   for (;;) {
     if (crank == 0 && threadIdx.x == 0) {
@@ -208,8 +294,28 @@ __global__ void __launch_bounds__(NTHREADS) k_batch(BArgs a) {
       ctl.t = 0.0; ctl.dt = a.dt0; ctl.acc = ctl.rej = ctl.evals = 0;
       ctl.cur = 0; ctl.k1_valid = 0; ctl.isave = 0; ctl.status = SPX_ST_RUNNING; ctl.saved = 0;
       if (0.0 >= a.t1) ctl.status = SPX_ST_DONE;
+      s_bad = 0;
+    }
+    __syncthreads();
+    // exact Hermitian test of y0 (every line of N entries: y(N-1-c) == conj y(c)),
+    // each rank a slice, combined over the cluster through distributed shared memory
+    if (I->herm_ok) {
+      int bad = 0;
+      for (long long i = (long long)crank * blockDim.x + threadIdx.x; i < len; i += (long long)C * blockDim.x) {
+        const long long l = i / N;
+        const int c = (int)(i - l * N);
+        const double2 u = __ldcg(a.y_in + I->y_off + i), v = __ldcg(a.y_in + I->y_off + l * N + (N - 1 - c));
+        if (!(u.x == v.x && u.y == -v.y)) bad = 1;
+      }
+      if (__syncthreads_or(bad) && threadIdx.x == 0) s_bad = 1;
     }
     __threadfence();
+    cl.sync();
+    if (threadIdx.x == 0) {
+      int any = I->herm_ok ? 0 : 1;
+      for (int r = 0; r < C; ++r) any |= *cl.map_shared_rank(&s_bad, r);
+      ctl.herm = any ? 0 : 1;
+    }
     cl.sync();
     // a save time at t0 = 0 is taken from y0
     {
@@ -243,45 +349,61 @@ __global__ void __launch_bounds__(NTHREADS) k_batch(BArgs a) {
       }
       const int cur = ctl.cur;
       const double2* Y = Yb[cur];
+      const bool herm = ctl.herm != 0;
       for (int stage = 0; stage < rk::S; ++stage) {
         const double2* in = (stage == 0) ? Y : Sb[stage & 1];
-        if (stage < rk::S - 1) {
-          EpiStageB epi{Y, K, Sb[(stage + 1) & 1], len, stage, h};
-          for (int t = crank; t < ntiles_all; t += C) {
-            if (t == ntiles_all - 1) {
-              if (stage == 0 && ctl.k1_valid) {
-                for (int i = threadIdx.x; i < 6 * N; i += blockDim.x) {
-                  const size_t e = (size_t)P.nc + i;
-                  epi(e, __ldcg(K + e));
-                }
-              } else {
-                maxwell_range<EpiStageB, LdCG>(P, stab, in, 0, P.plane, epi);
+        if (threadIdx.x == 0) fill_bterms(terms, stage, h);
+        __syncthreads();
+        double2* Ki = K + (size_t)stage * len;
+        // one tile of this stage: the field tile (Maxwell + current) or Hermite
+        // planes n0 .. n0+nt of species sp, staged into shared memory first
+        auto run_tile = [&](int t, auto& epi) {
+          if (t == ntiles_all - 1) {
+            if (stage == 0 && ctl.k1_valid) {
+              for (int i = threadIdx.x; i < 6 * N; i += blockDim.x) {
+                const size_t e = (size_t)P.nc + i;
+                epi(e, i, __ldcg(Ki + e));
               }
             } else {
-              const int s = t / P.ntiles, tile = t % P.ntiles;
-              const int n0 = tile * P.tile, nt = min(P.tile, P.pb.Nn - n0);
-              if (nt <= 0) continue;
-              if (stage == 0 && ctl.k1_valid) {
-                const size_t b0 = ((size_t)s * P.pb.Nn + n0) * N;
-                for (int i = threadIdx.x; i < nt * N; i += blockDim.x) epi(b0 + i, __ldcg(K + b0 + i));
-              } else {
-                rhs1v_tile_t<false, EpiStageB, LdCG>(P, stab, in, in, s, n0, nt, sA, sB, scoef, epi);
-              }
+              maxwell1v_g(P, stab, SrcCG{in}, sA, epi);
             }
+            return;
+          }
+          const int sp = t / P.ntiles, n0 = (t % P.ntiles) * P.tile, nt = min(P.tile, P.pb.Nn - n0);
+          if (nt <= 0) return;
+          const size_t sbase = (size_t)sp * P.pb.Nn * N;
+          if (stage == 0 && ctl.k1_valid) {
+            const size_t b0 = sbase + (size_t)n0 * N;
+            for (int i = threadIdx.x; i < nt * N; i += blockDim.x) epi(b0 + i, i, __ldcg(Ki + b0 + i));
+            return;
+          }
+          double2* tB = sA + (size_t)(P.tile + 1) * N;
+          double2* U = tB + (size_t)(P.tile + 1) * N;
+          double2* F3 = U + (size_t)(P.tile + 2) * N;
+          for (int i = threadIdx.x; i < (nt + 2) * N; i += blockDim.x) {
+            const int n = n0 - 1 + i / N;
+            U[i] = (n >= 0 && n < P.pb.Nn) ? __ldcg(in + sbase + (size_t)n * N + (i % N)) : make_double2(0.0, 0.0);
+          }
+          for (int i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+            const int q = i / N;        // E_x, B_z, B_y
+            F3[i] = __ldcg(in + P.nc + (size_t)(q == 0 ? 0 : (q == 1 ? 5 : 4)) * N + (i % N));
+          }
+          __syncthreads();
+          if (herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, tB, scoef, epi);
+          else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, tB, scoef, epi);
+        };
+        if (stage < rk::S - 1) {
+          EpiNextB epi{Ki, Sb[(stage + 1) & 1], Y, K, len, &terms};
+          for (int t = crank; t < ntiles_all; t += C) {
+            run_tile(t, epi);
             __syncthreads();
           }
           __threadfence();
           cl.sync();
         } else {
-          EpiLastB el{Y, K, Yb[cur ^ 1], len, h, a.rtol, a.atol, a.adaptive, 0.0, 0};
+          EpiFinalB el{Ki, Yb[cur ^ 1], Y, K, len, &terms, a.rtol, a.atol, a.adaptive, 0.0, 0};
           for (int t = crank; t < ntiles_all; t += C) {
-            if (t == ntiles_all - 1) {
-              maxwell_range<EpiLastB, LdCG>(P, stab, in, 0, P.plane, el);
-            } else {
-              const int s = t / P.ntiles, tile = t % P.ntiles;
-              const int n0 = tile * P.tile, nt = min(P.tile, P.pb.Nn - n0);
-              if (nt > 0) rhs1v_tile_t<false, EpiLastB, LdCG>(P, stab, in, in, s, n0, nt, sA, sB, scoef, el);
-            }
+            run_tile(t, el);
             __syncthreads();
           }
           const double q1 = bsum(el.sq, red);
@@ -352,7 +474,7 @@ __global__ void __launch_bounds__(NTHREADS) k_batch(BArgs a) {
       a.y_out[I->y_off + i] = __ldcg(Yf + i);
     if (crank == 0 && threadIdx.x == 0) {
       I->t = ctl.t; I->dt = ctl.dt; I->accepted = ctl.acc; I->rejected = ctl.rej;
-      I->evals = ctl.evals; I->status = ctl.status; I->saved = ctl.saved;
+      I->evals = ctl.evals; I->status = ctl.status; I->saved = ctl.saved; I->herm = ctl.herm;
     }
     __syncthreads();
   }
@@ -455,7 +577,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   b->nsave = o->nsave;
   std::vector<double2> tab;
   std::vector<double> cost(n);
-  int tab_max = 0, lines_max = 0;
+  int tab_max = 0, work_max = 0;
   long long pool = 0, yoff = 0;
   int en_off = 0;
   b->hinst.resize(n);
@@ -483,7 +605,15 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     I.tab_off = (int)tab.size();
     tab.insert(tab.end(), tmp.tab.begin(), tmp.tab.end());
     tab_max = std::max(tab_max, I.P.tab_len);
-    lines_max = std::max(lines_max, (T + 1) * p.Nx);
+    // work area: two line buffers (T+1 lines), staged planes (T+2), field lines (3);
+    // the field tile reuses it for its (2 Ns + 12)-line gather + output area
+    work_max = std::max(work_max, std::max(2 * (T + 1) + (T + 2) + 3, 2 * p.Ns + 12) * p.Nx);
+    if (o->hermitian && (p.Nx & 1)) {
+      bool anti = true;
+      for (int c = 0; c < p.Nx; ++c)
+        if (!(tmp.tab[I.P.ax[1].kofs + c].x == -tmp.tab[I.P.ax[1].kofs + p.Nx - 1 - c].x)) anti = false;
+      I.herm_ok = anti ? 1 : 0;
+    }
     I.len = (long long)I.P.nc + 6LL * I.P.plane;
     I.pool_off = pool;
     pool += 17 * ((I.len + 15) / 16 * 16);
@@ -505,7 +635,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
-  b->smem = ((size_t)tab_max * sizeof(double2) + 255) / 256 * 256 + 2 * (size_t)lines_max * sizeof(double2) +
+  b->smem = ((size_t)tab_max * sizeof(double2) + 255) / 256 * 256 + (size_t)work_max * sizeof(double2) +
             16 * 4 * sizeof(double);
   const int optin = smem_optin();
   cudaFuncAttributes fa;
@@ -567,7 +697,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   A.t1 = o->t1; A.dt0 = o->dt0; A.rtol = o->rtol; A.atol = o->atol;
   A.max_steps = o->max_steps; A.adaptive = o->adaptive ? 1 : 0;
   A.tab_max = tab_max;
-  A.lines_max = lines_max;
+  A.work_max = work_max;
   b->y_in = const_cast<double2*>(A.y_in);
   b->y_out = A.y_out;
   e = cudaMemcpy(A.inst, b->hinst.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice);
@@ -617,6 +747,7 @@ int spx_batch_results(spx_batch* b, spx_batch_stats* stats, double* energies, vo
       stats[i].t = h[i].t; stats[i].dt = h[i].dt;
       stats[i].accepted = h[i].accepted; stats[i].rejected = h[i].rejected; stats[i].rhs_evals = h[i].evals;
       stats[i].status = h[i].status; stats[i].saved = h[i].saved;
+      stats[i].hermitian = h[i].herm; stats[i].pad = 0;
     }
   }
   return SPX_OK;

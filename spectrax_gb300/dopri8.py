@@ -114,6 +114,108 @@ class Dopri8Solver:
             self.handle = None
 
 
+# Diffrax PIDController defaults, the same as the device controller (csrc/spx_tableau.cuh)
+_SAFETY, _FACTORMIN, _FACTORMAX, _EXPONENT, _SNAP = 0.9, 0.2, 10.0, -1.0 / 8.0, 1e-9
+
+
+def _controller_factor(en: float, accepted: bool) -> float:
+    if en == 0.0:
+        f = _FACTORMAX
+    elif not np.isfinite(en):
+        f = _FACTORMIN
+    else:
+        f = _SAFETY * en ** _EXPONENT
+    return min(max(f, 1.0 if accepted else _FACTORMIN), _FACTORMAX)
+
+
+def host_dopri8_solve(plan: Plan, y0, t1: float, dt0: float, ts=None, adaptive=True, rtol=1e-10,
+                      atol=1e-12, max_steps=1_000_000, stream=None):
+    """Dopri8 driven from the host around the plain right-hand side ``plan.rhs_into``.
+
+    This is how an external solver uses the drop-in vector field (the role
+    Diffrax plays for spectrax/_simulation.py:164-180): one RHS launch per
+    stage, the stage combinations as separate device operations, and the
+    step-size decision on the host after each attempt (one device-to-host read
+    per step).  Same tableau, controller and save-time rule as the device
+    solver.  Returns (final state, saved states (len(ts), n), stats dict)."""
+    from .tableau import A, B, E
+    y = torch.as_tensor(y0).to(plan.device, torch.complex128).contiguous().clone()
+    plan.check_state(y, "y0")
+    ts = np.asarray([] if ts is None else ts, np.float64)
+    K = [torch.empty_like(y) for _ in range(13)]
+    S = torch.empty_like(y)
+    ynew = torch.empty_like(y)
+    err = torch.empty_like(y)
+    saved = torch.empty((len(ts), y.numel()), dtype=torch.complex128, device=y.device)
+    t, dt = 0.0, float(dt0)
+    isave = 0
+    while isave < len(ts) and ts[isave] <= t:
+        saved[isave].copy_(y)
+        isave += 1
+    acc = rej = evals = 0
+    k1_valid = False
+    status = "DONE" if t >= t1 else "RUNNING"
+    while status == "RUNNING":
+        t_stop = min(ts[isave], t1) if isave < len(ts) else t1
+        h, landed = dt, False
+        if t + h * (1.0 + _SNAP) >= t_stop:
+            h, landed = t_stop - t, True
+        if h <= 0.0 or t + h == t:
+            status = "DT_UNDERFLOW"
+            break
+        if acc + rej >= max_steps:
+            status = "MAX_STEPS"
+            break
+        for i in range(13):
+            if i == 0:
+                if not k1_valid:
+                    plan.rhs_into(y, K[0], stream)
+                continue
+            S.copy_(y)
+            for j, a in A[i].items():
+                S.add_(K[j], alpha=h * a)
+            plan.rhs_into(S, K[i], stream)
+        ynew.copy_(y)
+        err.zero_()
+        for j in range(13):
+            if B[j] != 0.0:
+                ynew.add_(K[j], alpha=h * B[j])
+            if E[j] != 0.0:
+                err.add_(K[j], alpha=h * E[j])
+        evals += 12 if k1_valid else 13
+        nonfinite = False
+        if adaptive:
+            # one device-to-host read per attempt: the error norm and the finiteness of y_new
+            sc = atol + rtol * torch.maximum(y.abs(), ynew.abs())
+            en_t = torch.sqrt(torch.mean((err.abs() / sc) ** 2))
+            bad = (~torch.isfinite(torch.view_as_real(ynew)).all()).to(torch.float64)
+            en, nf = torch.stack([en_t, bad]).tolist()
+            nonfinite = nf != 0.0
+            accept = en < 1.0
+            dt_next = h * _controller_factor(en, accept)
+            if accept and landed and dt_next < dt:
+                dt_next = dt
+        else:
+            accept, dt_next = True, dt
+        if accept:
+            t = t_stop if landed else t + h
+            y, ynew = ynew, y
+            acc += 1
+            k1_valid = False
+            while isave < len(ts) and ts[isave] <= t:
+                saved[isave].copy_(y)
+                isave += 1
+            if nonfinite:
+                status = "NONFINITE"
+            elif t >= t1:
+                status = "DONE"
+        else:
+            rej += 1
+            k1_valid = True
+        dt = dt_next
+    return y, saved, dict(t=t, dt=dt, accepted=acc, rejected=rej, rhs_evals=evals, status_name=status)
+
+
 def solve(params, y0=None, t_max=None, dt=None, ts=None, adaptive=True, rtol=None, atol=None,
           max_steps=1_000_000, save_states=True, mask_mode=None):
     """Integrate one instance; returns (solver, status)."""

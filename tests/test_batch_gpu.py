@@ -85,3 +85,35 @@ def test_batch_status_and_reuse():
         b.run(y0)
         stats, _ = b.results()
         assert all(s["status"] == 2 and s["accepted"] == 7 for s in stats)
+
+
+def _hermitian(y, Nx):
+    L = np.array(y, np.complex128).reshape(-1, Nx)
+    c0 = Nx // 2
+    L[:, c0] = L[:, c0].real
+    L[:, :c0] = np.conj(L[:, ::-1][:, :c0])
+    return L.ravel()
+
+
+@pytest.mark.gpu
+def test_batch_hermitian_instances():
+    # exactly Hermitian initial states (odd Nx) take the packed real-transform tiles
+    import torch
+    from spectrax_gb300.batch import BatchSolver, serial_solve
+    insts = _small_insts(7)
+    for it in insts:
+        it["y0"] = _hermitian(it["y0"], it["shape"][0])
+    ts = np.linspace(0, 1.0, 3)
+    ref_y, ref_st, ref_en, _ = serial_solve(insts, 1.0, dt0=0.01, rtol=1e-9, atol=1e-9, save_ts=ts)
+    for herm in (True, False):
+        b = BatchSolver([it["problem"] for it in insts], 1.0, dt0=0.01, rtol=1e-9, atol=1e-9, save_ts=ts,
+                        cluster=2, tile=4, masses=[it["masses"] for it in insts], hermitian=herm)
+        ys = b.unpack(b.run(b.pack([it["y0"] for it in insts])))
+        stats, ens = b.results()
+        for i, it in enumerate(insts):
+            assert stats[i]["hermitian"] == herm
+            assert rel_err(ys[i], ref_y[i]) < 1e-9, (herm, i)
+            np.testing.assert_allclose(ens[i][:, 0], ref_en[i][:, 0], rtol=1e-9)
+            L = ys[i].reshape(-1, it["shape"][0])
+            if herm:
+                assert np.all(L == np.conj(L[:, ::-1]))          # symmetry kept exactly

@@ -117,3 +117,21 @@ def test_simulation_driver_defaults():
     assert set(["Ck", "Fk", "time", "dCk", "EM_energy", "total_energy"]) <= set(out)
     assert not np.all(out["Fk"] == 0)
     assert out["Ck"].shape == (11, 40, 1, 33, 1)
+
+
+@pytest.mark.gpu
+def test_host_driven_dopri8_matches_oracle():
+    # the plain RHS driven from the host (external-solver use of the drop-in)
+    import torch
+    from spectrax_gb300 import dopri8, vector_field
+    shape = (33, 1, 1, 16, 1, 1, 3)
+    p = _params(shape)
+    y0 = _y0(shape)
+    ts = np.linspace(0.0, 1.0, 5)
+    ref = od.solve(lambda t, y: orhs.rhs(p, y, "divide"), 0.0, 1.0, y0, 0.01, ts=ts, adaptive=True,
+                   rtol=1e-10, atol=1e-12)
+    plan = vector_field.plan_for_params(p, "divide")
+    y, ys, st = dopri8.host_dopri8_solve(plan, torch.from_numpy(y0), 1.0, 0.01, ts=ts, rtol=1e-10, atol=1e-12)
+    assert st["status_name"] == "DONE"
+    assert st["accepted"] == ref["accepted"] and st["rejected"] == ref["rejected"], (st, ref)
+    assert rel_err(ys.cpu().numpy(), ref["ys"]) < 1e-10
