@@ -142,6 +142,10 @@ int spx_vjp_noalloc(const spx_plan* plan, const void* y, const void* w, void* g,
  */
 int spx_rk_step_store(const spx_plan* plan, const void* y, double h, void* Ystages, void* Kstages,
                       void* ynext, void* stream);
+/* Status word of spx_rk_step_store since the last call (SPX_ST_RUNNING = 0: no
+ * problem; SPX_ST_WAIT_TIMEOUT: a bounded wait for staged data gave up and the
+ * outputs are invalid); reading it resets it.  Synchronises `stream`. */
+int spx_rk_status(int32_t* status, void* stream);
 /* out = sum_{i < nterms} coefs[i] * vecs[i] over len complex128 entries
  * (vecs: host array of device pointers, nterms <= 16; out may alias an input). */
 int spx_lincomb(int64_t len, int32_t nterms, const void* const* vecs, const double* coefs, void* out,
@@ -153,6 +157,13 @@ int spx_lincomb(int64_t len, int32_t nterms, const void* const* vecs, const doub
  * 2 + Ns doubles the caller zeroes).
  */
 int spx_param_dots(const spx_plan* plan, const void* y, const void* g, double* acc, void* stream);
+/* g = J(y)^T w together with acc[k] += Re sum_e w_e (df/dtheta_k)_e for
+ * theta = (nu, k (as k d/dk), u_x of each species): spx_vjp and spx_param_dots
+ * in one launch, the parameter sums added in a fixed order.  ws as for spx_rhs
+ * (spx_rhs_workspace_bytes); 1D1V layout only.  Calls on one plan must not run
+ * concurrently (the plan holds the kernel's completion ticket). */
+int spx_vjp_param(const spx_plan* plan, const void* y, const void* w, void* g, double* acc, void* ws,
+                  size_t ws_bytes, void* stream);
 
 /* ------------------------------------------------------------------ Dopri8 */
 typedef struct spx_dopri8_opts {

@@ -129,10 +129,8 @@ class Dopri8Adjoint:
                     if aij != 0.0:
                         terms.append((h * aij, gY[i]))
                 lincomb(gk, terms)
-                _lib.check(L.spx_vjp(self.plan.handle, _ptr(Yq[j]), _ptr(gk), _ptr(gY[j]), ws, wsb,
-                                     _stream_ptr()), "spx_vjp")
-                _lib.check(L.spx_param_dots(self.plan.handle, _ptr(Yq[j]), _ptr(gk), accp, _stream_ptr()),
-                           "spx_param_dots")
+                _lib.check(L.spx_vjp_param(self.plan.handle, _ptr(Yq[j]), _ptr(gk), _ptr(gY[j]), accp, ws, wsb,
+                                           _stream_ptr()), "spx_vjp_param")
             lincomb(mu, [(1.0, mu)] + [(1.0, gY[j]) for j in range(S)])
             mu[nc:].add_((B["coef"][q] * c2) * Yq[0, nc:].conj())
 
@@ -179,6 +177,10 @@ class Dopri8Adjoint:
             B["coef"][: b - a].copy_(dLdE[a:b])
             self._run("recompute", b - a, use_graphs)
             self._run("sweep", b - a, use_graphs)
+        st = C.c_int32()
+        _lib.check(_lib.lib().spx_rk_status(C.byref(st), _stream_ptr()), "spx_rk_status")
+        if st.value != 0:
+            raise RuntimeError(f"step recomputation failed: status {_lib.STATUS_NAMES.get(st.value, st.value)}")
         return mu.clone(), acc.clone()
 
 

@@ -1,7 +1,9 @@
 // spx_adjoint.cu — building blocks of the discrete adjoint of the Dopri8 step.
 //
 //  * spx_rk_step_store: one fixed Runge-Kutta step that keeps every stage input
-//    Y_j and stage derivative K_j = f(Y_j) (the backward sweep linearises at Y_j);
+//    Y_j and stage derivative K_j = f(Y_j) (the backward sweep linearises at Y_j),
+//    with the same staged stage kernels as the device Dopri8 solver, so a
+//    recomputed step reproduces the forward solve's arithmetic;
 //  * spx_lincomb: out = sum_i c_i v_i (real c_i), the adjoint recursion's combinations;
 //  * spx_param_dots: accumulates Re sum_e g_e (df/dtheta)_e for the parameters
 //    theta = (nu, k, u_x of each species) of a 1D1V problem.
@@ -10,6 +12,7 @@
 
 #include "spx_plan.h"
 #include "spx_rhs.cuh"
+#include "spx_stage.cuh"
 #include "spx_tableau.cuh"
 
 namespace spx {
@@ -18,59 +21,53 @@ __constant__ double aCoef[13][13];   // a(i, j)
 __constant__ double aB[13];
 __constant__ int aMask[13];
 
-// Stage epilogue: store K_j, write the next stage input Y_{j+1} = y + h sum_{l<=j} a(j+1, l) K_l.
-struct EpiStore2 {
-  const double2* y;
-  double2* Kb;
-  double2* Yb;
-  double2* ynext;   // written by the last stage: y + h sum b_l K_l
-  long long len;
-  int stage;
-  double h;
-  __device__ __forceinline__ void operator()(size_t e, double2 v) const {
-    Kb[(size_t)stage * len + e] = v;
-    double2 acc = y[e];
-    if (stage < rk::S - 1) {
-      const int row = stage + 1;
-      const int mask = aMask[row];
-      for (int j = 0; j < stage; ++j)
-        if (mask & (1 << j)) acc = crfma(h * aCoef[row][j], Kb[(size_t)j * len + e], acc);
-      acc = crfma(h * aCoef[row][stage], v, acc);
-      Yb[(size_t)(stage + 1) * len + e] = acc;
-    } else {
-      for (int j = 0; j < stage; ++j)
-        if (aB[j] != 0.0) acc = crfma(h * aB[j], Kb[(size_t)j * len + e], acc);
-      acc = crfma(h * aB[stage], v, acc);
-      ynext[e] = acc;
-    }
-  }
-};
+// Status of the staged recomputation (SPX_ST_WAIT_TIMEOUT if a bounded wait gave up).
+__device__ int g_rk_status;
 
-__global__ void __launch_bounds__(NTHREADS) k_rk_stage_1v(const DevPlan* __restrict__ gP,
-                                                          const double2* __restrict__ gtab,
-                                                          const double2* y, double2* Yb, double2* Kb,
-                                                          double2* ynext, double h, int stage) {
+// Stage term list for a fixed step h: stage i < 12 forms y + h sum_j a(i+1, j) K_j
+// (j < i, nonzero) + h a(i+1, i) K_i; the last stage y + h sum_j b_j K_j + h b_12 K_12.
+__device__ void fill_terms_fixed(EpiTerms& T, int stage, double h) {
+  T.n = 0;
+  if (stage < rk::S - 1) {
+    const int row = stage + 1, mask = aMask[row];
+    for (int j = 0; j < stage; ++j)
+      if (mask & (1 << j)) { T.j[T.n] = j; T.c[T.n] = h * aCoef[row][j]; T.e[T.n] = 0.0; ++T.n; }
+    T.cself = h * aCoef[row][stage];
+  } else {
+    for (int j = 0; j < stage; ++j)
+      if (aB[j] != 0.0) { T.j[T.n] = j; T.c[T.n] = h * aB[j]; T.e[T.n] = 0.0; ++T.n; }
+    T.cself = h * aB[stage];
+  }
+  T.eself = 0.0;
+}
+
+template <bool LAST>
+__global__ void __launch_bounds__(NTHREADS, 2) k_rk_stage_st(const DevPlan* __restrict__ gP,
+                                                            const double2* __restrict__ gtab,
+                                                            const double2* y, double2* Yb, double2* Kb,
+                                                            double2* ynext, double h, int stage, int npf) {
   __shared__ DevPlan P;
+  __shared__ EpiTerms terms;
+  __shared__ __align__(8) uint64_t bars[2];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   load_plan(P, stab, gP, gtab);
+  if (threadIdx.x == 0) fill_terms_fixed(terms, stage, h);
+  __syncthreads();
   const long long len = P.nc + 6LL * P.plane;
-  EpiStore2 epi{y, Kb, Yb, ynext, len, stage, h};
-  const double2* in = Yb + (size_t)stage * len;
-  const int nblk = P.pb.Ns * P.ntiles;
-  if ((int)blockIdx.x == nblk) {
-    maxwell_range(P, stab, in, 0, P.plane, epi);
-    return;
-  }
-  const int s = blockIdx.x / P.ntiles, tile = blockIdx.x % P.ntiles;
-  const int n0 = tile * P.tile;
-  const int nt = min(P.tile, P.pb.Nn - n0);
-  if (nt <= 0) return;
-  const int N = P.ax[1].n;
-  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + (size_t)(2 * P.tile + 2) * N;
-  double* scoef = reinterpret_cast<double*>(sB + (size_t)(2 * P.tile + 2) * N);
-  rhs1v_tile(P, stab, in, s, n0, nt, sA, sB, scoef, epi);
+  StageIO io;
+  io.in = Yb + (size_t)stage * len;
+  io.Y = y;
+  io.K = Kb;
+  io.len = len;
+  io.Ki = Kb + (size_t)stage * len;
+  io.out = LAST ? ynext : Yb + (size_t)(stage + 1) * len;
+  io.npf = npf;
+  io.herm = false;
+  io.rtol = io.atol = 0.0;
+  io.adaptive = 0;
+  io.timeout_status = &g_rk_status;
+  staged_stage_1v<LAST>(P, stab, io, terms, bars, [](auto&) {});
 }
 
 struct LinTerms {
@@ -88,9 +85,74 @@ __global__ void k_lincomb(LinTerms t, double2* __restrict__ out, long long len) 
   }
 }
 
-// acc[0] += Re sum g . (-col C)            (d/dnu)
-// acc[1] += Re sum g . f_K(y)               (k d/dk: the parts of f linear in K)
-// acc[2+s] += Re sum g . (d f / d u_x,s)
+// Parameter sensitivities of one entry e of f(y) contracted with g:
+//   loc[0] += Re g . (-col C)            (d/dnu)
+//   loc[1] += Re g . f_K(y)               (k d/dk: the parts of f linear in K)
+//   loc[2+s] += Re g . (d f / d u_x,s)
+__device__ __forceinline__ void param_terms(const DevPlan& P, const double2* __restrict__ tab,
+                                            const double2* __restrict__ y, const double2 ge, long long e,
+                                            double* loc) {
+  const int N = P.ax[1].n, Nn = P.pb.Nn, Ns = P.pb.Ns;
+  const long long nC = P.nc;
+  if (e < nC) {
+    const int c = (int)(e % N);
+    const int n = (int)((e / N) % Nn);
+    const int s = (int)(e / ((long long)N * Nn));
+    const double a0 = P.pb.alpha_s[3 * s], u0 = P.pb.u_s[3 * s];
+    const double2 C0 = y[e];
+    const double2 Cp = (n + 1 < Nn) ? y[e + N] : make_double2(0.0, 0.0);
+    const double2 Cm = (n >= 1) ? y[e - N] : make_double2(0.0, 0.0);
+    const double K = ktab(P, tab, 1, c).x;
+    // nu: -col(n) C
+    const double col = colc(Nn, n);
+    loc[0] += -col * (ge.x * C0.x - ge.y * C0.y);
+    // streaming -i K a0 t  with t = sqrt((n+1)/2) C+ + sqrt(n/2) C- + (u0/a0) C
+    double2 t = cscale(u0 / a0, C0);
+    t = crfma(sqrt((n + 1) * 0.5), Cp, t);
+    t = crfma(sqrt(n * 0.5), Cm, t);
+    const double w = K * a0;
+    const double2 fk = make_double2(w * t.y, -w * t.x);
+    loc[1] += ge.x * fk.x - ge.y * fk.y;
+    // u_x,s: -i K C
+    const double2 fu = make_double2(K * C0.y, -K * C0.x);
+    loc[2 + s] += ge.x * fu.x - ge.y * fu.y;
+  } else {
+    const int f = (int)((e - nC) / N), c = (int)((e - nC) % N);
+    const double K = ktab(P, tab, 1, c).x;
+    const double2* F = y + nC;
+    const double iO = 1.0 / P.pb.Omega_cs[0];
+    // curl parts with K = (Kx, 0, 0): dE_y = -i Kx B_z, dE_z = i Kx B_y, dB_y = i Kx E_z, dB_z = -i Kx E_y
+    double2 fk = make_double2(0.0, 0.0);
+    if (f == 1) { const double2 b = F[5 * N + c]; fk = make_double2(K * b.y, -K * b.x); }
+    else if (f == 2) { const double2 b = F[4 * N + c]; fk = make_double2(-K * b.y, K * b.x); }
+    else if (f == 4) { const double2 ez = F[2 * N + c]; fk = make_double2(-K * ez.y, K * ez.x); }
+    else if (f == 5) { const double2 ey = F[N + c]; fk = make_double2(K * ey.y, -K * ey.x); }
+    loc[1] += ge.x * fk.x - ge.y * fk.y;
+    if (f == 0) {
+      // dE_x = -J_x / Omega_0 with J_x containing q a0 a1 a2 u_x C_{s,000}
+      for (int s = 0; s < Ns; ++s) {
+        const double pre = P.pb.qs[s] * P.pb.alpha_s[3 * s] * P.pb.alpha_s[3 * s + 1] * P.pb.alpha_s[3 * s + 2];
+        const double2 C000 = y[(size_t)s * Nn * N + c];
+        loc[2 + s] += -pre * iO * (ge.x * C000.x - ge.y * C000.y);
+      }
+    }
+  }
+}
+
+// Block sums of loc[0 .. nk) (every thread's values); valid in threads 0 .. nk-1.
+__device__ __forceinline__ double block_sums(const double* loc, int nk, double (*red)[2 + SPX_MAX_SPECIES]) {
+  for (int k = 0; k < nk; ++k) {
+    double v = loc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
+  }
+  __syncthreads();
+  double v = 0.0;
+  if ((int)threadIdx.x < nk)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+  return v;
+}
+
 __global__ void __launch_bounds__(NTHREADS) k_param_dots_1v(const DevPlan* __restrict__ gP,
                                                             const double2* __restrict__ gtab,
                                                             const double2* __restrict__ y,
@@ -101,69 +163,119 @@ __global__ void __launch_bounds__(NTHREADS) k_param_dots_1v(const DevPlan* __res
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   load_plan(P, stab, gP, gtab);
-  const int N = P.ax[1].n, Nn = P.pb.Nn, Ns = P.pb.Ns;
-  const long long nC = P.nc;
+  const int nk = 2 + P.pb.Ns;
   double loc[2 + SPX_MAX_SPECIES];
   for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k) loc[k] = 0.0;
-  const double iO = 1.0 / P.pb.Omega_cs[0];
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nC + 6LL * N;
-       e += (long long)gridDim.x * blockDim.x) {
-    const double2 ge = g[e];
-    if (e < nC) {
-      const int c = (int)(e % N);
-      const int n = (int)((e / N) % Nn);
-      const int s = (int)(e / ((long long)N * Nn));
-      const double a0 = P.pb.alpha_s[3 * s], u0 = P.pb.u_s[3 * s];
-      const double2 C0 = y[e];
-      const double2 Cp = (n + 1 < Nn) ? y[e + N] : make_double2(0.0, 0.0);
-      const double2 Cm = (n >= 1) ? y[e - N] : make_double2(0.0, 0.0);
-      const double K = ktab(P, stab, 1, c).x;
-      // nu: -col(n) C
-      const double col = colc(Nn, n);
-      loc[0] += -col * (ge.x * C0.x - ge.y * C0.y);
-      // streaming -i K a0 t  with t = sqrt((n+1)/2) C+ + sqrt(n/2) C- + (u0/a0) C
-      double2 t = cscale(u0 / a0, C0);
-      t = crfma(sqrt((n + 1) * 0.5), Cp, t);
-      t = crfma(sqrt(n * 0.5), Cm, t);
-      const double w = K * a0;
-      const double2 fk = make_double2(w * t.y, -w * t.x);
-      loc[1] += ge.x * fk.x - ge.y * fk.y;
-      // u_x,s: -i K C
-      const double2 fu = make_double2(K * C0.y, -K * C0.x);
-      loc[2 + s] += ge.x * fu.x - ge.y * fu.y;
-    } else {
-      const int f = (int)((e - nC) / N), c = (int)((e - nC) % N);
-      const double K = ktab(P, stab, 1, c).x;
-      const double2* F = y + nC;
-      // curl parts with K = (Kx, 0, 0): dE_y = -i Kx B_z, dE_z = i Kx B_y, dB_y = i Kx E_z, dB_z = -i Kx E_y
-      double2 fk = make_double2(0.0, 0.0);
-      if (f == 1) { const double2 b = F[5 * N + c]; fk = make_double2(K * b.y, -K * b.x); }
-      else if (f == 2) { const double2 b = F[4 * N + c]; fk = make_double2(-K * b.y, K * b.x); }
-      else if (f == 4) { const double2 ez = F[2 * N + c]; fk = make_double2(-K * ez.y, K * ez.x); }
-      else if (f == 5) { const double2 ey = F[N + c]; fk = make_double2(K * ey.y, -K * ey.x); }
-      loc[1] += ge.x * fk.x - ge.y * fk.y;
-      if (f == 0) {
-        // dE_x = -J_x / Omega_0 with J_x containing q a0 a1 a2 u_x C_{s,000}
-        for (int s = 0; s < Ns; ++s) {
-          const double pre = P.pb.qs[s] * P.pb.alpha_s[3 * s] * P.pb.alpha_s[3 * s + 1] * P.pb.alpha_s[3 * s + 2];
-          const double2 C000 = y[(size_t)s * Nn * N + c];
-          loc[2 + s] += -pre * iO * (ge.x * C000.x - ge.y * C000.y);
-        }
+  const long long len = P.nc + 6LL * P.ax[1].n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len;
+       e += (long long)gridDim.x * blockDim.x)
+    param_terms(P, stab, y, g[e], e, loc);
+  const double v = block_sums(loc, nk, red);
+  if ((int)threadIdx.x < nk) atomicAdd(acc + threadIdx.x, v);
+}
+
+// VJP of one stage plus the parameter dot products, in one launch (1D1V):
+// g = J(y)^T w and acc[k] += Re sum_e w_e (df/dtheta_k)_e.  Tile CTAs run the
+// VJP tile and the parameter terms of their own planes, the extra CTA those of
+// the field entries; every CTA writes its partial sums, and the last to arrive
+// (atomic ticket) forms the field gradient from the tiles' partial field sums
+// and adds the parameter partials to acc in CTA order (deterministic).
+// ws: part (Ns * ntiles * N double2) | pp (grid x (2 + SPX_MAX_SPECIES) doubles); the
+// ticket lives in the plan (calls on one plan are serialised, as its workspace is).
+__global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __restrict__ gP,
+                                                              const double2* __restrict__ gtab,
+                                                              const double2* __restrict__ y,
+                                                              const double2* __restrict__ w,
+                                                              double2* __restrict__ g, double2* part, double* pp,
+                                                              unsigned int* ticket, double* acc) {
+  __shared__ DevPlan P;
+  __shared__ double red[NTHREADS / 32][2 + SPX_MAX_SPECIES];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int last;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  const int nblk = P.pb.Ns * P.ntiles;
+  const int N = P.ax[1].n, Nn = P.pb.Nn, T = P.tile;
+  const int nk = 2 + P.pb.Ns;
+  // work area: sA, sB (2T+1 lines each) | Uy, Uw (T+2 lines each) | yF3, wE (3 lines each) | coefficients
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)(2 * T + 1) * N;
+  double2* Uy = sB + (size_t)(2 * T + 1) * N;
+  double2* Uw = Uy + (size_t)(T + 2) * N;
+  double2* yF3 = Uw + (size_t)(T + 2) * N;
+  double2* wE = yF3 + 3 * (size_t)N;
+  double* scoef = reinterpret_cast<double*>(wE + 3 * (size_t)N);
+  double loc[2 + SPX_MAX_SPECIES];
+#pragma unroll
+  for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k) loc[k] = 0.0;
+  const int b = blockIdx.x;
+  bool timed_out = false;
+  if (b < nblk) {
+    const int s = b / P.ntiles, tile = b % P.ntiles;
+    const int m0 = tile * T, nt = min(T, Nn - m0);
+    if (nt > 0) {
+      // stage y and w planes m0-1 .. m0+nt, y's G lines and w's E lines
+      const size_t sbase = (size_t)s * Nn * N;
+      if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
       }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const int lo = max(m0 - 1, 0), hi = min(m0 + nt, Nn - 1);
+        const uint32_t bu = (uint32_t)((hi - lo + 1) * N * sizeof(double2));
+        const uint32_t bf = (uint32_t)(N * sizeof(double2));
+        mbar_arm(&bar, 2 * bu + 6 * bf);
+        const size_t d0 = (size_t)(lo - (m0 - 1)) * N;
+        bulk_g2s(Uy + d0, y + sbase + (size_t)lo * N, bu, &bar);
+        bulk_g2s(Uw + d0, w + sbase + (size_t)lo * N, bu, &bar);
+        const double2* F = y + P.nc;
+        bulk_g2s(yF3, F, bf, &bar);                          // E_x
+        bulk_g2s(yF3 + N, F + 5 * (size_t)N, bf, &bar);      // B_z
+        bulk_g2s(yF3 + 2 * N, F + 4 * (size_t)N, bf, &bar);  // B_y
+        bulk_g2s(wE, w + P.nc, 3 * bf, &bar);                // w's E_x, E_y, E_z
+      }
+      if (m0 == 0)
+        for (int i = threadIdx.x; i < N; i += blockDim.x) Uy[i] = Uw[i] = make_double2(0.0, 0.0);
+      if (m0 + nt == Nn)
+        for (int i = threadIdx.x; i < N; i += blockDim.x)
+          Uy[(size_t)(nt + 1) * N + i] = Uw[(size_t)(nt + 1) * N + i] = make_double2(0.0, 0.0);
+      const bool ok = mbar_wait_bounded(&bar, 0);
+      if (__syncthreads_or(!ok)) {
+        timed_out = true;
+      } else {
+        double pacc[3] = {0.0, 0.0, 0.0};
+        vjp1v_tile_u(P, stab, Uy, Uw, yF3, wE, g, part, s, tile, m0, nt, sA, sB, scoef, pacc);
+#pragma unroll
+        for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k)
+          loc[k] = (k == 0) ? pacc[0] : (k == 1) ? pacc[1] : (k == 2 + s) ? pacc[2] : 0.0;
+      }
+    } else {
+      for (int x = threadIdx.x; x < N; x += blockDim.x)
+        part[((size_t)s * P.ntiles + tile) * N + x] = make_double2(0.0, 0.0);
     }
+  } else {
+    for (long long e = P.nc + threadIdx.x; e < P.nc + 6LL * N; e += blockDim.x) param_terms(P, stab, y, w[e], e, loc);
   }
-  // block reduction of the 2 + Ns sums
-  for (int k = 0; k < 2 + Ns; ++k) {
-    double v = loc[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
-  }
+  if (timed_out && threadIdx.x == 0) atomicExch(&g_rk_status, SPX_ST_WAIT_TIMEOUT);
+  const double v = block_sums(loc, nk, red);
+  if ((int)threadIdx.x < nk) pp[(size_t)b * (2 + SPX_MAX_SPECIES) + threadIdx.x] = v;
+  __threadfence();
   __syncthreads();
-  if (threadIdx.x < 2 + Ns) {
-    double v = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
-    atomicAdd(acc + threadIdx.x, v);
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // the field pass ping-pongs Ns lines: second buffer after max(2T+1, Ns) lines
+  // (6T + 12 >= 2 Ns for every Ns <= 8, so both fit in the work area)
+  vjp1v_fields(P, stab, w, g, part, sA, sA + (size_t)max(2 * T + 1, P.pb.Ns) * N);
+  if ((int)threadIdx.x < nk) {
+    double sum = 0.0;
+    for (int q = 0; q < (int)gridDim.x; ++q) sum += __ldcg(pp + (size_t)q * (2 + SPX_MAX_SPECIES) + threadIdx.x);
+    acc[threadIdx.x] += sum;
   }
+  if (threadIdx.x == 0) *ticket = 0;
 }
 
 static int adj_setup() {
@@ -186,8 +298,12 @@ static int adj_setup() {
   SPX_CUDA(cudaMemcpyToSymbol(aMask, m, sizeof(m)));
   const int optin = smem_optin();
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_1v));
-  SPX_CUDA(cudaFuncSetAttribute(k_rk_stage_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_rk_stage_st<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_rk_stage_st<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v));
+  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_param_dots_1v));
   SPX_CUDA(cudaFuncSetAttribute(k_param_dots_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   done = true;
@@ -215,11 +331,36 @@ int spx_rk_step_store(const spx_plan* pl, const void* y, double h, void* Ystages
   double2* Yb = static_cast<double2*>(Ystages);
   if (static_cast<const void*>(Yb) != y)
     SPX_CUDA(cudaMemcpyAsync(Yb, y, sizeof(double2) * len, cudaMemcpyDeviceToDevice, st));
-  for (int stage = 0; stage < rk::S; ++stage)
-    k_rk_stage_1v<<<P.pb.Ns * P.ntiles + 1, pl->threads, pl->smem_1v, st>>>(
-        pl->d_plan, pl->d_tab, static_cast<const double2*>(y), Yb, static_cast<double2*>(Kstages),
-        static_cast<double2*>(ynext), h, stage);
+  cudaFuncAttributes fa;
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<true>));
+  int npf = 0;
+  const size_t smem = stage_smem_1v(pl, fa.sharedSizeBytes, &npf);
+  if (npf < 1) { set_error("spx_rk_step_store: Nx / tile too large for the stage kernel"); return SPX_E_UNSUPPORTED; }
+  const int grid = P.pb.Ns * P.ntiles + 1;
+  for (int stage = 0; stage < rk::S; ++stage) {
+    if (stage < rk::S - 1)
+      k_rk_stage_st<false><<<grid, pl->threads, smem, st>>>(pl->d_plan, pl->d_tab, Yb, Yb,
+                                                              static_cast<double2*>(Kstages),
+                                                              static_cast<double2*>(ynext), h, stage, npf);
+    else
+      k_rk_stage_st<true><<<grid, pl->threads, smem, st>>>(pl->d_plan, pl->d_tab, Yb, Yb,
+                                                             static_cast<double2*>(Kstages),
+                                                             static_cast<double2*>(ynext), h, stage, npf);
+  }
   SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+int spx_rk_status(int32_t* status, void* stream) {
+  if (!status) { set_error("spx_rk_status: null argument"); return SPX_E_ARG; }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int v = 0;
+  SPX_CUDA(cudaMemcpyFromSymbolAsync(&v, g_rk_status, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  SPX_CUDA(cudaStreamSynchronize(st));
+  const int zero = 0;
+  SPX_CUDA(cudaMemcpyToSymbolAsync(g_rk_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+  SPX_CUDA(cudaStreamSynchronize(st));
+  *status = v;
   return SPX_OK;
 }
 
@@ -257,6 +398,36 @@ int spx_param_dots(const spx_plan* pl, const void* y, const void* g, double* acc
   const int blocks = (int)std::min<long long>((len + NTHREADS - 1) / NTHREADS, 152LL * 2);
   k_param_dots_1v<<<std::max(blocks, 1), NTHREADS, pl->smem_tab, static_cast<cudaStream_t>(stream)>>>(
       pl->d_plan, pl->d_tab, static_cast<const double2*>(y), static_cast<const double2*>(g), acc);
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, double* acc, void* ws,
+                  size_t ws_bytes, void* stream) {
+  if (!pl || !y || !w || !g || !acc || !ws) { set_error("spx_vjp_param: null argument"); return SPX_E_ARG; }
+  if (pl->host.path != 0) {
+    set_error("spx_vjp_param: only the 1D1V layout is supported");
+    return SPX_E_UNSUPPORTED;
+  }
+  if (ws_bytes < pl->ws_bytes || (reinterpret_cast<uintptr_t>(ws) & 255)) {
+    set_error("spx_vjp_param: workspace too small or not 256-byte aligned");
+    return SPX_E_WORKSPACE;
+  }
+  int rc = adj_setup();
+  if (rc != SPX_OK) return rc;
+  const DevPlan& P = pl->host;
+  const int grid = P.pb.Ns * P.ntiles + 1;
+  char* wsb = static_cast<char*>(ws);
+  const size_t part_bytes = (size_t)P.pb.Ns * P.ntiles * P.ax[1].n * sizeof(double2);
+  double* pp = reinterpret_cast<double*>(wsb + part_bytes);
+  // the plan's ticket is zero between launches (the last CTA resets it)
+  unsigned int* ticket = pl->d_ticket;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int T = P.tile, N = P.ax[1].n;
+  const size_t smem = pl->smem_tab + (size_t)(6 * T + 12) * N * sizeof(double2) + 64 * sizeof(double);
+  k_vjp_param_1v<<<grid, pl->threads, smem, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y),
+                                                         static_cast<const double2*>(w), static_cast<double2*>(g),
+                                                         reinterpret_cast<double2*>(wsb), pp, ticket, acc);
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
 }

@@ -23,6 +23,7 @@
 #include "spx_plan.h"
 #include "spx_rhs.cuh"
 #include "spx_tableau.cuh"
+#include "spx_stage.cuh"
 #include "spx_tma.cuh"
 
 namespace spx {
@@ -248,18 +249,8 @@ __device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, doub
 // Epilogue term lists: stage i < 12 forms the next input y + h sum_j a(i+1, j)
 // K_j over j < i with a(i+1, j) != 0 (then + h a(i+1, i) K_i); the last stage
 // forms y_new and the error over j < 12 with b_j != 0 or e_j != 0.  Ascending j.
-constexpr int MAX_TERMS = 10;
 __constant__ int cEpiN[13];
 __constant__ int cEpiJ[13][MAX_TERMS];
-
-// Coefficients of the current launch's epilogue, in shared memory.
-struct EpiTerms {
-  int n;                       // number of K_j terms (j < stage)
-  int j[MAX_TERMS];
-  double c[MAX_TERMS];         // h a(stage+1, j)  or  h b_j
-  double e[MAX_TERMS];         // last stage: h e_j
-  double cself, eself;         // the current stage's own weights
-};
 
 __device__ void fill_terms(EpiTerms& T, int stage, double h) {
   const bool last = stage == rk::S - 1;
@@ -275,164 +266,9 @@ __device__ void fill_terms(EpiTerms& T, int stage, double h) {
   T.eself = last ? h * cCoef[13][stage] : 0.0;
 }
 
-// Epilogue of stages 0..11: store K_i and the next stage input.  The first
-// `npf` operands (y, then K_j in list order) of the CTA's own entries are
-// staged in shared memory `pf` (own entries each, local index il); the rest
-// are read from global memory, up to five loads in flight.
-struct EpiNext {
-  double2* __restrict__ Ki;
-  double2* __restrict__ Snext;
-  const double2* __restrict__ Y;
-  const double2* __restrict__ K;
-  long long len;
-  const EpiTerms* T;
-  const double2* pf;
-  int own, npf;
-  uint64_t* bar;               // completes when pf is filled (nullptr: nothing staged)
-  __device__ bool prepare() const {
-    if (!bar) return true;
-    const bool ok = mbar_wait_bounded(bar, 0);
-    return !__syncthreads_or(!ok);
-  }
-  __device__ __forceinline__ double2 operand(int q, size_t e, int il) const {
-    // q = 0: y, q >= 1: K_{j[q-1]}
-    if (q < npf) return pf[(size_t)q * own + il];
-    return q == 0 ? Y[e] : K[(size_t)T->j[q - 1] * len + e];
-  }
-  __device__ __forceinline__ void operator()(size_t e, int il, double2 v) const {
-    Ki[e] = v;
-    Snext[e] = next(e, il, v);
-  }
-  // exactly Hermitian operands: the mirrored entry e2 gets the conjugates
-  __device__ __forceinline__ void pair(size_t e, int il, size_t e2, int il2, double2 v, bool two) const {
-    const double2 sn = next(e, il, v);
-    Ki[e] = v;
-    Snext[e] = sn;
-    if (two) {
-      Ki[e2] = make_double2(v.x, -v.y);
-      Snext[e2] = make_double2(sn.x, -sn.y);
-    }
-  }
-  __device__ __forceinline__ double2 next(size_t e, int il, double2 v) const {
-    const int n = T->n;
-    double2 acc;
-    if (npf > n) {                       // every operand staged
-      acc = pf[il];
-#pragma unroll 1
-      for (int t = 0; t < n; ++t) acc = crfma(T->c[t], pf[(size_t)(1 + t) * own + il], acc);
-    } else {
-      acc = operand(0, e, il);
-#pragma unroll 1
-      for (int r = 0; r < n; r += 5) {
-        double2 k[5];
-#pragma unroll
-        for (int u = 0; u < 5; ++u)
-          if (r + u < n) k[u] = operand(1 + r + u, e, il);
-#pragma unroll
-        for (int u = 0; u < 5; ++u)
-          if (r + u < n) acc = crfma(T->c[r + u], k[u], acc);
-      }
-    }
-    return crfma(T->cself, v, acc);
-  }
-};
-
-// Epilogue of the last stage: y_new, scaled error, non-finite flag; operands
-// staged as in EpiNext.
-struct EpiFinal {
-  double2* __restrict__ Ki;
-  double2* __restrict__ Ynew;
-  const double2* __restrict__ Y;
-  const double2* __restrict__ K;
-  long long len;
-  const EpiTerms* T;
-  const double2* pf;
-  int own, npf;
-  uint64_t* bar;
-  double rtol, atol;
-  int adaptive;
-  double sq;
-  int nonfinite;
-  double2 last_yn;
-  double last_sq;
-  __device__ bool prepare() const {
-    if (!bar) return true;
-    const bool ok = mbar_wait_bounded(bar, 0);
-    return !__syncthreads_or(!ok);
-  }
-  __device__ __forceinline__ double2 operand(int q, size_t e, int il) const {
-    if (q < npf) return pf[(size_t)q * own + il];
-    return q == 0 ? Y[e] : K[(size_t)T->j[q - 1] * len + e];
-  }
-  __device__ __forceinline__ void operator()(size_t e, int il, double2 v) {
-    Ki[e] = v;
-    const double2 y0 = operand(0, e, il);
-    double2 yn = y0;
-    double2 er = make_double2(0.0, 0.0);
-    const int n = T->n;
-    if (npf > n) {                       // every operand staged
-#pragma unroll 1
-      for (int t = 0; t < n; ++t) {
-        const double2 k = pf[(size_t)(1 + t) * own + il];
-        yn = crfma(T->c[t], k, yn);
-        er = crfma(T->e[t], k, er);
-      }
-    } else {
-#pragma unroll 1
-      for (int r = 0; r < n; r += 5) {
-        double2 k[5];
-#pragma unroll
-        for (int u = 0; u < 5; ++u)
-          if (r + u < n) k[u] = operand(1 + r + u, e, il);
-#pragma unroll
-        for (int u = 0; u < 5; ++u)
-          if (r + u < n) {
-            yn = crfma(T->c[r + u], k[u], yn);
-            er = crfma(T->e[r + u], k[u], er);
-          }
-      }
-    }
-    yn = crfma(T->cself, v, yn);
-    er = crfma(T->eself, v, er);
-    Ynew[e] = yn;
-    last_yn = yn;
-    if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
-    if (adaptive) {
-      // |err / (atol + rtol max(|y0|, |y1|))|^2 with one division per entry
-      const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
-      const double inv = 1.0 / fma(rtol, sqrt(fmax(m0, m1)), atol);
-      const double rx = er.x * inv, ry = er.y * inv;
-      last_sq = fma(rx, rx, ry * ry);
-      sq += last_sq;
-    }
-  }
-  // exactly Hermitian operands: the mirrored entry has the conjugate y_new and
-  // the same error contribution
-  __device__ __forceinline__ void pair(size_t e, int il, size_t e2, int il2, double2 v, bool two) {
-    (*this)(e, il, v);
-    if (two) {
-      Ki[e2] = make_double2(v.x, -v.y);
-      Ynew[e2] = make_double2(last_yn.x, -last_yn.y);
-      if (adaptive) sq += last_sq;
-    }
-  }
-};
-
-// Shared-memory layout of the fused 1D1V stage kernel after the table (double2
-// units, all 16-byte aligned):
-//   sA, sB : (T+1)*N each   U : (T+2)*N   F3 : 3*N   (the field CTA reuses
-//   sA.. as its (2*Ns+12)*N gather + output area)   scoef : 64 doubles
-//   pf     : npf * T * N   (y and K_j of the CTA's own planes)
-__host__ __device__ __forceinline__ int d8_lines_1v(int T, int Ns) {
-  const int a = 2 * (T + 1) + (T + 2) + 3, b = 2 * Ns + 12;
-  return a > b ? a : b;
-}
-
-// One stage of the fused 1D1V path.  Thread 0 stages the tile's input planes
-// n0-1 .. n0+nt and the three field lines that G needs with bulk copies, plus
-// the epilogue's own-plane operands on a second barrier, so the latter arrive
-// while the transforms run.  The last stage (LAST) forms y_new and the error
-// and runs the controller in its last CTA.
+// One stage of the fused 1D1V path (staged_stage_1v): stage inputs and
+// epilogue operands arrive by bulk copies; the last stage (LAST) forms y_new
+// and the error and runs the controller in its last CTA.
 template <bool LAST>
 __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage) {
   __shared__ DevPlan P;
@@ -459,107 +295,36 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
   if (threadIdx.x == 0) fill_terms(terms, stage, at.h);
   const long long len = a.len;
   const double2* Y = pick(a.Y, s.cur);
-  const double2* in = (stage == 0) ? Y : pick(a.S, stage & 1);
   double2* Ki = a.K + (size_t)stage * len;
-  const int nblk = P.pb.Ns * P.ntiles;
-  const int N = P.ax[1].n, T = P.tile, Nn = P.pb.Nn;
-  const int b = blockIdx.x;
   if (!LAST && stage == 0 && s.k1_valid) {
     // rejected attempt: K_0 = f(y) is kept; rebuild the next input y + h a(1,0) K_0
     __syncthreads();
+    const int nblk = P.pb.Ns * P.ntiles, N = P.ax[1].n, b = blockIdx.x;
     double2* Sn = pick(a.S, 1);
     auto one = [&](size_t e) { Sn[e] = crfma(terms.cself, Ki[e], Y[e]); };
     if (b == nblk) {
       for (int i = threadIdx.x; i < 6 * N; i += blockDim.x) one((size_t)P.nc + i);
     } else {
-      const int sp = b / P.ntiles, n0 = (b % P.ntiles) * T, nt = min(T, Nn - n0);
-      const size_t base = ((size_t)sp * Nn + n0) * N;
+      const int sp = b / P.ntiles, n0 = (b % P.ntiles) * P.tile, nt = min(P.tile, P.pb.Nn - n0);
+      const size_t base = ((size_t)sp * P.pb.Nn + n0) * N;
       for (int i = threadIdx.x; i < nt * N; i += blockDim.x) one(base + i);
     }
     return;
   }
-  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double* scoef = reinterpret_cast<double*>(sA + (size_t)d8_lines_1v(T, P.pb.Ns) * N);
-  double2* pf = reinterpret_cast<double2*>(scoef + 64);
-  if (b == nblk) {
-    // field CTA: plain gather (one CTA, small) and global epilogue operands
-    __syncthreads();
-    if constexpr (!LAST) {
-      EpiNext epi{Ki, pick(a.S, (stage + 1) & 1), Y, a.K, len, &terms, nullptr, 0, 0, nullptr};
-      maxwell1v_g(P, stab, SrcPlain{in}, sA, epi);
-    } else {
-      EpiFinal el{Ki, pick(a.Y, s.cur ^ 1), Y, a.K, len, &terms, nullptr, 0, 0, nullptr,
-                  s.rtol, s.atol, s.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
-      maxwell1v_g(P, stab, SrcPlain{in}, sA, el);
-      last_stage_tail(a, at, el, red);
-    }
-    return;
-  }
-  const int sp = b / P.ntiles, n0 = (b % P.ntiles) * T, nt = min(T, Nn - n0);
-  if (nt <= 0) {
-    if constexpr (LAST) {
-      struct { double sq; int nonfinite; } none{0.0, 0};
-      __syncthreads();
-      last_stage_tail(a, at, none, red);
-    }
-    return;
-  }
-  double2* sB = sA + (size_t)(T + 1) * N;
-  double2* U = sB + (size_t)(T + 1) * N;
-  double2* F3 = U + (size_t)(T + 2) * N;
-  const size_t sbase = (size_t)sp * Nn * N;
-  const int own = nt * N;
-  const int npf = min(a.npf, 1 + cEpiN[stage]);
-  if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int lo = max(n0 - 1, 0), hi = min(n0 + nt, Nn - 1);     // staged planes, inclusive
-    const uint32_t bu = (uint32_t)((hi - lo + 1) * N * sizeof(double2));
-    const uint32_t bf = (uint32_t)(N * sizeof(double2));
-    mbar_arm(&bars[0], bu + 3 * bf);
-    bulk_g2s(U + (size_t)(lo - (n0 - 1)) * N, in + sbase + (size_t)lo * N, bu, &bars[0]);
-    const double2* F = in + P.nc;
-    bulk_g2s(F3, F, bf, &bars[0]);                    // E_x
-    bulk_g2s(F3 + N, F + 5 * (size_t)N, bf, &bars[0]); // B_z
-    bulk_g2s(F3 + 2 * N, F + 4 * (size_t)N, bf, &bars[0]); // B_y
-    const uint32_t bo = (uint32_t)(own * sizeof(double2));
-    mbar_arm(&bars[1], (uint32_t)npf * bo);
-    const size_t o0 = sbase + (size_t)n0 * N;
-    bulk_g2s(pf, Y + o0, bo, &bars[1]);
-    for (int q = 1; q < npf; ++q)
-      bulk_g2s(pf + (size_t)q * own, a.K + (size_t)terms.j[q - 1] * len + o0, bo, &bars[1]);
-  }
-  // planes outside [0, Nn) read as zero (disjoint from the staged ones)
-  if (n0 == 0)
-    for (int i = threadIdx.x; i < N; i += blockDim.x) U[i] = make_double2(0.0, 0.0);
-  if (n0 + nt == Nn)
-    for (int i = threadIdx.x; i < N; i += blockDim.x) U[(size_t)(nt + 1) * N + i] = make_double2(0.0, 0.0);
-  const bool ok = mbar_wait_bounded(&bars[0], 0);
-  if (__syncthreads_or(!ok)) {
-    // the staged input never arrived: stop the solve, give the copies a last chance
-    if (threadIdx.x == 0) {
-      atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
-      mbar_wait_bounded(&bars[1], 0);
-    }
-    return;
-  }
-  if constexpr (!LAST) {
-    EpiNext epi{Ki, pick(a.S, (stage + 1) & 1), Y, a.K, len, &terms, pf, own, npf, &bars[1]};
-    if (s.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
-    else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
-  } else {
-    EpiFinal el{Ki, pick(a.Y, s.cur ^ 1), Y, a.K, len, &terms, pf, own, npf, &bars[1],
-                s.rtol, s.atol, s.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
-    if (s.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
-    else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
-    last_stage_tail(a, at, el, red);
-  }
-  // a failed prepare() returns from the tile early: record it once
-  if (threadIdx.x == 0 && !mbar_try_wait(&bars[1], 0)) atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
+  StageIO io;
+  io.in = (stage == 0) ? Y : pick(a.S, stage & 1);
+  io.Y = Y;
+  io.K = a.K;
+  io.len = len;
+  io.Ki = Ki;
+  io.out = LAST ? pick(a.Y, s.cur ^ 1) : pick(a.S, (stage + 1) & 1);
+  io.npf = a.npf;
+  io.herm = s.herm != 0;
+  io.rtol = s.rtol;
+  io.atol = s.atol;
+  io.adaptive = s.adaptive;
+  io.timeout_status = &a.st->status;
+  staged_stage_1v<LAST>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
 }
 
 __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
@@ -861,20 +626,12 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   int npf = 0;
   if (P.path == 0) {
     // stage kernel shared memory: table + line buffers + coefficients + staged
-    // epilogue operands; stage as many operands (y, then K_j) as keep two CTAs
-    // per SM resident, at least y.
-    const int T = P.tile, N = P.ax[1].n;
-    const size_t base = plan->smem_tab + (size_t)d8_lines_1v(T, Ns) * N * sizeof(double2) + 64 * sizeof(double);
-    const size_t per = (size_t)T * N * sizeof(double2);
+    // epilogue operands (as many as keep two CTAs per SM resident, at least y)
     cudaFuncAttributes fa;
     cudaError_t ea = cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>);
     if (ea != cudaSuccess) { delete s; return cuda_fail(ea, "cudaFuncGetAttributes"); }
-    const size_t two_per_sm = 228 * 1024 / 2 - 1024 - fa.sharedSizeBytes;
-    const size_t optin = (size_t)smem_optin() - fa.sharedSizeBytes;
-    const size_t budget = (base + per <= two_per_sm) ? two_per_sm : optin;
-    npf = (int)std::min<size_t>(1 + MAX_TERMS, budget > base ? (budget - base) / per : 0);
+    s->smem_stage = stage_smem_1v(plan, fa.sharedSizeBytes, &npf);
     if (npf < 1) { delete s; set_error("Nx / tile too large for the Dopri8 stage kernel"); return SPX_E_UNSUPPORTED; }
-    s->smem_stage = base + (size_t)npf * per;
   } else {
     s->smem_stage = plan->smem_gen;
   }

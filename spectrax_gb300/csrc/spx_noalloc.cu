@@ -30,7 +30,7 @@ namespace spx {
 // Scratch for the per-(species, tile) partial field-gradient lines.
 static __device__ __align__(256) double2 g_vjp_scratch[SPX_VJP_NOALLOC_MAX_ENTRIES];
 
-__global__ void __launch_bounds__(NTHREADS) k_vjp1v_static(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(NTHREADS, 2) k_vjp1v_static(const DevPlan* __restrict__ gP,
                                                            const double2* __restrict__ gtab,
                                                            const double2* __restrict__ y,
                                                            const double2* __restrict__ w,
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(NTHREADS) k_vjp1v_static(const DevPlan* __rest
   vjp1v_tile(P, stab, y, w, g, part, s, tile, m0, nt, sA, sB, scoef);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_vjp1v_fields_static(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(NTHREADS, 2) k_vjp1v_fields_static(const DevPlan* __restrict__ gP,
                                                                   const double2* __restrict__ gtab,
                                                                   const double2* __restrict__ w,
                                                                   double2* __restrict__ g,

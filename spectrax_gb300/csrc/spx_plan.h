@@ -9,7 +9,8 @@ struct spx_plan {
   std::vector<double2> tab;     // host copy of the table
   spx::DevPlan* d_plan = nullptr;
   double2* d_tab = nullptr;
-  void* d_block = nullptr;      // single allocation holding d_plan and d_tab
+  void* d_block = nullptr;      // single allocation holding d_plan, d_tab and d_ticket
+  unsigned int* d_ticket = nullptr;  // zero between launches: last-CTA ticket of spx_vjp_param
   int device = 0;
   int nsm = 0;
   size_t smem_tab = 0;          // bytes of the table in shared memory

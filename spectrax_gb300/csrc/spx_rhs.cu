@@ -143,8 +143,10 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
     P.tile = T;
     P.ntiles = ntiles;
     pl->smem_1v = pl->smem_tab + (size_t)lines_1v(T, p.Ns) * N * sizeof(double2) + 16 * 4 * sizeof(double);
-    // the VJP keeps one partial field line per (species, tile)
-    pl->ws_bytes = (size_t)p.Ns * ntiles * N * sizeof(double2);
+    // the VJP keeps one partial field line per (species, tile); the fused
+    // VJP + parameter kernel adds per-CTA parameter partials
+    pl->ws_bytes = (size_t)p.Ns * ntiles * N * sizeof(double2) +
+                   (size_t)(p.Ns * ntiles + 1) * (2 + SPX_MAX_SPECIES) * sizeof(double);
   } else {
     P.path = 1;
     pl->smem_gen = pl->smem_tab + 2 * (size_t)P.plane * sizeof(double2);
@@ -161,7 +163,7 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
 }
 
 // ------------------------------------------------------------------ kernels
-__global__ void __launch_bounds__(NTHREADS) k_rhs1v(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(NTHREADS, 2) k_rhs1v(const DevPlan* __restrict__ gP,
                                                     const double2* __restrict__ gtab,
                                                     const double2* __restrict__ y,
                                                     double2* __restrict__ dy) {
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(NTHREADS) k_gen_nl(const DevPlan* __restrict__
   general_nl_plane(P, stab, y, ws, GB, blockIdx.x, sA, sB, epi);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_jvp1v(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(NTHREADS, 2) k_jvp1v(const DevPlan* __restrict__ gP,
                                                     const double2* __restrict__ gtab,
                                                     const double2* __restrict__ y,
                                                     const double2* __restrict__ v,
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(NTHREADS) k_jvp1v(const DevPlan* __restrict__ 
   rhs1v_tile_t<true>(P, stab, y, v, s, n0, nt, sA, sB, scoef, epi);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_vjp1v(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(NTHREADS, 2) k_vjp1v(const DevPlan* __restrict__ gP,
                                                     const double2* __restrict__ gtab,
                                                     const double2* __restrict__ y,
                                                     const double2* __restrict__ w,
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(NTHREADS) k_vjp1v(const DevPlan* __restrict__ 
   vjp1v_tile(P, stab, y, w, g, part, s, tile, m0, nt, sA, sB, scoef);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_vjp1v_fields(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(NTHREADS, 2) k_vjp1v_fields(const DevPlan* __restrict__ gP,
                                                            const double2* __restrict__ gtab,
                                                            const double2* __restrict__ w,
                                                            double2* __restrict__ g,
@@ -419,12 +421,15 @@ int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx
   rc = set_attrs();
   if (rc != SPX_OK) { delete pl; return rc; }
   const size_t hdr = (sizeof(DevPlan) + 255) / 256 * 256;
-  const size_t bytes = hdr + pl->tab.size() * sizeof(double2);
+  const size_t tab_bytes = (pl->tab.size() * sizeof(double2) + 255) / 256 * 256;
+  const size_t bytes = hdr + tab_bytes + 256;
   cudaError_t e = cudaMalloc(&pl->d_block, bytes);
   if (e != cudaSuccess) { delete pl; return cuda_fail(e, "cudaMalloc(plan)"); }
   pl->d_plan = reinterpret_cast<DevPlan*>(pl->d_block);
   pl->d_tab = reinterpret_cast<double2*>(reinterpret_cast<char*>(pl->d_block) + hdr);
-  e = cudaMemcpy(pl->d_plan, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
+  pl->d_ticket = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes);
+  e = cudaMemset(pl->d_ticket, 0, 256);
+  if (e == cudaSuccess) e = cudaMemcpy(pl->d_plan, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !pl->tab.empty())
     e = cudaMemcpy(pl->d_tab, pl->tab.data(), pl->tab.size() * sizeof(double2), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(pl->d_block); delete pl; return cuda_fail(e, "cudaMemcpy(plan)"); }

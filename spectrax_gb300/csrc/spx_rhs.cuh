@@ -631,7 +631,7 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
                                   const double2* __restrict__ y, const double2* __restrict__ w,
                                   double2* __restrict__ g, double2* __restrict__ part,
                                   int s, int tile, int m0, int nt, double2* sA, double2* sB,
-                                  double* scoef) {
+                                  double* scoef, double* pacc = nullptr) {
   const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
   const double2* __restrict__ Cs = y + (size_t)s * Nn * N;
   const double2* __restrict__ Ws = w + (size_t)s * Nn * N;
@@ -648,7 +648,7 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
     c[0] = sqrt((double)(m + 1) * 0.5);
     c[1] = sqrt((double)m * 0.5);
     c[2] = (m + 1 < Nn) ? qOc * sqrt(2.0 * (double)(m + 1)) / a0 / (double)N : 0.0;   // k_{m+1}
-    c[3] = P.pb.nu * colc(Nn, m);
+    c[3] = colc(Nn, m);
   }
   for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
     const int l = i / N, c = i - l * N;
@@ -697,6 +697,7 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
   const double Dd = P.pb.D;
   const double iO = 1.0 / P.pb.Omega_cs[0];
   const double pre = P.pb.qs[s] * a0 * a1 * a2;
+  double p_nu = 0.0, p_k = 0.0, p_u = 0.0;     // parameter terms of the own planes (pacc)
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
     const int l = i / N, c = i - l * N;
     const int m = m0 + l;
@@ -706,10 +707,22 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
     const double2 W0 = Ws[(size_t)m * N + c];
     const double2 Wp = (m + 1 < Nn) ? Ws[(size_t)(m + 1) * N + c] : make_double2(0.0, 0.0);
     const double2 Wm = (m >= 1) ? Ws[(size_t)(m - 1) * N + c] : make_double2(0.0, 0.0);
+    if (pacc) {
+      // Re w . df/dtheta at this entry: nu (-col C), k d/dk (streaming), u_x,s (-i K C)
+      const double2 C0 = Cs[(size_t)m * N + c];
+      const double2 Cp = (m + 1 < Nn) ? Cs[(size_t)(m + 1) * N + c] : make_double2(0.0, 0.0);
+      const double2 Cm = (m >= 1) ? Cs[(size_t)(m - 1) * N + c] : make_double2(0.0, 0.0);
+      p_nu += -cf[3] * (W0.x * C0.x - W0.y * C0.y);
+      double2 tc = cscale(ua, C0);
+      tc = crfma(cf[0], Cp, tc);
+      tc = crfma(cf[1], Cm, tc);
+      p_k += W0.x * (wk * tc.y) - W0.y * (-wk * tc.x);
+      p_u += W0.x * (kt.x * C0.y) - W0.y * (-kt.x * C0.x);
+    }
     double2 t = cscale(ua, W0);
     t = crfma(cf[0], Wp, t);
     t = crfma(cf[1], Wm, t);
-    double d = cf[3];
+    double d = P.pb.nu * cf[3];
     if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
     double re = fma(wk, t.y, -d * W0.x);
     double im = fma(-wk, t.x, -d * W0.y);
@@ -730,6 +743,117 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
     }
     g[(size_t)(s * Nn + m) * N + c] = make_double2(re, im);
   }
+  if (pacc) { pacc[0] += p_nu; pacc[1] += p_k; pacc[2] += p_u; }
+}
+
+// VJP tile over operands staged in shared memory (same arithmetic as
+// vjp1v_tile):  Uy / Uw: planes m0-1 .. m0+nt of y and w for species s
+// ((nt+2)*N each, zero outside [0, Nn)); yF3: y's E_x, B_z, B_y lines; wE: w's
+// E_x, E_y, E_z lines (3*N each).  pacc (3 doubles) accumulates the parameter
+// terms of the own planes: Re w . (-col C), Re w . f_K, Re w . (-i K C).
+__device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict__ tab,
+                                    const double2* Uy, const double2* Uw, const double2* yF3,
+                                    const double2* wE, double2* __restrict__ g,
+                                    double2* __restrict__ part, int s, int tile, int m0, int nt,
+                                    double2* sA, double2* sB, double* scoef, double* pacc) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  const double a0 = P.pb.alpha_s[3 * s], a1 = P.pb.alpha_s[3 * s + 1], a2 = P.pb.alpha_s[3 * s + 2];
+  const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
+  const int nl = 2 * nt + 1;
+  if (threadIdx.x < nt) {
+    const int m = m0 + threadIdx.x;
+    double* c = scoef + 4 * threadIdx.x;
+    c[0] = sqrt((double)(m + 1) * 0.5);
+    c[1] = sqrt((double)m * 0.5);
+    c[2] = (m + 1 < Nn) ? qOc * sqrt(2.0 * (double)(m + 1)) / a0 / (double)N : 0.0;   // k_{m+1}
+    c[3] = colc(Nn, m);
+  }
+  // lines: [G_y | c_m (nt) | W_{m+1} (nt)], masked, transform order (U line l = plane m0-1+l)
+  for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    double2 v = make_double2(0.0, 0.0);
+    if (kept(c, N, cut)) {
+      if (l == 0) {
+        v = yF3[c];
+        v = crfma(u1, yF3[N + c], v);
+        v = crfma(-u2, yF3[2 * N + c], v);
+      } else if (l <= nt) {
+        v = Uy[(size_t)l * N + c];                    // plane m0 + l - 1
+      } else {
+        // forward transform of W as conj(inverse transform of conj W), so that all
+        // 2 nt + 1 lines go through one transform pass
+        const double2 wv = Uw[(size_t)(l - nt + 1) * N + c];   // plane m0 + (l - 1 - nt) + 1
+        v = make_double2(wv.x, -wv.y);
+      }
+    }
+    sA[l * N + std_index(c, N)] = v;
+  }
+  __syncthreads();
+  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
+  double2* o = (r == sA) ? sB : sA;
+  double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
+  for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int l = 0; l < nt; ++l) {
+      const double k = scoef[4 * l + 2];
+      const double2 wt = r[(1 + nt + l) * N + x];
+      acc = cfma(cscale(k, r[(1 + l) * N + x]), make_double2(wt.x, -wt.y), acc);
+    }
+    Rp[x] = acc;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int x = i % N;
+    const double2 wt = r[(1 + nt) * N + i];
+    r[(1 + nt) * N + i] = cmul(r[x], make_double2(wt.x, -wt.y));
+  }
+  __syncthreads();
+  double2* q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
+  const double ua = u0 / a0;
+  const double Dd = P.pb.D;
+  const double iO = 1.0 / P.pb.Omega_cs[0];
+  const double pre = P.pb.qs[s] * a0 * a1 * a2;
+  double p_nu = 0.0, p_k = 0.0, p_u = 0.0;
+  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+    const int l = i / N, c = i - l * N;
+    const int m = m0 + l;
+    const double* cf = scoef + 4 * l;
+    const double2 kt = ktab(P, tab, 1, c);
+    const double wk = kt.x * a0;
+    const double2 Wm = Uw[(size_t)l * N + c], W0 = Uw[(size_t)(l + 1) * N + c], Wp = Uw[(size_t)(l + 2) * N + c];
+    const double2 Cm = Uy[(size_t)l * N + c], C0 = Uy[(size_t)(l + 1) * N + c], Cp = Uy[(size_t)(l + 2) * N + c];
+    p_nu += -cf[3] * (W0.x * C0.x - W0.y * C0.y);
+    double2 tc = cscale(ua, C0);
+    tc = crfma(cf[0], Cp, tc);
+    tc = crfma(cf[1], Cm, tc);
+    p_k += W0.x * (wk * tc.y) - W0.y * (-wk * tc.x);
+    p_u += W0.x * (kt.x * C0.y) - W0.y * (-kt.x * C0.x);
+    double2 t = cscale(ua, W0);
+    t = crfma(cf[0], Wp, t);
+    t = crfma(cf[1], Wm, t);
+    double d = P.pb.nu * cf[3];
+    if (Dd != 0.0) d = fma(Dd, kt.y * kt.y, d);
+    double re = fma(wk, t.y, -d * W0.x);
+    double im = fma(-wk, t.x, -d * W0.y);
+    if (m + 1 < Nn && kept(c, N, cut)) {
+      const double2 v = q[l * N + std_index(c, N)];
+      re = fma(cf[2], v.x, re);
+      im = fma(cf[2], v.y, im);
+    }
+    if (m == 0) {
+      const double2 ex = wE[c], ey = wE[N + c], ez = wE[2 * N + c];
+      const double co = -pre * iO;
+      re = fma(co, fma(u0, ex.x, fma(u1, ey.x, u2 * ez.x)), re);
+      im = fma(co, fma(u0, ex.y, fma(u1, ey.y, u2 * ez.y)), im);
+    } else if (m == 1) {
+      const double co = -pre * iO * a0 * 0.70710678118654752440;
+      re = fma(co, wE[c].x, re);
+      im = fma(co, wE[c].y, im);
+    }
+    g[(size_t)(s * Nn + m) * N + c] = make_double2(re, im);
+  }
+  pacc[0] += p_nu; pacc[1] += p_k; pacc[2] += p_u;
 }
 
 // VJP of the fused 1D1V path, pass 2 (fields): one CTA.
@@ -741,9 +865,18 @@ __device__ inline void vjp1v_fields(const DevPlan& P, const double2* __restrict_
   const int N = P.ax[1].n, cut = P.ax[1].cut, Ns = P.pb.Ns;
   for (int i = threadIdx.x; i < Ns * N; i += blockDim.x) {
     const int s = i / N, x = i - s * N;
-    double2 acc = make_double2(0.0, 0.0);
-    for (int t = 0; t < P.ntiles; ++t) acc = cadd(acc, part[((size_t)s * P.ntiles + t) * N + x]);
-    sA[s * N + x] = acc;
+    // four interleaved partial sums (tiles t = 4q + r), combined in a fixed order
+    const double2* pt = part + (size_t)s * P.ntiles * N + x;
+    double2 a0 = make_double2(0.0, 0.0), a1 = a0, a2 = a0, a3 = a0;
+    int t = 0;
+    for (; t + 4 <= P.ntiles; t += 4) {
+      a0 = cadd(a0, pt[(size_t)t * N]);
+      a1 = cadd(a1, pt[(size_t)(t + 1) * N]);
+      a2 = cadd(a2, pt[(size_t)(t + 2) * N]);
+      a3 = cadd(a3, pt[(size_t)(t + 3) * N]);
+    }
+    for (; t < P.ntiles; ++t) a0 = cadd(a0, pt[(size_t)t * N]);
+    sA[s * N + x] = cadd(cadd(a0, a1), cadd(a2, a3));
   }
   __syncthreads();
   double2* r = fft_axis_t<true, true>(sA, sB, P.ax[1], tab, Lines{Ns, 1, 1, N, 0}, cut);

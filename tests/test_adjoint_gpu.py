@@ -68,3 +68,33 @@ def test_autograd_function_wiring():
     _, g = prob.loss_and_grad(0.35, 1.0, 0.5, 1e-3)
     assert abs(k.grad.item() - g["k"]) <= 1e-12 * abs(g["k"])
     assert abs(amp.grad.item() - g["amp"]) <= 1e-12 * abs(g["amp"])
+
+
+@pytest.mark.gpu
+def test_fused_vjp_param_matches_separate_kernels():
+    import ctypes as C
+    import torch
+    from spectrax_gb300 import _lib
+    from spectrax_gb300.adjoint import two_stream_setup
+    from spectrax_gb300.vector_field import plan_for_params
+    p, bg, delta, _ = two_stream_setup(0.3, 1.2, 0.5, 1e-3, 17, 24, seed=2)
+    plan = plan_for_params(p, "divide")
+    n = plan.state_len
+    rng = np.random.default_rng(5)
+    y = torch.from_numpy(bg + 1e-2 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))).cuda()
+    w = torch.from_numpy(rng.standard_normal(n) + 1j * rng.standard_normal(n)).cuda()
+    g1, g2 = torch.empty_like(y), torch.empty_like(y)
+    a1 = torch.zeros(2 + 3, dtype=torch.float64, device="cuda")
+    a2 = torch.full((2 + 3,), 0.25, dtype=torch.float64, device="cuda")     # accumulates onto its input
+    L = _lib.lib()
+    ws, wsb = plan.ws_ptr()
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+    _lib.check(L.spx_vjp(plan.handle, ptr(y), ptr(w), ptr(g1), ws, wsb, None), "spx_vjp")
+    _lib.check(L.spx_param_dots(plan.handle, ptr(y), ptr(w), dp(a1), None), "spx_param_dots")
+    for _ in range(2):                                  # the ticket resets itself
+        _lib.check(L.spx_vjp_param(plan.handle, ptr(y), ptr(w), ptr(g2), dp(a2), ws, wsb, None), "spx_vjp_param")
+    torch.cuda.synchronize()
+    # same algebra; the fused kernel forms the forward transform of w as conj(inverse(conj w))
+    assert (torch.linalg.vector_norm(g1 - g2) / torch.linalg.vector_norm(g1)).item() < 1e-13
+    np.testing.assert_allclose((a2.cpu().numpy() - 0.25) / 2, a1.cpu().numpy(), rtol=1e-12, atol=1e-300)
