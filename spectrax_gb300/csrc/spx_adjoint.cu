@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_rk_stage_st(const DevPlan* __re
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   load_plan(P, stab, gP, gtab);
   if (threadIdx.x == 0) fill_terms_fixed(terms, stage, h);
+  pdl_wait_and_release();
   __syncthreads();
   const long long len = P.nc + 6LL * P.plane;
   StageIO io;
@@ -77,6 +78,7 @@ struct LinTerms {
 };
 
 __global__ void k_lincomb(LinTerms t, double2* __restrict__ out, long long len) {
+  pdl_wait_and_release();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len;
        i += (long long)gridDim.x * blockDim.x) {
     double2 acc = make_double2(0.0, 0.0);
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
                                                               unsigned int* ticket, double* acc) {
   __shared__ DevPlan P;
   __shared__ double red[NTHREADS / 32][2 + SPX_MAX_SPECIES];
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bars[2];
   __shared__ int last;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
@@ -211,37 +213,46 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
   for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k) loc[k] = 0.0;
   const int b = blockIdx.x;
   bool timed_out = false;
-  if (b < nblk) {
-    const int s = b / P.ntiles, tile = b % P.ntiles;
-    const int m0 = tile * T, nt = min(T, Nn - m0);
+  // y (the stage input) does not depend on the previous launch (the combination
+  // that forms w): its planes are requested first
+  const bool tile_cta = b < nblk;
+  const int s = tile_cta ? b / P.ntiles : 0, tile = tile_cta ? b % P.ntiles : 0;
+  const int m0 = tile * T, nt = tile_cta ? min(T, Nn - m0) : 0;
+  const size_t sbase = (size_t)s * Nn * N;
+  const int lo = max(m0 - 1, 0), hi = min(m0 + nt, Nn - 1);
+  const uint32_t bu = (uint32_t)((hi - lo + 1) * N * sizeof(double2));
+  const uint32_t bf = (uint32_t)(N * sizeof(double2));
+  const size_t d0 = (size_t)(lo - (m0 - 1)) * N;
+  if (nt > 0) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bars[0], 1);
+      mbar_init(&bars[1], 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_arm(&bars[0], bu + 3 * bf);
+      bulk_g2s(Uy + d0, y + sbase + (size_t)lo * N, bu, &bars[0]);
+      const double2* F = y + P.nc;
+      bulk_g2s(yF3, F, bf, &bars[0]);                          // E_x
+      bulk_g2s(yF3 + N, F + 5 * (size_t)N, bf, &bars[0]);      // B_z
+      bulk_g2s(yF3 + 2 * N, F + 4 * (size_t)N, bf, &bars[0]);  // B_y
+    }
+  }
+  pdl_wait_and_release();
+  if (tile_cta) {
     if (nt > 0) {
-      // stage y and w planes m0-1 .. m0+nt, y's G lines and w's E lines
-      const size_t sbase = (size_t)s * Nn * N;
       if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_mbar_init();
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        const int lo = max(m0 - 1, 0), hi = min(m0 + nt, Nn - 1);
-        const uint32_t bu = (uint32_t)((hi - lo + 1) * N * sizeof(double2));
-        const uint32_t bf = (uint32_t)(N * sizeof(double2));
-        mbar_arm(&bar, 2 * bu + 6 * bf);
-        const size_t d0 = (size_t)(lo - (m0 - 1)) * N;
-        bulk_g2s(Uy + d0, y + sbase + (size_t)lo * N, bu, &bar);
-        bulk_g2s(Uw + d0, w + sbase + (size_t)lo * N, bu, &bar);
-        const double2* F = y + P.nc;
-        bulk_g2s(yF3, F, bf, &bar);                          // E_x
-        bulk_g2s(yF3 + N, F + 5 * (size_t)N, bf, &bar);      // B_z
-        bulk_g2s(yF3 + 2 * N, F + 4 * (size_t)N, bf, &bar);  // B_y
-        bulk_g2s(wE, w + P.nc, 3 * bf, &bar);                // w's E_x, E_y, E_z
+        mbar_arm(&bars[1], bu + 3 * bf);
+        bulk_g2s(Uw + d0, w + sbase + (size_t)lo * N, bu, &bars[1]);
+        bulk_g2s(wE, w + P.nc, 3 * bf, &bars[1]);                // w's E_x, E_y, E_z
       }
       if (m0 == 0)
         for (int i = threadIdx.x; i < N; i += blockDim.x) Uy[i] = Uw[i] = make_double2(0.0, 0.0);
       if (m0 + nt == Nn)
         for (int i = threadIdx.x; i < N; i += blockDim.x)
           Uy[(size_t)(nt + 1) * N + i] = Uw[(size_t)(nt + 1) * N + i] = make_double2(0.0, 0.0);
-      const bool ok = mbar_wait_bounded(&bar, 0);
+      const bool ok = mbar_wait_bounded(&bars[0], 0) && mbar_wait_bounded(&bars[1], 0);
       if (__syncthreads_or(!ok)) {
         timed_out = true;
       } else {
@@ -338,14 +349,15 @@ int spx_rk_step_store(const spx_plan* pl, const void* y, double h, void* Ystages
   if (npf < 1) { set_error("spx_rk_step_store: Nx / tile too large for the stage kernel"); return SPX_E_UNSUPPORTED; }
   const int grid = P.pb.Ns * P.ntiles + 1;
   for (int stage = 0; stage < rk::S; ++stage) {
+    const DevPlan* dp = pl->d_plan;
+    const double2* dt = pl->d_tab;
+    const double2* yb = Yb;
+    double2* kb = static_cast<double2*>(Kstages);
+    double2* yn = static_cast<double2*>(ynext);
     if (stage < rk::S - 1)
-      k_rk_stage_st<false><<<grid, pl->threads, smem, st>>>(pl->d_plan, pl->d_tab, Yb, Yb,
-                                                              static_cast<double2*>(Kstages),
-                                                              static_cast<double2*>(ynext), h, stage, npf);
+      SPX_CUDA(launch_pdl(k_rk_stage_st<false>, grid, pl->threads, smem, st, dp, dt, yb, Yb, kb, yn, h, stage, npf));
     else
-      k_rk_stage_st<true><<<grid, pl->threads, smem, st>>>(pl->d_plan, pl->d_tab, Yb, Yb,
-                                                             static_cast<double2*>(Kstages),
-                                                             static_cast<double2*>(ynext), h, stage, npf);
+      SPX_CUDA(launch_pdl(k_rk_stage_st<true>, grid, pl->threads, smem, st, dp, dt, yb, Yb, kb, yn, h, stage, npf));
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
@@ -425,9 +437,13 @@ int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, dou
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int T = P.tile, N = P.ax[1].n;
   const size_t smem = pl->smem_tab + (size_t)(6 * T + 12) * N * sizeof(double2) + 64 * sizeof(double);
-  k_vjp_param_1v<<<grid, pl->threads, smem, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y),
-                                                         static_cast<const double2*>(w), static_cast<double2*>(g),
-                                                         reinterpret_cast<double2*>(wsb), pp, ticket, acc);
+  const DevPlan* dp = pl->d_plan;
+  const double2* dt = pl->d_tab;
+  // a plain launch: with a programmatic early start the CTAs of this small grid
+  // (one per SM) were placed less evenly and the kernel ran longer
+  k_vjp_param_1v<<<grid, pl->threads, smem, st>>>(dp, dt, static_cast<const double2*>(y),
+                                                  static_cast<const double2*>(w), static_cast<double2*>(g),
+                                                  reinterpret_cast<double2*>(wsb), pp, ticket, acc);
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
 }

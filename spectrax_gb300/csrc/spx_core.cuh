@@ -34,6 +34,14 @@ struct AxisPlan {
   int kofs;              // offset of the per-axis k table: (k_c / L, k_c) pairs, n entries
 };
 
+// Programmatic dependent launch: wait until the previous launch in the stream
+// has completed and its writes are visible, then let the next launch start its
+// own prologue.  Both are no-ops when the launch has no programmatic dependency.
+__device__ __forceinline__ void pdl_wait_and_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Shared-memory lines (of N double2) after the table on the fused 1D1V path:
 // two JVP line buffers of 2T+2 lines, or the gathered field CTA's 2*Ns+6 lines.
 __host__ __device__ __forceinline__ int lines_1v(int T, int Ns) {

@@ -63,13 +63,6 @@ __device__ __forceinline__ T* pick(T* const (&p)[2], int i) { return i ? p[1] : 
 __constant__ double cCoef[14][13];
 __constant__ int cMask[14];
 
-// Programmatic dependent launch: wait until the previous launch in the stream
-// has completed and its writes are visible, then let the next launch start its
-// own prologue.  Both are no-ops when the launch has no programmatic dependency.
-__device__ __forceinline__ void pdl_wait_and_release() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
 
 struct Attempt {
   double h, t_stop;
@@ -548,22 +541,6 @@ static int d8_attrs() {
   return SPX_OK;
 }
 
-// Launch with a programmatic dependency on the previous kernel in the stream, so
-// its prologue overlaps the tail of that kernel.
-template <class... Args>
-static void launch_pdl(void (*k)(Args...), int grid, int threads, size_t smem, cudaStream_t st, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid, 1, 1);
-  cfg.blockDim = dim3(threads, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k, args...);
-}
 
 static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;

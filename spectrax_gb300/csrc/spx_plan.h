@@ -31,6 +31,25 @@ int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, c
 int smem_optin();
 }  // namespace spx
 
+namespace spx {
+// Launch with a programmatic dependency on the previous kernel in the stream, so
+// its prologue overlaps the tail of that kernel.
+template <class... Args>
+inline cudaError_t launch_pdl(void (*k)(Args...), int grid, int threads, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+}  // namespace spx
+
 #define SPX_CUDA(call)                                         \
   do {                                                         \
     cudaError_t e__ = (call);                                  \
