@@ -327,8 +327,13 @@ def run_ours(args):
     from spectrax_gb300.vector_field import plan_for_params
 
     p, y0 = two_stream_params(seed=rank)
-    # tile / CTA width autotuned on Dopri8 attempts of this very state
-    plan = plan_for_params(p, "divide", tuned=True, tune_for="dopri8", sample=torch.from_numpy(y0))
+    if args.tile > 0:
+        # a fixed plan (e.g. the autotuner's earlier choice, for profiling runs)
+        from spectrax_gb300.vector_field import get_plan, problem_from_params
+        plan = get_plan(problem_from_params(p, "divide"), None, args.tile, args.threads)
+    else:
+        # tile / CTA width autotuned on Dopri8 attempts of this very state
+        plan = plan_for_params(p, "divide", tuned=True, tune_for="dopri8", sample=torch.from_numpy(y0))
     n = plan.state_len
     solver = Dopri8Solver(plan, 0.0, 1e9, 0.01, ts=None, adaptive=True, rtol=RTOL, atol=ATOL,
                           max_steps=1 << 40, save_states=False, masses=[1.0, 1.0, 1836.0])
@@ -437,6 +442,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--extras", type=int, default=1, help="also time the batched scan and the adjoint")
     ap.add_argument("--scan-t1", type=float, default=4.0, help="horizon of the batched scan extra")
+    ap.add_argument("--tile", type=int, default=0, help="Hermite planes per CTA (0: autotune)")
+    ap.add_argument("--threads", type=int, default=256, help="CTA width when --tile is given")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
