@@ -180,8 +180,8 @@ __global__ void __launch_bounds__(NTHREADS) k_param_dots_1v(const DevPlan* __res
 // g = J(y)^T w and acc[k] += Re sum_e w_e (df/dtheta_k)_e.  Tile CTAs run the
 // VJP tile and the parameter terms of their own planes, the extra CTA those of
 // the field entries; every CTA writes its partial sums, and the last to arrive
-// (atomic ticket) forms the field gradient from the tiles' partial field sums
-// and adds the parameter partials to acc in CTA order (deterministic).
+// (atomic ticket) sums the tiles' transformed field partials into the field
+// gradient and adds the parameter partials to acc in a fixed order.
 // ws: part (Ns * ntiles * N double2) | pp (grid x (2 + SPX_MAX_SPECIES) doubles); the
 // ticket lives in the plan (calls on one plan are serialised, as its workspace is).
 __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __restrict__ gP,
@@ -200,10 +200,10 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
   const int nblk = P.pb.Ns * P.ntiles;
   const int N = P.ax[1].n, Nn = P.pb.Nn, T = P.tile;
   const int nk = 2 + P.pb.Ns;
-  // work area: sA, sB (2T+1 lines each) | Uy, Uw (T+2 lines each) | yF3, wE (3 lines each) | coefficients
+  // work area: sA, sB (2T+2 lines each) | Uy, Uw (T+2 lines each) | yF3, wE (3 lines each) | coefficients
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + (size_t)(2 * T + 1) * N;
-  double2* Uy = sB + (size_t)(2 * T + 1) * N;
+  double2* sB = sA + (size_t)(2 * T + 2) * N;
+  double2* Uy = sB + (size_t)(2 * T + 2) * N;
   double2* Uw = Uy + (size_t)(T + 2) * N;
   double2* yF3 = Uw + (size_t)(T + 2) * N;
   double2* wE = yF3 + 3 * (size_t)N;
@@ -278,14 +278,21 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // the field pass ping-pongs Ns lines: second buffer after max(2T+1, Ns) lines
-  // (6T + 12 >= 2 Ns for every Ns <= 8, so both fit in the work area)
-  vjp1v_fields(P, stab, w, g, part, sA, sA + (size_t)max(2 * T + 1, P.pb.Ns) * N);
-  if ((int)threadIdx.x < nk) {
-    double sum = 0.0;
-    for (int q = 0; q < (int)gridDim.x; ++q) sum += __ldcg(pp + (size_t)q * (2 + SPX_MAX_SPECIES) + threadIdx.x);
-    acc[threadIdx.x] += sum;
+  // field pass over the tiles' transformed partials (Ns lines of scratch)
+  vjp1v_fields_spectral(P, stab, w + P.nc, g + P.nc, part, sA);
+  // parameter partials: every thread loads its CTAs' values at once, then a
+  // fixed-order block reduction per parameter
+  __syncthreads();
+  double part_k[2 + SPX_MAX_SPECIES];
+#pragma unroll
+  for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k) part_k[k] = 0.0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k)
+      if (k < nk) part_k[k] += __ldcg(pp + (size_t)q * (2 + SPX_MAX_SPECIES) + k);
   }
+  const double tot = block_sums(part_k, nk, red);
+  if ((int)threadIdx.x < nk) acc[threadIdx.x] += tot;
   if (threadIdx.x == 0) *ticket = 0;
 }
 
@@ -436,7 +443,7 @@ int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, dou
   unsigned int* ticket = pl->d_ticket;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int T = P.tile, N = P.ax[1].n;
-  const size_t smem = pl->smem_tab + (size_t)(6 * T + 12) * N * sizeof(double2) + 64 * sizeof(double);
+  const size_t smem = pl->smem_tab + (size_t)(6 * T + 14) * N * sizeof(double2) + 64 * sizeof(double);
   const DevPlan* dp = pl->d_plan;
   const double2* dt = pl->d_tab;
   // a plain launch: with a programmatic early start the CTAs of this small grid

@@ -792,7 +792,9 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
   __syncthreads();
   double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
   double2* o = (r == sA) ? sB : sA;
-  double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
+  // this tile's share of the field sum R_s(x) = sum_n k_n c_{n-1}(x) W_n(x), as an
+  // extra line after the nt product lines: its inverse transform (masked) goes
+  // through the same pass, and the tile stores the kept modes as its partial
   for (int x = threadIdx.x; x < N; x += blockDim.x) {
     double2 acc = make_double2(0.0, 0.0);
     for (int l = 0; l < nt; ++l) {
@@ -800,7 +802,7 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
       const double2 wt = r[(1 + nt + l) * N + x];
       acc = cfma(cscale(k, r[(1 + l) * N + x]), make_double2(wt.x, -wt.y), acc);
     }
-    Rp[x] = acc;
+    r[(1 + 2 * nt) * N + x] = acc;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
@@ -809,7 +811,10 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
     r[(1 + nt) * N + i] = cmul(r[x], make_double2(wt.x, -wt.y));
   }
   __syncthreads();
-  double2* q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
+  double2* q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
+  double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
+  for (int c = threadIdx.x; c < N; c += blockDim.x)
+    Rp[c] = kept(c, N, cut) ? q[nt * N + std_index(c, N)] : make_double2(0.0, 0.0);
   const double ua = u0 / a0;
   const double Dd = P.pb.D;
   const double iO = 1.0 / P.pb.Omega_cs[0];
@@ -865,18 +870,22 @@ __device__ inline void vjp1v_fields(const DevPlan& P, const double2* __restrict_
   const int N = P.ax[1].n, cut = P.ax[1].cut, Ns = P.pb.Ns;
   for (int i = threadIdx.x; i < Ns * N; i += blockDim.x) {
     const int s = i / N, x = i - s * N;
-    // four interleaved partial sums (tiles t = 4q + r), combined in a fixed order
+    // eight interleaved partial sums (tiles t = 8q + r, eight loads in flight),
+    // combined in a fixed order
     const double2* pt = part + (size_t)s * P.ntiles * N + x;
-    double2 a0 = make_double2(0.0, 0.0), a1 = a0, a2 = a0, a3 = a0;
+    double2 a[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) a[r] = make_double2(0.0, 0.0);
     int t = 0;
-    for (; t + 4 <= P.ntiles; t += 4) {
-      a0 = cadd(a0, pt[(size_t)t * N]);
-      a1 = cadd(a1, pt[(size_t)(t + 1) * N]);
-      a2 = cadd(a2, pt[(size_t)(t + 2) * N]);
-      a3 = cadd(a3, pt[(size_t)(t + 3) * N]);
+    for (; t + 8 <= P.ntiles; t += 8) {
+      double2 v[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = __ldcg(pt + (size_t)(t + r) * N);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) a[r] = cadd(a[r], v[r]);
     }
-    for (; t < P.ntiles; ++t) a0 = cadd(a0, pt[(size_t)t * N]);
-    sA[s * N + x] = cadd(cadd(a0, a1), cadd(a2, a3));
+    for (int r = 0; t < P.ntiles; ++t, ++r) a[r] = cadd(a[r], __ldcg(pt + (size_t)t * N));
+    sA[s * N + x] = cadd(cadd(cadd(a[0], a[1]), cadd(a[2], a[3])), cadd(cadd(a[4], a[5]), cadd(a[6], a[7])));
   }
   __syncthreads();
   double2* r = fft_axis_t<true, true>(sA, sB, P.ax[1], tab, Lines{Ns, 1, 1, N, 0}, cut);
@@ -896,6 +905,58 @@ __device__ inline void vjp1v_fields(const DevPlan& P, const double2* __restrict_
     const double2 wEy = Wf[N + c], wEz = Wf[2 * N + c];
     const double2 wBy = Wf[4 * N + c], wBz = Wf[5 * N + c];
     // i K x w_B with K = (Kx, 0, 0): (0, -Kx wBz, Kx wBy) * i
+    const double2 kbx = make_double2(0, 0);
+    const double2 kby = cscale(-Kx, wBz), kbz = cscale(Kx, wBy);
+    const double2 kex = make_double2(0, 0);
+    const double2 key = cscale(-Kx, wEz), kez = cscale(Kx, wEy);
+    gF[c] = make_double2(-kbx.y + gx.x, kbx.x + gx.y);
+    gF[N + c] = make_double2(-kby.y, kby.x);
+    gF[2 * N + c] = make_double2(-kbz.y, kbz.x);
+    gF[3 * N + c] = make_double2(kex.y, -kex.x);
+    gF[4 * N + c] = make_double2(key.y + gy.x, -key.x + gy.y);
+    gF[5 * N + c] = make_double2(kez.y + gz.x, -kez.x + gz.y);
+  }
+}
+
+// Field pass of the staged VJP (one CTA): like vjp1v_fields, with per-tile
+// partials that the tiles already transformed (kept modes, centred order), so
+// only their sum over tiles (eight loads in flight, fixed order) is left here.
+__device__ inline void vjp1v_fields_spectral(const DevPlan& P, const double2* __restrict__ tab,
+                                             const double2* __restrict__ Wf, double2* __restrict__ gF,
+                                             const double2* __restrict__ part, double2* sA) {
+  const int N = P.ax[1].n, cut = P.ax[1].cut, Ns = P.pb.Ns;
+  for (int i = threadIdx.x; i < Ns * N; i += blockDim.x) {
+    const int s = i / N, c = i - s * N;
+    if (!kept(c, N, cut)) { sA[i] = make_double2(0.0, 0.0); continue; }
+    const double2* pt = part + (size_t)s * P.ntiles * N + c;
+    double2 a[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) a[r] = make_double2(0.0, 0.0);
+    int t = 0;
+    for (; t + 8 <= P.ntiles; t += 8) {
+      double2 v[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = __ldcg(pt + (size_t)(t + r) * N);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) a[r] = cadd(a[r], v[r]);
+    }
+    for (int r = 0; t < P.ntiles; ++t, ++r) a[r] = cadd(a[r], __ldcg(pt + (size_t)t * N));
+    sA[i] = cadd(cadd(cadd(a[0], a[1]), cadd(a[2], a[3])), cadd(cadd(a[4], a[5]), cadd(a[6], a[7])));
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    double2 gx = make_double2(0, 0), gy = make_double2(0, 0), gz = make_double2(0, 0);
+    if (kept(c, N, cut)) {
+      for (int s = 0; s < Ns; ++s) {
+        const double2 v = sA[s * N + c];
+        gx = cadd(gx, v);
+        gy = crfma(-P.pb.u_s[3 * s + 2], v, gy);   // d G / d B_y = -u_z
+        gz = crfma(P.pb.u_s[3 * s + 1], v, gz);    // d G / d B_z = +u_y
+      }
+    }
+    const double Kx = ktab(P, tab, 1, c).x;   // Ky = Kz = 0 on this path
+    const double2 wEy = Wf[N + c], wEz = Wf[2 * N + c];
+    const double2 wBy = Wf[4 * N + c], wBz = Wf[5 * N + c];
     const double2 kbx = make_double2(0, 0);
     const double2 kby = cscale(-Kx, wBz), kbz = cscale(Kx, wBy);
     const double2 kex = make_double2(0, 0);
