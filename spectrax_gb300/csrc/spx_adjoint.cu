@@ -182,14 +182,15 @@ __global__ void __launch_bounds__(NTHREADS) k_param_dots_1v(const DevPlan* __res
 // the field entries; every CTA writes its partial sums, and the last to arrive
 // (atomic ticket) sums the tiles' transformed field partials into the field
 // gradient and adds the parameter partials to acc in a fixed order.
-// ws: part (Ns * ntiles * N double2) | pp (grid x (2 + SPX_MAX_SPECIES) doubles); the
-// ticket lives in the plan (calls on one plan are serialised, as its workspace is).
+// ws: part (Ns * ntiles * N double2) | pp (grid x (2 + SPX_MAX_SPECIES) doubles) |
+// gpart (Ns * groups * N double2); the tickets live in the plan (calls on one
+// plan are serialised, as its workspace is).
 __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __restrict__ gP,
                                                               const double2* __restrict__ gtab,
                                                               const double2* __restrict__ y,
                                                               const double2* __restrict__ w,
                                                               double2* __restrict__ g, double2* part, double* pp,
-                                                              unsigned int* ticket, double* acc) {
+                                                              double2* gpart, unsigned int* ticket, double* acc) {
   __shared__ DevPlan P;
   __shared__ double red[NTHREADS / 32][2 + SPX_MAX_SPECIES];
   __shared__ __align__(8) uint64_t bars[2];
@@ -272,14 +273,31 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
   if (timed_out && threadIdx.x == 0) atomicExch(&g_rk_status, SPX_ST_WAIT_TIMEOUT);
   const double v = block_sums(loc, nk, red);
   if ((int)threadIdx.x < nk) pp[(size_t)b * (2 + SPX_MAX_SPECIES) + threadIdx.x] = v;
+  // group of 8 tiles: the last tile of a group to finish sums the group's
+  // partials (while other tiles still run); then every CTA takes the ticket
+  const int ngroups = (P.ntiles + 7) / 8;
+  if (tile_cta) {
+    const int grp = tile >> 3, gsz = min(8, P.ntiles - grp * 8);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(ticket + 64 + s * ngroups + grp, 1u) == (unsigned)gsz - 1);
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      const double2* p0 = part + ((size_t)s * P.ntiles + grp * 8) * N;
+      for (int c = threadIdx.x; c < N; c += blockDim.x)
+        gpart[((size_t)s * ngroups + grp) * N + c] = sum_lines8(p0 + c, gsz, N);
+      if (threadIdx.x == 0) ticket[64 + s * ngroups + grp] = 0;
+    }
+  }
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // field pass over the tiles' transformed partials (Ns lines of scratch)
-  vjp1v_fields_spectral(P, stab, w + P.nc, g + P.nc, part, sA);
+  // field pass over the groups' transformed partials (Ns lines of scratch)
+  vjp1v_fields_spectral(P, stab, w + P.nc, g + P.nc, gpart, ngroups, sA);
   // parameter partials: every thread loads its CTAs' values at once, then a
   // fixed-order block reduction per parameter
   __syncthreads();
@@ -439,6 +457,7 @@ int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, dou
   char* wsb = static_cast<char*>(ws);
   const size_t part_bytes = (size_t)P.pb.Ns * P.ntiles * P.ax[1].n * sizeof(double2);
   double* pp = reinterpret_cast<double*>(wsb + part_bytes);
+  double2* gpart = reinterpret_cast<double2*>(wsb + part_bytes + (size_t)grid * (2 + SPX_MAX_SPECIES) * sizeof(double));
   // the plan's ticket is zero between launches (the last CTA resets it)
   unsigned int* ticket = pl->d_ticket;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -450,7 +469,7 @@ int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, dou
   // (one per SM) were placed less evenly and the kernel ran longer
   k_vjp_param_1v<<<grid, pl->threads, smem, st>>>(dp, dt, static_cast<const double2*>(y),
                                                   static_cast<const double2*>(w), static_cast<double2*>(g),
-                                                  reinterpret_cast<double2*>(wsb), pp, ticket, acc);
+                                                  reinterpret_cast<double2*>(wsb), pp, gpart, ticket, acc);
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
 }

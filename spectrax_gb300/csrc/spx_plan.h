@@ -10,7 +10,8 @@ struct spx_plan {
   spx::DevPlan* d_plan = nullptr;
   double2* d_tab = nullptr;
   void* d_block = nullptr;      // single allocation holding d_plan, d_tab and d_ticket
-  unsigned int* d_ticket = nullptr;  // zero between launches: last-CTA ticket of spx_vjp_param
+  unsigned int* d_ticket = nullptr;  // zero between launches: tickets of spx_vjp_param ([0] completion,
+                                     // [64 + g] group g of 8 Hermite tiles)
   int device = 0;
   int nsm = 0;
   size_t smem_tab = 0;          // bytes of the table in shared memory

@@ -144,9 +144,11 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
     P.ntiles = ntiles;
     pl->smem_1v = pl->smem_tab + (size_t)lines_1v(T, p.Ns) * N * sizeof(double2) + 16 * 4 * sizeof(double);
     // the VJP keeps one partial field line per (species, tile); the fused
-    // VJP + parameter kernel adds per-CTA parameter partials
+    // VJP + parameter kernel adds per-CTA parameter partials and one partial
+    // line per group of 8 tiles
     pl->ws_bytes = (size_t)p.Ns * ntiles * N * sizeof(double2) +
-                   (size_t)(p.Ns * ntiles + 1) * (2 + SPX_MAX_SPECIES) * sizeof(double);
+                   (size_t)(p.Ns * ntiles + 1) * (2 + SPX_MAX_SPECIES) * sizeof(double) +
+                   (size_t)p.Ns * ((ntiles + 7) / 8) * N * sizeof(double2);
   } else {
     P.path = 1;
     pl->smem_gen = pl->smem_tab + 2 * (size_t)P.plane * sizeof(double2);
@@ -422,13 +424,17 @@ int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx
   if (rc != SPX_OK) { delete pl; return rc; }
   const size_t hdr = (sizeof(DevPlan) + 255) / 256 * 256;
   const size_t tab_bytes = (pl->tab.size() * sizeof(double2) + 255) / 256 * 256;
-  const size_t bytes = hdr + tab_bytes + 256;
+  // tickets: [0] the fused VJP's completion ticket, from [64] one counter per
+  // group of 8 Hermite tiles (its group-partial reduction)
+  const size_t ngroups = (size_t)pb->Ns * ((pl->host.ntiles + 7) / 8 + 1);
+  const size_t ticket_bytes = (256 + 4 * ngroups + 255) / 256 * 256;
+  const size_t bytes = hdr + tab_bytes + ticket_bytes;
   cudaError_t e = cudaMalloc(&pl->d_block, bytes);
   if (e != cudaSuccess) { delete pl; return cuda_fail(e, "cudaMalloc(plan)"); }
   pl->d_plan = reinterpret_cast<DevPlan*>(pl->d_block);
   pl->d_tab = reinterpret_cast<double2*>(reinterpret_cast<char*>(pl->d_block) + hdr);
   pl->d_ticket = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes);
-  e = cudaMemset(pl->d_ticket, 0, 256);
+  e = cudaMemset(pl->d_ticket, 0, ticket_bytes);
   if (e == cudaSuccess) e = cudaMemcpy(pl->d_plan, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !pl->tab.empty())
     e = cudaMemcpy(pl->d_tab, pl->tab.data(), pl->tab.size() * sizeof(double2), cudaMemcpyHostToDevice);

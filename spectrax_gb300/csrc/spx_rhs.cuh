@@ -918,30 +918,34 @@ __device__ inline void vjp1v_fields(const DevPlan& P, const double2* __restrict_
   }
 }
 
-// Field pass of the staged VJP (one CTA): like vjp1v_fields, with per-tile
-// partials that the tiles already transformed (kept modes, centred order), so
-// only their sum over tiles (eight loads in flight, fixed order) is left here.
+// Field pass of the staged VJP (one CTA): like vjp1v_fields, with partials the
+// tiles already transformed (kept modes, centred order) and summed per group of
+// 8 tiles, so only the sum over groups is left here.
+// Sum of `cnt` partial lines spaced `stride` entries apart, at entry c (eight
+// loads in flight, a fixed order).
+__device__ __forceinline__ double2 sum_lines8(const double2* __restrict__ p, int cnt, size_t stride) {
+  double2 a[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) a[r] = make_double2(0.0, 0.0);
+  int t = 0;
+  for (; t + 8 <= cnt; t += 8) {
+    double2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = __ldcg(p + (size_t)(t + r) * stride);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) a[r] = cadd(a[r], v[r]);
+  }
+  for (int r = 0; t < cnt; ++t, ++r) a[r] = cadd(a[r], __ldcg(p + (size_t)t * stride));
+  return cadd(cadd(cadd(a[0], a[1]), cadd(a[2], a[3])), cadd(cadd(a[4], a[5]), cadd(a[6], a[7])));
+}
+
 __device__ inline void vjp1v_fields_spectral(const DevPlan& P, const double2* __restrict__ tab,
                                              const double2* __restrict__ Wf, double2* __restrict__ gF,
-                                             const double2* __restrict__ part, double2* sA) {
+                                             const double2* __restrict__ gpart, int ngroups, double2* sA) {
   const int N = P.ax[1].n, cut = P.ax[1].cut, Ns = P.pb.Ns;
   for (int i = threadIdx.x; i < Ns * N; i += blockDim.x) {
     const int s = i / N, c = i - s * N;
-    if (!kept(c, N, cut)) { sA[i] = make_double2(0.0, 0.0); continue; }
-    const double2* pt = part + (size_t)s * P.ntiles * N + c;
-    double2 a[8];
-#pragma unroll
-    for (int r = 0; r < 8; ++r) a[r] = make_double2(0.0, 0.0);
-    int t = 0;
-    for (; t + 8 <= P.ntiles; t += 8) {
-      double2 v[8];
-#pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = __ldcg(pt + (size_t)(t + r) * N);
-#pragma unroll
-      for (int r = 0; r < 8; ++r) a[r] = cadd(a[r], v[r]);
-    }
-    for (int r = 0; t < P.ntiles; ++t, ++r) a[r] = cadd(a[r], __ldcg(pt + (size_t)t * N));
-    sA[i] = cadd(cadd(cadd(a[0], a[1]), cadd(a[2], a[3])), cadd(cadd(a[4], a[5]), cadd(a[6], a[7])));
+    sA[i] = kept(c, N, cut) ? sum_lines8(gpart + (size_t)s * ngroups * N + c, ngroups, N) : make_double2(0.0, 0.0);
   }
   __syncthreads();
   for (int c = threadIdx.x; c < N; c += blockDim.x) {
