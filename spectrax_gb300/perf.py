@@ -109,11 +109,11 @@ def rhs_ops(shape, tile=None, ntiles=None) -> Ops:
         o.add(fma=4, addmul=2, mult=Ns * Nx)                 # G combination
         o.add(fma=8 * Ns + 6, addmul=24, mult=Nx)            # Maxwell + current
         return o
-    def plane(mode):
+    def plane_ops(mode):
         fy, fx, fz = (fft_line_ops(N, N // 3, mode) for N in (Ny, Nx, Nz))
         return Ops(instr=fy.instr * Nx * Nz + fx.instr * Ny * Nz + fz.instr * Ny * Nx,
                    flops=fy.flops * Nx * Nz + fx.flops * Ny * Nz + fz.flops * Ny * Nx)
-    pi, pf = plane("dit"), plane("dif")
+    pi, pf = plane_ops("dit"), plane_ops("dif")
     nplanes = Ns * Nn * Nm * Np
     o.instr += pi.instr * (nplanes + 3 * Ns + 3) + pf.instr * nplanes
     o.flops += pi.flops * (nplanes + 3 * Ns + 3) + pf.flops * nplanes
