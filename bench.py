@@ -269,7 +269,124 @@ def run_extras(args):
                           "loss": L, "gradient": g, "checkpoints": "every ceil(sqrt(2000)) = 45 steps"}
     except Exception as e:
         out["adjoint"] = {"error": repr(e)}
+    for name, fn in (("landau", _extra_landau), ("two_stream_run", _extra_two_stream_run),
+                     ("orszag_tang", _extra_orszag_tang)):
+        try:
+            out[name] = fn()
+        except Exception as e:
+            out[name] = {"error": repr(e)}
     return out
+
+
+def _extra_landau():
+    """Landau damping (Nx=33, Nn=64, k=0.5, nu=2, fixed dt=0.05 to t=40): the fitted damping
+    rate of the field energy (the parity of this run against the oracle is a GPU test)."""
+    import torch
+    from spectrax_gb300.dopri8 import Dopri8Solver, species_masses
+    from spectrax_gb300.fits import landau_damping_rate
+    from spectrax_gb300.params import initialize_simulation_parameters, landau_initial_state
+    from spectrax_gb300.vector_field import plan_for_params
+    Nx, Nn = 33, 64
+    user = landau_user(4 * np.pi)
+    p = initialize_simulation_parameters(user, Nx, 1, 1, Nn, 1, 1, 2, 401, 0.05)
+    y0 = landau_initial_state(p, 0.01)
+    ts = np.linspace(0.0, 40.0, 401)
+    plan = plan_for_params(p, "divide")
+    s = Dopri8Solver(plan, 0.0, 40.0, 0.05, ts=ts, adaptive=False, masses=species_masses(p), max_steps=10000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.reset(torch.from_numpy(y0))
+    s.run()
+    torch.cuda.synchronize()
+    tg = time.perf_counter() - t0
+    st = s.stats()
+    E = s.energies().cpu().numpy()[:, 0]
+    return {"workload": "Landau 1D1V Nx=33 Nn=64 Ns=2 k=0.5 nu=2, Dopri8 dt=0.05 to t=40 (800 steps)",
+            "seconds": tg, "steps_per_s": st["accepted"] / tg, "rhs_evals_per_s": st["rhs_evals"] / tg,
+            "hermitian_stages": st["hermitian"], "damping_rate": landau_damping_rate(ts, E, len(ts))}
+
+
+def landau_user(Lx, nu=2.0, mi_me=1836.0):
+    """Input parameters of the Landau workload (electrons alpha = sqrt2, ions alpha_e sqrt(1/mi_me))."""
+    ae = np.sqrt(2.0)
+    return dict(Lx=Lx, nu=nu, D=0.0, qs=[-1.0, 1.0], alpha_s=[ae] * 3 + [ae * np.sqrt(1 / mi_me)] * 3,
+                u_s=[0.0] * 6, Omega_cs=[1.0, 1.0 / mi_me], mi_me=mi_me)
+
+
+def _extra_two_stream_run():
+    """The two-stream workload to t=100 (adaptive, rtol 1e-10): growth rate and energy drift."""
+    import torch
+    from spectrax_gb300.dopri8 import Dopri8Solver
+    from spectrax_gb300.fits import window_slope
+    from spectrax_gb300.vector_field import plan_for_params
+    p, y0 = two_stream_params(seed=0)
+    plan = plan_for_params(p, "divide", tuned=True, tune_for="dopri8", sample=torch.from_numpy(y0))
+    ts = np.linspace(0.0, 100.0, 201)
+    s = Dopri8Solver(plan, 0.0, 100.0, 0.01, ts=ts, adaptive=True, rtol=RTOL, atol=ATOL,
+                     masses=[1.0, 1.0, 1836.0], save_states=False, max_steps=1 << 30)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.reset(torch.from_numpy(y0))
+    status = s.run()
+    torch.cuda.synchronize()
+    dt_s = time.perf_counter() - t0
+    st = s.stats()
+    en = s.energies().cpu().numpy()
+    E, tot = en[:, 0], en[:, 0] + en[:, 1]
+    return {"workload": WORKLOAD + ", t=0..100, 201 saves", "status": st["status_name"], "seconds": dt_s,
+            "accepted": st["accepted"], "rejected": st["rejected"], "rhs_evals": st["rhs_evals"],
+            "rhs_evals_per_s": st["rhs_evals"] / dt_s, "steps_per_s": st["accepted"] / dt_s,
+            "hermitian_stages": st["hermitian"],
+            "growth_rate_t10_40": 0.5 * window_slope(ts, E, 10.0, 40.0),
+            "total_energy_rel_drift": float(abs(tot[-1] - tot[0]) / abs(tot[0])),
+            "total_energy_abs_drift": float(abs(tot[-1] - tot[0])),
+            "field_plus_electron_energy_rel_drift": float(abs((E[-1] + en[-1, 2] + en[-1, 3]) -
+                                                              (E[0] + en[0, 2] + en[0, 3])) /
+                                                          abs(E[0] + en[0, 2] + en[0, 3])),
+            "field_energy_final": float(E[-1])}
+
+
+def _extra_orszag_tang():
+    """2D3V Orszag-Tang-like state (64x64, 8^3 Hermite, 2 species, 67.5 MB): RHS and JVP rates,
+    three implicit-midpoint steps (Newton-GMRES, restart 30) and the energy change over them."""
+    import torch
+    from spectrax_gb300 import midpoint
+    from spectrax_gb300.maxwellian import orszag_tang_state
+    from spectrax_gb300.params import ImplicitMidpoint
+    from spectrax_gb300.vector_field import plan_for_params
+    p, y0 = orszag_tang_state()
+    plan = plan_for_params(p, "divide")
+    y = torch.from_numpy(y0).cuda()
+    dy = torch.empty_like(y)
+    v = torch.randn_like(y)
+    for _ in range(2):
+        plan.rhs_into(y, dy)
+        plan.jvp_into(y, v, dy)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    for _ in range(10):
+        plan.rhs_into(y, dy)
+    ev[1].record()
+    for _ in range(10):
+        plan.jvp_into(y, v, dy)
+    ev[2].record()
+    torch.cuda.synchronize()
+    rhs_ms, jvp_ms = ev[0].elapsed_time(ev[1]) / 10, ev[1].elapsed_time(ev[2]) / 10
+    n = plan.state_len
+    solver = ImplicitMidpoint(rtol=1e-10, atol=1e-10, restart=30, gmres_tol=1e-10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ys, en, info = midpoint.solve(plan, y, 0.3, 0.1, [0.0, 0.3], solver, [1.0, 25.0], save_states=False)
+    torch.cuda.synchronize()
+    tm = time.perf_counter() - t0
+    tot = en[:, 0] + en[:, 1]
+    return {"workload": "Orszag-Tang 2D3V Nx=Ny=64, Nn=Nm=Np=8, Ns=2 (4.2M coefficients)",
+            "rhs_ms": rhs_ms, "rhs_evals_per_s": 1e3 / rhs_ms,
+            "rhs_hbm_gbs": 32.0 * n / (rhs_ms * 1e-3) / 1e9,
+            "jvp_ms": jvp_ms, "midpoint_steps": info["steps"], "midpoint_s": tm,
+            "midpoint_steps_per_s": info["steps"] / tm, "newton_iterations": info.get("newton"),
+            "jvp_matvecs": info.get("matvecs"),
+            "total_energy_rel_change_3_steps": float(abs(tot[-1] - tot[0]) / abs(tot[0]))}
 
 
 def dist_setup(args):

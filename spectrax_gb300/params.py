@@ -142,6 +142,27 @@ def initial_state(p):
                            np.asarray(p["Fk_0"], np.complex128).ravel()])
 
 
+def landau_initial_state(p, dn=0.01, n=1):
+    """Perturbed-Maxwellian 1D1V initial state of the Landau examples
+    (Examples/1D_Landau_damping.py:41-54): C_{s,0}(k=0) = 1/alpha_s^3, the
+    electrons (species 0) get C_0(-k_n) = +i dn/(2 a^3), C_0(+k_n) = -i dn/(2 a^3)
+    at the centred indices (Nx-1)/2 -/+ n, and E_x(+-k_n) = dn Lx / (4 pi n Omega_0)."""
+    Nx, Nn, Ns = int(p["Nx"]), int(p["Nn"]), int(p["Ns"])
+    if int(p["Ny"]) != 1 or int(p["Nz"]) != 1 or int(p["Nm"]) != 1 or int(p["Np"]) != 1:
+        raise ValueError("landau_initial_state builds 1D1V states")
+    a = np.asarray(p["alpha_s"], np.float64).reshape(Ns, 3)[:, 0]
+    c0 = (Nx - 1) // 2
+    Ck = np.zeros((Ns, Nn, Nx), np.complex128)
+    for s in range(Ns):
+        Ck[s, 0, c0] = 1.0 / a[s] ** 3
+    Ck[0, 0, c0 - n] = 1j * dn / (2 * a[0] ** 3)
+    Ck[0, 0, c0 + n] = -1j * dn / (2 * a[0] ** 3)
+    Fk = np.zeros((6, Nx), np.complex128)
+    Om0 = float(np.asarray(p["Omega_cs"], np.float64).ravel()[0])
+    Fk[0, c0 - n] = Fk[0, c0 + n] = dn * float(p["Lx"]) / (4 * np.pi * n * Om0)
+    return np.concatenate([Ck.ravel(), Fk.ravel()])
+
+
 def make_problem(Nx, Ny, Nz, Nn, Nm, Np, Ns, qs, nu, D, Omega_cs, alpha_s, u_s, Lx, Ly, Lz,
                  mask_mode: str | None = None) -> spx_problem:
     """Pack shapes and physical scalars into ``spx_problem``."""
