@@ -59,6 +59,10 @@ class NewtonGMRES:
         its = 0
         rel = 1.0
         for _cycle in range(self.maxiter):
+            # the projections below always run over all m + 1 basis rows (rows not
+            # yet built are zero), so every cycle issues the same few operation
+            # shapes instead of a new one per Arnoldi step
+            V.zero_()
             V[0].copy_(r / beta)
             H = np.zeros((m + 1, m), np.complex128)
             cs = np.zeros(m, np.complex128)
@@ -70,11 +74,11 @@ class NewtonGMRES:
                 self._A(ymid, V[j], w, c)
                 its += 1
                 # classical Gram-Schmidt, twice
-                h = torch.mv(V[: j + 1].conj(), w)
-                w.sub_(torch.mv(V[: j + 1].T, h))
-                h2 = torch.mv(V[: j + 1].conj(), w)
-                w.sub_(torch.mv(V[: j + 1].T, h2))
-                hh = (h + h2).cpu().numpy()
+                h = torch.mv(V.conj(), w)
+                w.sub_(torch.mv(V.T, h))
+                h2 = torch.mv(V.conj(), w)
+                w.sub_(torch.mv(V.T, h2))
+                hh = (h + h2)[: j + 1].cpu().numpy()
                 hn = torch.linalg.vector_norm(w).item()
                 H[: j + 1, j] = hh
                 H[j + 1, j] = hn
