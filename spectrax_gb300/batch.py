@@ -207,17 +207,22 @@ def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses
 def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermitian=False):
     """Solve the instances one after another with the single-instance device
     Dopri8 (plain GPU right-hand side per stage).  Returns (final states, stats,
-    energies, seconds).  hermitian=False keeps the general complex-transform
-    stages, the same arithmetic as the batched kernel."""
+    energies, seconds); the plans and solvers (device buffers, captured graphs)
+    are built before the clock starts, so the seconds cover only the solves.
+    hermitian=False keeps the general complex-transform stages, the same
+    arithmetic as the batched kernel."""
     from .dopri8 import Dopri8Solver
+    solvers = []
+    for it in insts:
+        plan = get_plan(it["problem"])
+        solvers.append(Dopri8Solver(plan, 0.0, t1, dt0, ts=save_ts, adaptive=True, rtol=rtol, atol=atol,
+                                    save_states=False, masses=it.get("masses"), hermitian=hermitian))
+    y0s = [torch.from_numpy(it["y0"]).to(solvers[0].plan.device) for it in insts]
     finals, stats, ens = [], [], []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for it in insts:
-        plan = get_plan(it["problem"])
-        s = Dopri8Solver(plan, 0.0, t1, dt0, ts=save_ts, adaptive=True, rtol=rtol, atol=atol,
-                         save_states=False, masses=it.get("masses"), hermitian=hermitian)
-        s.reset(torch.from_numpy(it["y0"]))
+    for s, y0 in zip(solvers, y0s):
+        s.reset(y0)
         s.run()
         finals.append(s.state())
         stats.append(s.stats())
