@@ -31,6 +31,8 @@ namespace cg = cooperative_groups;
 
 namespace spx {
 
+constexpr int BATCH_MAX_TILE = 32;   // Hermite planes per tile at most
+
 __constant__ double bCoef[14][13];
 __constant__ int bMask[14];
 
@@ -252,7 +254,14 @@ __device__ void batch_energies(const DevPlan& P, const double2* Y, const double*
   }
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_batch(BArgs a) {
+// CTAs per SM the register allocation aims at
+// (2: two CTAs per SM at up to 128 registers; measured faster on the Landau scan
+// than one CTA per SM at 255 registers, despite a few hundred bytes of spills)
+#ifndef SPX_BATCH_MIN_BLOCKS
+#define SPX_BATCH_MIN_BLOCKS 2
+#endif
+
+__global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   const int crank = (int)cl.block_rank();
   const int C = (int)cl.num_blocks();
@@ -562,7 +571,7 @@ extern "C" {
 int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o, spx_batch** out) {
   if (!pbs || !o || !out || n <= 0) { set_error("spx_batch_create: bad argument"); return SPX_E_ARG; }
   *out = nullptr;
-  if (o->cluster < 1 || o->cluster > 8) { set_error("spx_batch_create: cluster must be 1..8"); return SPX_E_ARG; }
+  if (o->cluster < 1 || o->cluster > 16) { set_error("spx_batch_create: cluster must be 1..16"); return SPX_E_ARG; }
   if (!(o->t1 >= 0.0) || !(o->dt0 > 0.0) || o->max_steps <= 0 || o->nsave < 0 || (o->nsave && !o->save_ts)) {
     set_error("spx_batch_create: bad options"); return SPX_E_ARG;
   }
@@ -597,7 +606,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     I.P = tmp.host;
     // batch tiling: `tile` planes per tile (0: 8)
     int T = o->tile > 0 ? o->tile : 8;
-    T = std::min(std::min(T, 16), p.Nn);   // the per-plane coefficient scratch holds 16 planes
+    T = std::min(std::min(T, BATCH_MAX_TILE), p.Nn);   // the per-plane coefficient scratch holds 32 planes
     int ntiles = (p.Nn + T - 1) / T;
     T = (p.Nn + ntiles - 1) / ntiles;
     I.P.tile = T;
@@ -636,7 +645,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
   b->smem = ((size_t)tab_max * sizeof(double2) + 255) / 256 * 256 + (size_t)work_max * sizeof(double2) +
-            16 * 4 * sizeof(double);
+            BATCH_MAX_TILE * 4 * sizeof(double);
   const int optin = smem_optin();
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, k_batch);
@@ -647,6 +656,8 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     return SPX_E_UNSUPPORTED;
   }
   e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  // clusters of more than 8 CTAs need the non-portable size opt-in
+  if (e == cudaSuccess && o->cluster > 8) e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) { batch_free(b); return cuda_fail(e, "cudaFuncSetAttribute(k_batch)"); }
   // persistent grid: as many clusters as can be co-resident
   {
