@@ -181,6 +181,10 @@ typedef struct spx_dopri8_opts {
                            bit for bit, every plane) on the fused 1D1V path with odd Nx; when it
                            holds, evaluate stages with packed real transforms (half the FFTs).
                            The symmetry is then kept exactly by every stage.  0: never. */
+  int32_t persistent; /* 1: on the fused 1D1V path, run all attempts of a replay in one
+                           cooperative launch whose CTAs chain stages through completion
+                           counters (used when every CTA fits on the GPU at once);
+                           0: one launch per stage. */
 } spx_dopri8_opts;
 
 typedef struct spx_dopri8 spx_dopri8;   /* opaque: stage buffers + CUDA graph */
@@ -191,7 +195,7 @@ typedef struct spx_dopri8_stats {
   int64_t accepted, rejected, rhs_evals;
   int32_t status, saved;
   int32_t hermitian;  /* 1 if the packed real-transform stages are in use */
-  int32_t pad;
+  int32_t persistent; /* 1 if attempts run in the persistent cooperative kernel */
 } spx_dopri8_stats;
 
 /*

@@ -54,6 +54,7 @@ class spx_dopri8_opts(C.Structure):
         ("save_states", C.c_int32),
         ("masses", C.POINTER(C.c_double)),
         ("hermitian", C.c_int32),
+        ("persistent", C.c_int32),
     ]
 
 
@@ -62,7 +63,7 @@ class spx_dopri8_stats(C.Structure):
         ("t", C.c_double), ("dt", C.c_double),
         ("accepted", C.c_int64), ("rejected", C.c_int64), ("rhs_evals", C.c_int64),
         ("status", C.c_int32), ("saved", C.c_int32),
-        ("hermitian", C.c_int32), ("pad", C.c_int32),
+        ("hermitian", C.c_int32), ("persistent", C.c_int32),
     ]
 
 

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_rk_stage_st(const DevPlan* __re
   io.rtol = io.atol = 0.0;
   io.adaptive = 0;
   io.timeout_status = &g_rk_status;
+  io.persistent = false;
   staged_stage_1v<LAST>(P, stab, io, terms, bars, [](auto&) {});
 }
 

@@ -35,6 +35,8 @@ struct D8Dev {
   int isave, nsave, save_pending, save_lo, save_hi, saved;
   unsigned int arrive;
   int herm;           // 1: the state is exactly Hermitian, stages use packed real transforms
+  unsigned int att;       // attempts finished since reset (the persistent kernel's attempt barrier)
+  unsigned int save_seq;  // incremented whenever an accepted step crosses save times
 };
 
 struct D8Args {
@@ -52,6 +54,8 @@ struct D8Args {
   const double* masses;
   long long len;
   int npf;            // fused 1D1V path: epilogue operands staged in shared memory (y first)
+  double2* S3;        // persistent kernel: third stage-input buffer (ring S0, S1, S3)
+  unsigned int* done; // persistent kernel: stages finished since reset, per CTA
 };
 
 // Element i (0 or 1) of a two-pointer kernel argument, by select: indexing the
@@ -170,7 +174,10 @@ __device__ void finalize_step(const D8Args& a, const Attempt& at, double sum, in
     st->k1_valid = 0;
     int lo = st->isave, hi = lo;
     while (hi < st->nsave && __ldcg(a.save_ts + hi) <= st->t) ++hi;
-    if (hi > lo) { st->save_pending = 1; st->save_lo = lo; st->save_hi = hi; st->isave = hi; }
+    if (hi > lo) {
+      st->save_pending = 1; st->save_lo = lo; st->save_hi = hi; st->isave = hi;
+      st->save_seq += 1;
+    }
     if (nonf) st->status = SPX_ST_NONFINITE;
     else if (st->t >= st->t1) st->status = SPX_ST_DONE;
   } else {
@@ -180,6 +187,8 @@ __device__ void finalize_step(const D8Args& a, const Attempt& at, double sum, in
   st->dt = dt_next;
   st->arrive = 0;
   __threadfence();
+  // publish: the persistent kernel's CTAs wait for this count before the next attempt
+  st_release_u32(&st->att, st->att + 1);
 }
 
 // Elements owned by CTA `b` on the fused 1D1V path (plane tiles, then the field CTA).
@@ -317,7 +326,184 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
   io.atol = s.atol;
   io.adaptive = s.adaptive;
   io.timeout_status = &a.st->status;
+  io.persistent = false;
   staged_stage_1v<LAST>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
+}
+
+// ------------------------------------------------------------------ persistent 1D1V solver
+// All attempts of a replay in one cooperative launch (every CTA resident): a CTA
+// starts stage i as soon as the CTAs whose data it reads have finished stage i-1
+// (per-CTA completion counters, release/acquire), instead of waiting for the
+// whole grid at a kernel boundary.  Stage inputs rotate through three buffers;
+// the field CTA, whose output every tile reads, also waits until every tile has
+// finished stage i-2, so no buffer is overwritten while a slower CTA reads it.
+// After stage 12 the last CTA runs the controller and bumps st->att; every CTA
+// waits for that (attempt barrier), then performs pending saves.  Every wait is
+// bounded and ends the solve with SPX_ST_WAIT_TIMEOUT.
+
+// Copy of the controller state through L2 (other CTAs wrote it in this launch).
+__device__ __forceinline__ void load_state_l2(D8Dev& s, const D8Dev* st) {
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(st);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s);
+  for (int i = 0; i < (int)(sizeof(D8Dev) / 8); ++i) dst[i] = __ldcg(src + i);
+}
+
+// Energies of one saved state (the formulas of k_d8_save), by one CTA through L2.
+__device__ void persist_energies(const D8Args& a, const DevPlan& P, const D8Dev& s, const double2* Y,
+                                 double* red) {
+  const spx_problem& pb = P.pb;
+  const size_t pl = (size_t)P.plane;
+  double em = 0.0;
+  for (size_t i = threadIdx.x; i < 6 * pl; i += blockDim.x) {
+    const double2 f = __ldcg(Y + P.nc + i);
+    em = fma(f.x, f.x, fma(f.y, f.y, em));
+  }
+  em = block_sum(em, red);
+  if (threadIdx.x == 0) {
+    const int Ns = pb.Ns, Hs = P.nh;
+    const int kc = ((P.ax[0].n / 2) * P.ax[1].n + P.ax[1].n / 2) * P.ax[2].n + P.ax[2].n / 2;
+    const int offs[7] = {0, 1, pb.Nn, pb.Nn * pb.Nm, 2, 2 * pb.Nn, 2 * pb.Nn * pb.Nm};
+    const double O0 = pb.Omega_cs[0];
+    const double EM = 0.5 * em * O0 * O0;
+    double ke_tot = 0.0;
+    double kes[SPX_MAX_SPECIES];
+    for (int sp = 0; sp < Ns; ++sp) {
+      double c[7];
+      for (int k = 0; k < 7; ++k)
+        c[k] = (offs[k] >= 0 && offs[k] < Hs) ? __ldcg(Y + ((size_t)sp * Hs + offs[k]) * pl + kc).x : 0.0;
+      const double a0 = pb.alpha_s[3 * sp], a1 = pb.alpha_s[3 * sp + 1], a2 = pb.alpha_s[3 * sp + 2];
+      const double u0 = pb.u_s[3 * sp], u1 = pb.u_s[3 * sp + 1], u2 = pb.u_s[3 * sp + 2];
+      const double m = a.masses[sp];
+      const double pref = 0.5 * m * a0 * a1 * a2;
+      const double t0 = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) + (u0 * u0 + u1 * u1 + u2 * u2);
+      const double t1 = 1.41421356237309504880 * (a0 * u0 * c[1] + a1 * u1 * c[2] + a2 * u2 * c[3]);
+      const double t2 = 0.70710678118654752440 * (a0 * a0 * c[4] + a1 * a1 * c[5] + a2 * a2 * c[6]);
+      kes[sp] = pref * (t0 * c[0] + t1 + t2);
+      ke_tot += kes[sp];
+    }
+    for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
+      double* e = a.energies + (size_t)idx * (2 + Ns);
+      e[0] = EM;
+      e[1] = ke_tot;
+      for (int sp = 0; sp < Ns; ++sp) e[2 + sp] = kes[sp];
+    }
+    a.st->saved = s.save_hi;
+  }
+}
+
+__global__ void __launch_bounds__(NTHREADS, 2) k_d8_persist(D8Args a, int natt) {
+  __shared__ DevPlan P;
+  __shared__ D8Dev s;
+  __shared__ Attempt at;
+  __shared__ double red[NTHREADS / 32];
+  __shared__ EpiTerms terms;
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ unsigned int saves_seen;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, a.plan, a.tab);
+  // uniform values live in shared memory (P, s, at): registers stay with the stage body
+  if (threadIdx.x == 0) {
+    load_state_l2(s, a.st);
+    saves_seen = s.save_seq;
+  }
+  __syncthreads();
+  for (int q = 0; q < natt; ++q) {
+    if (threadIdx.x == 0) {
+      load_state_l2(s, a.st);
+      at = attempt_params(s, a.save_ts);
+    }
+    __syncthreads();
+    if (!at.go) {
+      if (blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING)
+        a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
+      return;
+    }
+    for (int stage = 0; stage < rk::S; ++stage) {
+      // the producers of this stage's inputs have finished stage - 1
+      const int nblk = P.pb.Ns * P.ntiles;
+      bool ok = true;
+      if (stage > 0) {
+        const unsigned int need = s.att * rk::S + stage;
+        const int b = blockIdx.x;
+        if (b < nblk) {
+          const int tl = b % P.ntiles;
+          if (threadIdx.x == 0 && tl > 0) ok = wait_counter(a.done + b - 1, need);
+          if (threadIdx.x == 1 && tl + 1 < P.ntiles) ok = wait_counter(a.done + b + 1, need);
+          if (threadIdx.x == 2) ok = wait_counter(a.done + nblk, need);
+        } else {
+          // the field CTA reads the tiles holding planes 0 and 1; the others must be
+          // past stage - 2 before this stage overwrites their stage - 2 input buffer
+          const int t01 = 1 / P.tile;
+          for (int c = threadIdx.x; c < nblk && ok; c += blockDim.x)
+            ok = wait_counter(a.done + c, (c % P.ntiles) <= t01 ? need : need - 1);
+        }
+      }
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
+        return;
+      }
+      if (threadIdx.x == 0) fill_terms(terms, stage, at.h);
+      __syncthreads();
+      const long long len = a.len;
+      const double2* Y = s.cur ? a.Y[1] : a.Y[0];
+      double2* Ki = a.K + (size_t)stage * len;
+      auto ring = [&](int i) { return i == 0 ? a.S[0] : (i == 1 ? a.S[1] : a.S3); };
+      if (stage == 0 && s.k1_valid) {
+        // rejected attempt: K_0 = f(y) is kept; rebuild the next input y + h a(1,0) K_0
+        double2* Sn = ring(1);
+        for_each_owned_1v(P, blockIdx.x, [&](size_t e) { Sn[e] = crfma(terms.cself, Ki[e], Y[e]); });
+      } else {
+        StageIO io;
+        io.in = (stage == 0) ? Y : ring(stage % 3);
+        io.Y = Y;
+        io.K = a.K;
+        io.len = len;
+        io.Ki = Ki;
+        io.out = (stage == rk::S - 1) ? (s.cur ? a.Y[0] : a.Y[1]) : ring((stage + 1) % 3);
+        io.npf = a.npf;
+        io.herm = s.herm != 0;
+        io.rtol = s.rtol;
+        io.atol = s.atol;
+        io.adaptive = s.adaptive;
+        io.timeout_status = &a.st->status;
+        io.persistent = true;
+        const bool ok_stage =
+            (stage < rk::S - 1)
+                ? staged_stage_1v<false>(P, stab, io, terms, bars, [](auto&) {})
+                : staged_stage_1v<true>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
+        if (!ok_stage) return;   // status already says WAIT_TIMEOUT; the CTAs waiting on this one time out too
+      }
+      // this stage's writes (generic proxy) are read by later bulk copies (async proxy)
+      fence_proxy_async();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_u32(a.done + blockIdx.x, s.att * rk::S + stage + 1);
+      }
+    }
+    // attempt barrier: the controller of this attempt has run
+    bool ok = true;
+    if (threadIdx.x == 0) ok = wait_counter(&a.st->att, s.att + 1);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
+      return;
+    }
+    if (threadIdx.x == 0) load_state_l2(s, a.st);
+    __syncthreads();
+    if (s.save_seq != saves_seen) {
+      const double2* Yc = s.cur ? a.Y[1] : a.Y[0];
+      if (a.saved)
+        for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
+          double2* dst = a.saved + (size_t)idx * a.len;
+          for_each_owned_1v(P, blockIdx.x, [&](size_t e) { dst[e] = __ldcg(Yc + e); });
+        }
+      if ((int)blockIdx.x == P.pb.Ns * P.ntiles) persist_energies(a, P, s, Yc, red);
+      __syncthreads();
+      if (threadIdx.x == 0) saves_seen = s.save_seq;
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
@@ -480,6 +666,7 @@ struct spx_dopri8 {
   int* h_status = nullptr;   // pinned
   std::vector<double> ts;
   bool herm_allowed = false;  // requested, fused 1D1V path, odd Nx, antisymmetric k table
+  bool persistent = false;    // attempts run by k_d8_persist (one cooperative launch per replay)
 };
 
 static bool g_d8_consts = false;
@@ -531,6 +718,8 @@ static int d8_attrs() {
   SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>));
   SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_persist));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_real));
   SPX_CUDA(cudaFuncSetAttribute(k_d8_real, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_gen<false>));
@@ -541,6 +730,21 @@ static int d8_attrs() {
   return SPX_OK;
 }
 
+
+// All `natt` attempts in one cooperative launch (every CTA co-resident).
+static void enqueue_persistent(spx_dopri8* s, cudaStream_t st, int natt) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(s->grid_stage, 1, 1);
+  cfg.blockDim = dim3(s->plan->threads, 1, 1);
+  cfg.dynamicSmemBytes = s->smem_stage;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_d8_persist, s->args, natt);
+}
 
 static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;
@@ -609,10 +813,22 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
     if (ea != cudaSuccess) { delete s; return cuda_fail(ea, "cudaFuncGetAttributes"); }
     s->smem_stage = stage_smem_1v(plan, fa.sharedSizeBytes, &npf);
     if (npf < 1) { delete s; set_error("Nx / tile too large for the Dopri8 stage kernel"); return SPX_E_UNSUPPORTED; }
+    if (o->persistent) {
+      // the persistent kernel needs every CTA resident at once (a cooperative launch)
+      int coop = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, plan->device);
+      cudaFuncAttributes fp;
+      if (cudaFuncGetAttributes(&fp, k_d8_persist) == cudaSuccess &&
+          fp.sharedSizeBytes + s->smem_stage <= (size_t)smem_optin() &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_d8_persist, plan->threads, s->smem_stage) ==
+              cudaSuccess)
+        s->persistent = coop && (long long)per_sm * plan->nsm >= s->grid_stage;
+      cudaGetLastError();
+    }
   } else {
     s->smem_stage = plan->smem_gen;
   }
-  // one allocation: st | part | save_ts | masses | energies | Y0 Y1 S0 S1 | K[13] | ws | saved
+  // one allocation: st | part | save_ts | masses | energies | Y0 Y1 S0 S1 S3 | done | K[13] | ws | saved
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t vec = al((size_t)len * sizeof(double2));
   size_t off = 0;
@@ -621,7 +837,8 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   const size_t o_ts = off; off += al(std::max(1, o->nsave) * sizeof(double));
   const size_t o_m = off; off += al(SPX_MAX_SPECIES * sizeof(double));
   const size_t o_en = off; off += al(std::max(1, o->nsave) * (size_t)(2 + Ns) * sizeof(double));
-  const size_t o_y = off; off += 4 * vec;
+  const size_t o_y = off; off += 5 * vec;      // Y0 Y1 S0 S1 S3
+  const size_t o_done = off; off += al(sizeof(unsigned int) * (size_t)s->grid_stage);
   const size_t o_k = off; off += 13 * vec;
   const size_t o_ws = off; off += al(plan->ws_bytes);
   const size_t o_sv = off; off += o->save_states ? (size_t)std::max(1, o->nsave) * vec : 0;
@@ -640,6 +857,8 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
     A.Y[i] = reinterpret_cast<double2*>(b + o_y + i * vec);
     A.S[i] = reinterpret_cast<double2*>(b + o_y + (2 + i) * vec);
   }
+  A.S3 = reinterpret_cast<double2*>(b + o_y + 4 * vec);
+  A.done = reinterpret_cast<unsigned int*>(b + o_done);
   A.K = reinterpret_cast<double2*>(b + o_k);   // stage j at K + j*len
   A.ws = reinterpret_cast<double2*>(b + o_ws);
   A.saved = o->save_states ? reinterpret_cast<double2*>(b + o_sv) : nullptr;
@@ -673,12 +892,15 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   // capture `attempts_per_graph` step attempts into one graph
   e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "cudaStreamBeginCapture"); }
-  for (int i = 0; i < s->attempts_per_graph; ++i) enqueue_attempt(s, s->cap);
+  if (s->persistent) enqueue_persistent(s, s->cap, s->attempts_per_graph);
+  else
+    for (int i = 0; i < s->attempts_per_graph; ++i) enqueue_attempt(s, s->cap);
   e = cudaStreamEndCapture(s->cap, &s->graph);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    enqueue_attempt(s, s->cap);
+    if (s->persistent) enqueue_persistent(s, s->cap, 1);
+    else enqueue_attempt(s, s->cap);
     e = cudaStreamEndCapture(s->cap, &s->graph1);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec1, s->graph1, 0);
@@ -702,6 +924,7 @@ int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
   I.herm = s->herm_allowed ? 1 : 0;
   SPX_CUDA(cudaMemcpyAsync(s->args.st, &I, sizeof(I), cudaMemcpyHostToDevice, st));
   SPX_CUDA(cudaMemcpyAsync(s->args.Y[0], y0, (size_t)s->args.len * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  SPX_CUDA(cudaMemsetAsync(s->args.done, 0, sizeof(unsigned int) * (size_t)s->grid_stage, st));
   if (s->herm_allowed) {
     const int N = s->plan->host.ax[1].n;
     const long long nlines = s->args.len / N;
@@ -767,7 +990,7 @@ int spx_dopri8_stats_get(spx_dopri8* s, spx_dopri8_stats* out, void* stream) {
   out->t = d.t; out->dt = d.dt;
   out->accepted = d.accepted; out->rejected = d.rejected; out->rhs_evals = d.evals;
   out->status = d.status; out->saved = d.saved;
-  out->hermitian = d.herm; out->pad = 0;
+  out->hermitian = d.herm; out->persistent = s->persistent ? 1 : 0;
   return SPX_OK;
 }
 

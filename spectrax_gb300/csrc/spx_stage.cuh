@@ -211,6 +211,14 @@ struct StageIO {
   double rtol, atol;          // last stage: error scaling
   int adaptive;
   int* timeout_status;        // gets SPX_ST_WAIT_TIMEOUT if a staged copy never lands
+  bool persistent;            // called again in the same launch: fence the async proxy before
+                              // the copies, invalidate the barriers afterwards
+};
+
+// Field-CTA source reading through L2 (data other CTAs wrote in the same launch).
+struct SrcL2 {
+  const double2* y;
+  __device__ __forceinline__ double2 operator()(size_t e) const { return __ldcg(y + e); }
 };
 
 // Runs the CTA's share of one stage (block b of Ns * ntiles tile CTAs + the
@@ -218,7 +226,7 @@ struct StageIO {
 // caller's shared scratch.  LAST: `tail(el)` is called by every thread of every
 // CTA with the stage's EpiFinal (or an empty accumulator) for the error reduction.
 template <bool LAST, class Tail>
-__device__ void staged_stage_1v(const DevPlan& P, const double2* __restrict__ stab, const StageIO& io,
+__device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ stab, const StageIO& io,
                                 const EpiTerms& terms, uint64_t* bars, Tail&& tail) {
   const long long len = io.len;
   const int nblk = P.pb.Ns * P.ntiles;
@@ -232,14 +240,14 @@ __device__ void staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
     __syncthreads();
     if constexpr (!LAST) {
       EpiNext epi{io.Ki, io.out, io.Y, io.K, len, &terms, nullptr, 0, 0, nullptr};
-      maxwell1v_g(P, stab, SrcPlain{io.in}, sA, epi);
+      maxwell1v_g(P, stab, SrcL2{io.in}, sA, epi);
     } else {
       EpiFinal el{io.Ki, io.out, io.Y, io.K, len, &terms, nullptr, 0, 0, nullptr,
                   io.rtol, io.atol, io.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
-      maxwell1v_g(P, stab, SrcPlain{io.in}, sA, el);
+      maxwell1v_g(P, stab, SrcL2{io.in}, sA, el);
       tail(el);
     }
-    return;
+    return true;
   }
   const int sp = b / P.ntiles, n0 = (b % P.ntiles) * T, nt = min(T, Nn - n0);
   if (nt <= 0) {
@@ -249,7 +257,7 @@ __device__ void staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
       __syncthreads();
       tail(none);
     }
-    return;
+    return true;
   }
   double2* sB = sA + (size_t)(T + 1) * N;
   double2* U = sB + (size_t)(T + 1) * N;
@@ -264,6 +272,7 @@ __device__ void staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    if (io.persistent) fence_proxy_async();
     const int lo = max(n0 - 1, 0), hi = min(n0 + nt, Nn - 1);     // staged planes, inclusive
     const uint32_t bu = (uint32_t)((hi - lo + 1) * N * sizeof(double2));
     const uint32_t bf = (uint32_t)(N * sizeof(double2));
@@ -292,7 +301,7 @@ __device__ void staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
       atomicExch(io.timeout_status, SPX_ST_WAIT_TIMEOUT);
       mbar_wait_bounded(&bars[1], 0);
     }
-    return;
+    return false;
   }
   if constexpr (!LAST) {
     EpiNext epi{io.Ki, io.out, io.Y, io.K, len, &terms, pf, own, npf, &bars[1]};
@@ -306,7 +315,20 @@ __device__ void staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
     tail(el);
   }
   // a failed prepare() returns from the tile early: record it once
-  if (threadIdx.x == 0 && !mbar_try_wait(&bars[1], 0)) atomicExch(io.timeout_status, SPX_ST_WAIT_TIMEOUT);
+  bool bad = false;
+  if (threadIdx.x == 0 && !mbar_try_wait(&bars[1], 0)) {
+    atomicExch(io.timeout_status, SPX_ST_WAIT_TIMEOUT);
+    bad = true;
+  }
+  if (io.persistent) {
+    // the barriers are initialised again by the next stage: only complete ones are invalidated
+    if (__syncthreads_or(bad)) return false;
+    if (threadIdx.x == 0) {
+      mbar_inval(&bars[0]);
+      mbar_inval(&bars[1]);
+    }
+  }
+  return !bad;
 }
 
 }  // namespace spx

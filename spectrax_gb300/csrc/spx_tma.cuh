@@ -40,6 +40,34 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// invalidate a barrier whose phases are all complete, so it can be initialised again
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// order this thread's earlier generic-proxy view of memory (including data other
+// CTAs published and this thread acquired) before its later bulk copies
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait until *p >= target (wrap-free counters), giving up after `limit` polls.
+__device__ __forceinline__ bool wait_counter(const unsigned int* p, unsigned int target, int limit = 1 << 22) {
+  for (int i = 0; i < limit; ++i) {
+    if (ld_acquire_u32(p) >= target) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

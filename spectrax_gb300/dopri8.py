@@ -34,7 +34,7 @@ def species_masses(params):
 class Dopri8Solver:
     def __init__(self, plan: Plan, t0: float, t1: float, dt0: float, ts=None, adaptive=True,
                  rtol=1e-10, atol=1e-12, max_steps=1_000_000, save_states=True, masses=None,
-                 hermitian=True):
+                 hermitian=True, persistent=False):
         L = _lib.lib()
         self.plan = plan
         self.ts = np.ascontiguousarray(np.asarray([] if ts is None else ts, np.float64))
@@ -52,6 +52,10 @@ class Dopri8Solver:
         # detect an exactly Hermitian y0 at reset (odd Nx, fused 1D1V path) and use
         # packed real transforms for it
         o.hermitian = 1 if hermitian else 0
+        # optional: one cooperative launch per replay, stages chained by per-CTA
+        # completion counters (same results bit for bit; not faster on the
+        # two-stream workload, where the stages are FP64-issue bound)
+        o.persistent = 1 if persistent else 0
         self.save_states = bool(save_states)
         h = C.c_void_p()
         with torch.cuda.device(plan.device):
@@ -86,7 +90,7 @@ class Dopri8Solver:
         _lib.check(_lib.lib().spx_dopri8_stats_get(self.handle, C.byref(s), _stream_ptr(stream)), "stats")
         return dict(t=s.t, dt=s.dt, accepted=s.accepted, rejected=s.rejected, rhs_evals=s.rhs_evals,
                     status=s.status, status_name=_lib.STATUS_NAMES.get(s.status, "?"), saved=s.saved,
-                    hermitian=bool(s.hermitian))
+                    hermitian=bool(s.hermitian), persistent=bool(s.persistent))
 
     def _copy(self, what, out):
         _lib.check(_lib.lib().spx_dopri8_copy(self.handle, what, C.c_void_p(out.data_ptr()),
