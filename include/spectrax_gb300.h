@@ -107,6 +107,21 @@ int spx_jvp(const spx_plan* plan, const void* y, const void* v, void* Jv, void* 
             size_t ws_bytes, void* stream);
 
 /*
+ * Repeated JVPs at one state, the split jax.linearize makes
+ * (spectrax/midpoint_solver.py:75: linearise once per Newton iteration, then one
+ * product per GMRES iteration).  spx_linearize stores in `lin`
+ * (spx_linearize_bytes() bytes, 16-byte aligned) what J(y) v needs from y: the
+ * real-space Hermite planes and field combinations of y on the general layout
+ * (saving one inverse transform per plane in every later product), a copy of y
+ * on the 1D1V layout.  `lin` no longer refers to y.  spx_jvp_lin then returns
+ * J(y) v bit for bit as spx_jvp(y, v) would; `ws` as for spx_jvp.
+ */
+size_t spx_linearize_bytes(const spx_plan* plan);
+int spx_linearize(const spx_plan* plan, const void* y, void* lin, size_t lin_bytes, void* stream);
+int spx_jvp_lin(const spx_plan* plan, const void* lin, const void* v, void* Jv, void* ws,
+                size_t ws_bytes, void* stream);
+
+/*
  * g = J(y)^T w (plain transpose, no conjugation): the vector-Jacobian product of
  * the holomorphic right-hand side.  conj(J^T conj(w)) = J^H w is what
  * torch autograd needs; the Python layer applies the conjugations.

@@ -101,6 +101,9 @@ _PROTOS = {
     "spx_rhs_workspace_bytes": (C.c_size_t, [_VP]),
     "spx_rhs": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_jvp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
+    "spx_linearize_bytes": (C.c_size_t, [_VP]),
+    "spx_linearize": (C.c_int, [_VP, _VP, _VP, C.c_size_t, _VP]),
+    "spx_jvp_lin": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_vjp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_vjp_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "spx_dopri8_create": (C.c_int, [_VP, C.POINTER(spx_dopri8_opts), C.POINTER(_VP)]),

@@ -60,6 +60,8 @@ struct DevPlan {
   int path;              // 0: fused 1D1V path; 1: general path
   int tile;              // Hermite planes per CTA on the fused path
   int ntiles;            // tiles per species on the fused path
+  int prow;              // general path: shared-memory row length (Nx*Nz, odd when Ny > 1)
+  int pplane;            // general path: shared-memory plane length Ny*prow
 };
 
 // ------------------------------------------------------------------ complex helpers
@@ -97,9 +99,18 @@ __device__ __forceinline__ int std_index(int c, int n) { int k = c - n / 2; retu
 // ------------------------------------------------------------------ line addressing
 // nl lines of length n inside one shared buffer: element e of line l sits at
 // base(l) + e*es with base(l) = (l / div)*shi + (l % div)*slo.
+// Optional: lines l > rk are taken as l + rg (skips a block of rg lines, e.g.
+// rows that are all zero or not needed beyond a 2/3 cut); lf = 1 puts the line
+// index fastest across threads in the register-radix stages (consecutive
+// threads on neighbouring lines: conflict-free shared-memory access when the
+// lines are strided or padded rows).  Zero-initialised members change nothing.
 struct Lines {
   int nl, es, div, shi, slo;
-  __device__ __forceinline__ int base(int l) const { return (l / div) * shi + (l % div) * slo; }
+  int rk, rg, lf;
+  __device__ __forceinline__ int base(int l) const {
+    if (l > rk) l += rg;
+    return (l / div) * shi + (l % div) * slo;
+  }
 };
 
 // ------------------------------------------------------------------ register butterflies
@@ -170,7 +181,8 @@ __device__ __forceinline__ void stage_reg_dit(const double2* __restrict__ in, do
   const int M = n / R;
   const int ntask = L.nl * M;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
-    const int l = t / M, j = t - l * M;
+    const int l = L.lf ? t % L.nl : t / M;
+    const int j = L.lf ? t / L.nl : t - l * M;
     const int b = L.base(l);
     const int k = j % Ns;
     double2 v[R];
@@ -196,7 +208,8 @@ __device__ __forceinline__ void stage_reg_dif(const double2* __restrict__ in, do
   const int M = n / R;
   const int ntask = L.nl * M;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
-    const int l = t / M, j = t - l * M;
+    const int l = L.lf ? t % L.nl : t / M;
+    const int j = L.lf ? t / L.nl : t - l * M;
     const int b = L.base(l);
     const int k = j % Ns;
     const int idx = (j / Ns) * Ns * R + k;
@@ -412,29 +425,63 @@ __device__ __forceinline__ double2* fft_axis(double2* a, double2* b, const AxisP
   return fft_axis_t<INV, false>(a, b, ap, tab, L, -1);
 }
 
-// 3-D transform of `np` contiguous planes of shape (Ny, Nx, Nz) (element
-// (y*Nx + x)*Nz + z of plane p at p*Ny*Nx*Nz) held in buffer a; b is the
-// ping-pong partner.  DIF = false: masked input (zero beyond each axis' cut),
-// DIF = true: only the masked outputs are needed.  Returns the result buffer.
+// 3-D transform of one plane of shape (Ny, Nx, Nz) held in buffer a with rows
+// of P.prow entries (element (y, x, z) at y*prow + x*Nz + z; prow is Nx*Nz
+// rounded up to an odd count when Ny > 1, so neighbouring rows fall in different
+// shared-memory banks); b is the ping-pong partner.  DIF = false: masked input
+// (zero beyond each axis' cut), DIF = true: only the masked outputs are needed.
+// On 2-D planes (Nz = 1) the inverse skips the x-lines of rows beyond the y cut
+// (all zero) and the forward skips the y-lines of columns beyond the x cut (never
+// read).  Returns the result buffer.
+__device__ __forceinline__ bool prunable(const AxisPlan& ap) { return ap.cut >= 0 && 2 * ap.cut + 1 < ap.n; }
+
 template <bool INV, bool DIF>
-__device__ double2* fft_planes_t(double2* a, double2* b, const DevPlan& P, const double2* tab, int np) {
+__device__ double2* fft_planes_t(double2* a, double2* b, const DevPlan& P, const double2* tab) {
   const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
-  if (Nz > 1) {   // z-lines, l = (p*Ny + y)*Nx + x, base = l*Nz
-    Lines L{np * Ny * Nx, 1, 1, Nz, 0};
+  const int R = P.prow;
+  if (Nz > 1) {   // z-lines, l = y*Nx + x, base = y*prow + x*Nz
+    Lines L{Ny * Nx, 1, Nx, R, Nz};
     double2* r = fft_axis_t<INV, DIF>(a, b, P.ax[2], tab, L, P.ax[2].cut);
     if (r != a) { b = a; a = r; }
   }
-  if (Nx > 1) {   // x-lines, l = (p*Ny + y)*Nz + z, base = (l/Nz)*Nx*Nz + l%Nz
-    Lines L{np * Ny * Nz, Nz, Nz, Nx * Nz, 1};
+  if (Nx > 1) {   // x-lines, l = y*Nz + z, base = y*prow + z
+    Lines L{Ny * Nz, Nz, Nz, R, 1};
+    L.lf = 1;
+    if (!DIF && Nz == 1 && Ny > 1 && prunable(P.ax[0])) {
+      const int cy = P.ax[0].cut;
+      L.nl = 2 * cy + 1;
+      L.rk = cy;
+      L.rg = Ny - L.nl;
+      if (P.ax[1].nst & 1) {
+        // the result lands in b: its skipped rows must read as zero
+        for (int i = threadIdx.x; i < L.rg * Nx; i += blockDim.x) {
+          const int y = cy + 1 + i / Nx;
+          b[y * R + i % Nx] = make_double2(0.0, 0.0);
+        }
+      }
+    }
     double2* r = fft_axis_t<INV, DIF>(a, b, P.ax[1], tab, L, P.ax[1].cut);
     if (r != a) { b = a; a = r; }
   }
-  if (Ny > 1) {   // y-lines, l = p*Nx*Nz + x*Nz + z, base = p*plane + l%(Nx*Nz)
-    Lines L{np * Nx * Nz, Nx * Nz, Nx * Nz, P.plane, 1};
+  if (Ny > 1) {   // y-lines, l = x*Nz + z, base = l, stride prow
+    Lines L{Nx * Nz, R, Nx * Nz, 0, 1};
+    L.lf = 1;
+    if (DIF && Nz == 1 && Nx > 1 && prunable(P.ax[1])) {
+      const int cx = P.ax[1].cut;
+      L.nl = 2 * cx + 1;
+      L.rk = cx;
+      L.rg = Nx - L.nl;
+    }
     double2* r = fft_axis_t<INV, DIF>(a, b, P.ax[0], tab, L, P.ax[0].cut);
     if (r != a) { b = a; a = r; }
   }
   return a;
+}
+
+// Shared-memory position of plane entry pt = (y*Nx + x)*Nz + z (padded rows).
+__device__ __forceinline__ int padded(const DevPlan& P, int pt) {
+  const int row = P.ax[1].n * P.ax[2].n;
+  return (pt / row) * P.prow + pt % row;
 }
 
 // k-table entry (k_c / L, k_c) of axis `ax` at centered index c.

@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
   if (!at.go || (stage == 0 && s.k1_valid)) return;
   const double2* in = (stage == 0) ? pick(a.Y, s.cur) : pick(a.S, stage & 1);
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + P.plane;
+  double2* sB = sA + P.pplane;
   general_to_real(P, stab, in, blockIdx.x, a.ws + (size_t)blockIdx.x * P.plane, sA, sB);
 }
 
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stag
   const double2* in = (stage == 0) ? Y : pick(a.S, stage & 1);
   const int nplanes = P.pb.Ns * P.nh;
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + P.plane;
+  double2* sB = sA + P.pplane;
   const int b = blockIdx.x;
   const double2* GB = a.ws + (size_t)nplanes * P.plane;
   if constexpr (!LAST) {

@@ -126,6 +126,8 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
   P.nh = p.Nn * p.Nm * p.Np;
   P.nc = (long long)p.Ns * P.nh * P.plane;
   P.tab_len = (int)pl->tab.size();
+  P.prow = p.Nx * p.Nz;
+  P.pplane = P.plane;
   pl->nsm = nsm > 0 ? nsm : 152;
   pl->smem_tab = ((size_t)P.tab_len * sizeof(double2) + 255) / 256 * 256;
   const size_t smem_max = 227 * 1024 - 4096;
@@ -151,7 +153,11 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
                    (size_t)p.Ns * ((ntiles + 7) / 8) * N * sizeof(double2);
   } else {
     P.path = 1;
-    pl->smem_gen = pl->smem_tab + 2 * (size_t)P.plane * sizeof(double2);
+    // shared-memory rows padded to an odd length (see fft_planes_t)
+    P.prow = p.Nx * p.Nz;
+    if (p.Ny > 1 && (P.prow & 1) == 0) P.prow += 1;
+    P.pplane = p.Ny * P.prow;
+    pl->smem_gen = pl->smem_tab + 2 * (size_t)P.pplane * sizeof(double2);
     if (pl->smem_gen > smem_max) {
       set_error("a Fourier plane of this size does not fit in shared memory");
       return SPX_E_UNSUPPORTED;
@@ -199,7 +205,7 @@ __global__ void __launch_bounds__(NTHREADS) k_gen_real(const DevPlan* __restrict
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   load_plan(P, stab, gP, gtab);
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + P.plane;
+  double2* sB = sA + P.pplane;
   const int id = blockIdx.x;
   general_to_real(P, stab, y, id, ws + (size_t)id * P.plane, sA, sB);
 }
@@ -220,7 +226,7 @@ __global__ void __launch_bounds__(NTHREADS) k_gen_nl(const DevPlan* __restrict__
     return;
   }
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + P.plane;
+  double2* sB = sA + P.pplane;
   const double2* GB = ws + (size_t)nplanes * P.plane;
   general_nl_plane(P, stab, y, ws, GB, blockIdx.x, sA, sB, epi);
 }
@@ -301,7 +307,7 @@ __global__ void __launch_bounds__(NTHREADS) k_jvp_real(const DevPlan* __restrict
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   load_plan(P, stab, gP, gtab);
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + P.plane;
+  double2* sB = sA + P.pplane;
   const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
   const int b = blockIdx.x;
   const bool second = b >= nreal;
@@ -309,10 +315,12 @@ __global__ void __launch_bounds__(NTHREADS) k_jvp_real(const DevPlan* __restrict
   general_to_real(P, stab, second ? v : y, id, ws + (size_t)b * P.plane, sA, sB);
 }
 
+// wy: real-space planes and field combinations of y; wv: the same of v
 __global__ void __launch_bounds__(NTHREADS) k_jvp_nl(const DevPlan* __restrict__ gP,
                                                      const double2* __restrict__ gtab,
                                                      const double2* __restrict__ v,
-                                                     const double2* __restrict__ ws,
+                                                     const double2* __restrict__ wy,
+                                                     const double2* __restrict__ wv,
                                                      double2* __restrict__ out) {
   __shared__ DevPlan P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -325,13 +333,12 @@ __global__ void __launch_bounds__(NTHREADS) k_jvp_nl(const DevPlan* __restrict__
     return;
   }
   const size_t pl = (size_t)P.plane;
-  const int nreal = nplanes + 3 * P.pb.Ns + 3;
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + P.plane;
-  const double2* Cy = ws;
-  const double2* Gy = ws + (size_t)nplanes * pl;
-  const double2* Cv = ws + (size_t)nreal * pl;
-  const double2* Gv = Cv + (size_t)nplanes * pl;
+  double2* sB = sA + P.pplane;
+  const double2* Cy = wy;
+  const double2* Gy = wy + (size_t)nplanes * pl;
+  const double2* Cv = wv;
+  const double2* Gv = wv + (size_t)nplanes * pl;
   general_nl_plane_t<true>(P, stab, v, Cv, Gy, Cy, Gv, blockIdx.x, sA, sB, epi);
 }
 
@@ -502,7 +509,55 @@ int spx_jvp(const spx_plan* pl, const void* y, const void* v, void* Jv, void* ws
     const int nplanes = P.pb.Ns * P.nh;
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
     k_jvp_real<<<2 * nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, vv, w);
-    k_jvp_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w, out);
+    k_jvp_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w,
+                                                            w + (size_t)nreal * P.plane, out);
+  }
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+size_t spx_linearize_bytes(const spx_plan* pl) {
+  if (!pl) return 0;
+  const DevPlan& P = pl->host;
+  if (P.path == 0) return (size_t)(P.nc + 6LL * P.plane) * sizeof(double2);
+  const size_t nreal = (size_t)P.pb.Ns * P.nh + 3 * (size_t)P.pb.Ns + 3;
+  return nreal * (size_t)P.plane * sizeof(double2);
+}
+
+int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes, void* stream) {
+  if (!pl || !y || !lin) { set_error("spx_linearize: null argument"); return SPX_E_ARG; }
+  if (((uintptr_t)y | (uintptr_t)lin) & 15) { set_error("spx_linearize: pointers must be 16-byte aligned"); return SPX_E_ARG; }
+  if (lin_bytes < spx_linearize_bytes(pl)) { set_error("spx_linearize: lin too small"); return SPX_E_WORKSPACE; }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const DevPlan& P = pl->host;
+  if (P.path == 0) {
+    SPX_CUDA(cudaMemcpyAsync(lin, y, spx_linearize_bytes(pl), cudaMemcpyDeviceToDevice, st));
+    return SPX_OK;
+  }
+  const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
+  k_gen_real<<<nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y),
+                                                      static_cast<double2*>(lin));
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+int spx_jvp_lin(const spx_plan* pl, const void* lin, const void* v, void* Jv, void* ws, size_t ws_bytes,
+                void* stream) {
+  int rc = check_vec_args(pl, lin, v, Jv, ws, ws_bytes, "spx_jvp_lin");
+  if (rc != SPX_OK) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const DevPlan& P = pl->host;
+  const double2* ll = static_cast<const double2*>(lin);
+  const double2* vv = static_cast<const double2*>(v);
+  double2* out = static_cast<double2*>(Jv);
+  if (P.path == 0) {
+    k_jvp1v<<<P.pb.Ns * P.ntiles + 1, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, ll, vv, out);
+  } else {
+    const int nplanes = P.pb.Ns * P.nh;
+    const int nreal = nplanes + 3 * P.pb.Ns + 3;
+    double2* w = static_cast<double2*>(ws);
+    k_gen_real<<<nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w);
+    k_jvp_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, ll, w, out);
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;

@@ -420,12 +420,12 @@ __device__ inline void general_to_real(const DevPlan& P, const double2* __restri
     if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut)) {
       v = (id < nplanes) ? y[(size_t)id * pl + pt] : field_combo_point(P, y + P.nc, id - nplanes, pt);
     }
-    const int d = (std_index(cy, Ny) * Nx + std_index(cx, Nx)) * Nz + std_index(cz, Nz);
+    const int d = std_index(cy, Ny) * P.prow + std_index(cx, Nx) * Nz + std_index(cz, Nz);
     sA[d] = v;
   }
   __syncthreads();
-  double2* r = fft_planes_t<true, false>(sA, sB, P, tab, 1);
-  for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) out[pt] = r[pt];
+  double2* r = fft_planes_t<true, false>(sA, sB, P, tab);
+  for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) out[pt] = r[padded(P, pt)];
 }
 
 // Per-plane coefficients of the general nonlinear bracket (spectrax/_model.py:168-184).
@@ -543,10 +543,10 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
     double2 acc = bracket_point(cf, RA, FA, pl, pt, anyx, anyy, anyz, make_double2(0.0, 0.0));
     if (JVP) acc = bracket_point(cf, RB, FB, pl, pt, anyx, anyy, anyz, acc);
-    sA[pt] = acc;
+    sA[padded(P, (int)pt)] = acc;
   }
   __syncthreads();
-  double2* f = fft_planes_t<false, true>(sA, sB, P, tab, 1);
+  double2* f = fft_planes_t<false, true>(sA, sB, P, tab);
 
   const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
   const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
@@ -594,7 +594,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     re = fma(-d, C0.x, re);
     im = fma(-d, C0.y, im);
     if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut)) {
-      const int sidx = (std_index(cy, Ny) * Nx + std_index(cx, Nx)) * Nz + std_index(cz, Nz);
+      const int sidx = std_index(cy, Ny) * P.prow + std_index(cx, Nx) * Nz + std_index(cz, Nz);
       const double2 v = f[sidx];
       re = fma(sc, v.x, re);
       im = fma(sc, v.y, im);

@@ -3,7 +3,8 @@
 Each step solves F(y1) = y1 - y0 - dt f((y0 + y1)/2) = 0 by Newton iterations
 from the explicit-Euler guess; every Newton system (I - dt/2 J(y_mid)) delta = -F
 is solved matrix-free by restarted GMRES whose matrix-vector product is the
-hand-written linearised right-hand side ``spx_jvp``.  The Newton stopping rule is
+hand-written linearised right-hand side (``spx_linearize`` once per Newton
+system, then ``spx_jvp_lin`` per product).  The Newton stopping rule is
 the reference's (scaled 2-norm < 1, at most 300 iterations,
 spectrax/midpoint_solver.py:56-98); the inner solve uses restart 30 and a
 relative tolerance of 1e-10 by default, a deliberate difference from the
@@ -37,11 +38,14 @@ class NewtonGMRES:
         self.V = torch.empty((self.m + 1, n), dtype=torch.complex128, device=dev)
         self.w = torch.empty(n, dtype=torch.complex128, device=dev)
         self.jv = torch.empty(n, dtype=torch.complex128, device=dev)
+        # J(ymid) linearised once per Newton system (jax.linearize,
+        # spectrax/midpoint_solver.py:75), reused by every GMRES product
+        self.lin = torch.empty(plan.linearize_bytes, dtype=torch.uint8, device=dev)
         self.matvecs = 0
 
     def _A(self, ymid, v, out, c):
-        """out = v - c * J(ymid) v."""
-        self.plan.jvp_into(ymid, v, self.jv)
+        """out = v - c * J(ymid) v, with J(ymid) from the last ``linearize``."""
+        self.plan.jvp_lin_into(self.lin, v, self.jv)
         torch.add(v, self.jv, alpha=-c, out=out)
         self.matvecs += 1
         return out
@@ -49,6 +53,7 @@ class NewtonGMRES:
     def solve(self, ymid, b, c, atol=0.0):
         """Solve (I - c J(ymid)) x = b; returns (x, relative residual, iterations)."""
         V, w, m = self.V, self.w, self.m
+        self.plan.linearize(ymid, self.lin)
         x = torch.zeros_like(b)
         bnorm = torch.linalg.vector_norm(b).item()
         if bnorm == 0.0:

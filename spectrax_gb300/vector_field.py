@@ -89,6 +89,35 @@ class Plan:
                                       C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_jvp")
         return out
 
+    def linearize(self, y, lin=None, stream=None):
+        """What J(y) v needs from y, computed once (jax.linearize,
+        spectrax/midpoint_solver.py:75); reuse it with ``jvp_lin_into``.
+        ``lin`` (uint8, ``linearize_bytes``) is reused when given."""
+        self.check_state(y)
+        nb = self.linearize_bytes
+        if lin is None:
+            lin = torch.empty(nb, dtype=torch.uint8, device=self.device)
+        if lin.dtype != torch.uint8 or lin.numel() < nb or not lin.is_cuda or lin.device != self.device:
+            raise ValueError(f"lin must be a uint8 CUDA tensor of {nb} bytes on {self.device}")
+        _lib.check(_lib.lib().spx_linearize(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(lin.data_ptr()),
+                                            C.c_size_t(lin.numel()), _stream_ptr(stream)), "spx_linearize")
+        return lin
+
+    @property
+    def linearize_bytes(self) -> int:
+        return int(_lib.lib().spx_linearize_bytes(self.handle))
+
+    def jvp_lin_into(self, lin, v, out, stream=None):
+        """J(y) v for the y given to ``linearize`` (same bits as ``jvp_into(y, v)``)."""
+        for t, nm in ((v, "v"), (out, "out")):
+            self.check_state(t, nm)
+        if lin.numel() < self.linearize_bytes:
+            raise ValueError("lin is too small for this plan")
+        ws, nb = self.ws_ptr()
+        _lib.check(_lib.lib().spx_jvp_lin(self.handle, C.c_void_p(lin.data_ptr()), C.c_void_p(v.data_ptr()),
+                                          C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_jvp_lin")
+        return out
+
     def vjp_into(self, y, w, out, stream=None):
         for t, nm in ((y, "y"), (w, "w"), (out, "out")):
             self.check_state(t, nm)

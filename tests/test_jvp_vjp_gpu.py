@@ -57,6 +57,35 @@ def test_jvp_matches_central_difference(shape):
     assert rel_err(out.cpu().numpy(), ref) <= TOL
 
 
+LIN_SHAPES = JVP_SHAPES + [(5, 6, 1, 2, 3, 2, 2), (64, 64, 1, 2, 2, 2, 1), (16, 16, 1, 3, 3, 3, 2)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", LIN_SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_linearized_jvp_is_bit_identical(shape):
+    # spx_linearize once, then spx_jvp_lin for several v: the same bits as spx_jvp,
+    # and y may change after spx_linearize without affecting later products
+    import torch
+    p = _params(shape, 5)
+    rng = np.random.default_rng(6)
+    n = _n(shape)
+    plan = _plan(p)
+    yt = torch.from_numpy(_rand(n, rng)).cuda()
+    y_keep = yt.clone()
+    lin = plan.linearize(yt)
+    yt.mul_(3.0)
+    a, b = torch.empty_like(yt), torch.empty_like(yt)
+    for _ in range(3):
+        vt = torch.from_numpy(_rand(n, rng)).cuda()
+        plan.jvp_lin_into(lin, vt, a)
+        plan.jvp_into(y_keep, vt, b)
+        assert torch.equal(a, b)
+    if n <= 20000:
+        ref = 0.5 * (orhs.rhs(p, y_keep.cpu().numpy() + vt.cpu().numpy()) -
+                     orhs.rhs(p, y_keep.cpu().numpy() - vt.cpu().numpy()))
+        assert rel_err(a.cpu().numpy(), ref) <= TOL
+
+
 VJP_SHAPES = [(9, 1, 1, 6, 1, 1, 2), (16, 1, 1, 5, 1, 1, 3), (17, 1, 1, 40, 1, 1, 2)]
 
 
