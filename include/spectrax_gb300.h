@@ -122,6 +122,23 @@ int spx_jvp_lin(const spx_plan* plan, const void* lin, const void* v, void* Jv, 
                 size_t ws_bytes, void* stream);
 
 /*
+ * Krylov-basis kernels of the implicit midpoint's restarted GMRES (the reference
+ * uses jax.scipy's GMRES, spectrax/midpoint_solver.py:37-98).  V: device basis of
+ * rows of n complex128 entries (row i at V + i*n); only rows i < k are read.
+ * spx_krylov_cgs2: classical Gram-Schmidt with one re-orthogonalisation pass,
+ *   h = V[:k]^H w, w -= V[:k]^T h, h2 = V[:k]^H w, w -= V[:k]^T h2;
+ *   writes out[i] = h[i] + h2[i] (i < k) and out[k] = (||w||_2, 0) (device,
+ *   k + 1 complex128); ws holds spx_krylov_ws_bytes(n) bytes.  Sums in a fixed
+ *   order (deterministic).
+ * spx_krylov_axpy: x += sum_{i<k} c[i] V_i (c: k complex128 on the device).
+ */
+#define SPX_KRYLOV_MAX_ROWS 64
+size_t spx_krylov_ws_bytes(int64_t n);
+int spx_krylov_cgs2(const void* V, int64_t n, int32_t k, void* w, void* out, void* ws, size_t ws_bytes,
+                    void* stream);
+int spx_krylov_axpy(const void* V, int64_t n, int32_t k, const void* c, void* x, void* stream);
+
+/*
  * g = J(y)^T w (plain transpose, no conjugation): the vector-Jacobian product of
  * the holomorphic right-hand side.  conj(J^T conj(w)) = J^H w is what
  * torch autograd needs; the Python layer applies the conjugations.

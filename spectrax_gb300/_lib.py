@@ -16,6 +16,8 @@ MAX_SPECIES = 8
 MAX_AXIS = 256
 
 SPX_OK, SPX_E_ARG, SPX_E_CUDA, SPX_E_WORKSPACE, SPX_E_UNSUPPORTED = 0, -1, -2, -3, -4
+KRYLOV_MAX_ROWS = 64   # SPX_KRYLOV_MAX_ROWS
+
 STATUS_NAMES = {0: "RUNNING", 1: "DONE", 2: "MAX_STEPS", 3: "DT_UNDERFLOW", 4: "NONFINITE", 5: "WAIT_TIMEOUT"}
 
 
@@ -104,6 +106,9 @@ _PROTOS = {
     "spx_linearize_bytes": (C.c_size_t, [_VP]),
     "spx_linearize": (C.c_int, [_VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_jvp_lin": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
+    "spx_krylov_ws_bytes": (C.c_size_t, [C.c_int64]),
+    "spx_krylov_cgs2": (C.c_int, [_VP, C.c_int64, C.c_int32, _VP, _VP, _VP, C.c_size_t, _VP]),
+    "spx_krylov_axpy": (C.c_int, [_VP, C.c_int64, C.c_int32, _VP, _VP, _VP]),
     "spx_vjp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_vjp_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "spx_dopri8_create": (C.c_int, [_VP, C.POINTER(spx_dopri8_opts), C.POINTER(_VP)]),

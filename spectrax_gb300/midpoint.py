@@ -13,8 +13,9 @@ converged root rather than on the iterates.
 
 Krylov vectors live in one (restart+1, n) complex128 block on the device; the
 orthogonalisation is classical Gram-Schmidt with one re-orthogonalisation pass
-(two GEMVs per iteration); the small Hessenberg least-squares problem is solved
-on the host with Givens rotations.
+against the rows built so far (``spx_krylov_cgs2``: four streaming passes, the
+projections and the norm come back in one copy); the small Hessenberg
+least-squares problem is solved on the host with Givens rotations.
 """
 from __future__ import annotations
 
@@ -23,21 +24,29 @@ import math
 import numpy as np
 import torch
 
+import ctypes as C
+
+from . import _lib
 from .params import ImplicitMidpoint
-from .vector_field import Plan, plan_for_params
+from .vector_field import Plan, _stream_ptr, plan_for_params
 
 
 class NewtonGMRES:
     def __init__(self, plan: Plan, restart=30, gmres_tol=1e-10, gmres_maxiter=20):
         self.plan = plan
         self.m = int(restart)
+        if not 1 <= self.m < _lib.KRYLOV_MAX_ROWS:
+            raise ValueError(f"restart must be in [1, {_lib.KRYLOV_MAX_ROWS - 1}]")
         self.tol = float(gmres_tol)
         self.maxiter = int(gmres_maxiter)
         n = plan.state_len
         dev = plan.device
+        self.n = n
         self.V = torch.empty((self.m + 1, n), dtype=torch.complex128, device=dev)
         self.w = torch.empty(n, dtype=torch.complex128, device=dev)
         self.jv = torch.empty(n, dtype=torch.complex128, device=dev)
+        self.hout = torch.empty(self.m + 2, dtype=torch.complex128, device=dev)
+        self.kws = torch.empty(int(_lib.lib().spx_krylov_ws_bytes(n)), dtype=torch.uint8, device=dev)
         # J(ymid) linearised once per Newton system (jax.linearize,
         # spectrax/midpoint_solver.py:75), reused by every GMRES product
         self.lin = torch.empty(plan.linearize_bytes, dtype=torch.uint8, device=dev)
@@ -49,6 +58,21 @@ class NewtonGMRES:
         torch.add(v, self.jv, alpha=-c, out=out)
         self.matvecs += 1
         return out
+
+    def _cgs2(self, k):
+        """Orthogonalise w against V[:k]; returns (projections h (k,), ||w||)."""
+        _lib.check(_lib.lib().spx_krylov_cgs2(C.c_void_p(self.V.data_ptr()), C.c_int64(self.n), C.c_int32(k),
+                                              C.c_void_p(self.w.data_ptr()), C.c_void_p(self.hout.data_ptr()),
+                                              C.c_void_p(self.kws.data_ptr()), C.c_size_t(self.kws.numel()),
+                                              _stream_ptr(None)), "spx_krylov_cgs2")
+        hv = self.hout[: k + 1].cpu().numpy()
+        return hv[:k], float(hv[k].real)
+
+    def _axpy(self, k, coef, x):
+        """x += sum_{i<k} coef[i] V[i] (coef: device complex128)."""
+        _lib.check(_lib.lib().spx_krylov_axpy(C.c_void_p(self.V.data_ptr()), C.c_int64(self.n), C.c_int32(k),
+                                              C.c_void_p(coef.data_ptr()), C.c_void_p(x.data_ptr()),
+                                              _stream_ptr(None)), "spx_krylov_axpy")
 
     def solve(self, ymid, b, c, atol=0.0):
         """Solve (I - c J(ymid)) x = b; returns (x, relative residual, iterations)."""
@@ -64,11 +88,7 @@ class NewtonGMRES:
         its = 0
         rel = 1.0
         for _cycle in range(self.maxiter):
-            # the projections below always run over all m + 1 basis rows (rows not
-            # yet built are zero), so every cycle issues the same few operation
-            # shapes instead of a new one per Arnoldi step
-            V.zero_()
-            V[0].copy_(r / beta)
+            torch.div(r, beta, out=V[0])
             H = np.zeros((m + 1, m), np.complex128)
             cs = np.zeros(m, np.complex128)
             sn = np.zeros(m, np.complex128)
@@ -78,13 +98,7 @@ class NewtonGMRES:
             for j in range(m):
                 self._A(ymid, V[j], w, c)
                 its += 1
-                # classical Gram-Schmidt, twice
-                h = torch.mv(V.conj(), w)
-                w.sub_(torch.mv(V.T, h))
-                h2 = torch.mv(V.conj(), w)
-                w.sub_(torch.mv(V.T, h2))
-                hh = (h + h2)[: j + 1].cpu().numpy()
-                hn = torch.linalg.vector_norm(w).item()
+                hh, hn = self._cgs2(j + 1)          # classical Gram-Schmidt, twice
                 H[: j + 1, j] = hh
                 H[j + 1, j] = hn
                 # apply previous rotations, then a new one
@@ -109,7 +123,7 @@ class NewtonGMRES:
                 k_done = j + 1
                 res = abs(g[j + 1])
                 if hn > 0.0 and j + 1 < m + 1:
-                    V[j + 1].copy_(w / hn)
+                    torch.div(w, hn, out=V[j + 1])
                 if res <= target or hn == 0.0:
                     break
             # back substitution and update
@@ -117,8 +131,8 @@ class NewtonGMRES:
             yk = np.zeros(k, np.complex128)
             for i in reversed(range(k)):
                 yk[i] = (g[i] - np.dot(H[i, i + 1:k], yk[i + 1:k])) / H[i, i]
-            yt = torch.from_numpy(yk).to(V.device)
-            x.add_(torch.mv(V[:k].T, yt))
+            if k > 0:
+                self._axpy(k, torch.from_numpy(yk).to(V.device), x)
             # true residual for the restart
             self._A(ymid, x, w, c)
             r = b - w

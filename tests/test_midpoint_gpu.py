@@ -74,3 +74,59 @@ def test_simulation_with_implicit_midpoint():
     assert out["Ck"].shape == (4, 16, 1, 9, 1)
     assert out["solver_stats"]["steps"] == 3
     assert np.all(np.isfinite(out["EM_energy"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,k", [(1000, 1), (777, 9), (300001, 31), (200, 64), (5, 3)])
+def test_krylov_cgs2_and_axpy(n, k):
+    # the native Gram-Schmidt pass against the same two passes in numpy
+    import ctypes as C
+    import torch
+    from spectrax_gb300 import _lib
+    rng = np.random.default_rng(n + k)
+    V = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    w = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    h = V.conj() @ w
+    w1 = w - V.T @ h
+    h2 = V.conj() @ w1
+    w2 = w1 - V.T @ h2
+    Vt = torch.from_numpy(V).cuda().contiguous()
+    wt = torch.from_numpy(w).cuda()
+    out = torch.empty(k + 1, dtype=torch.complex128, device="cuda")
+    ws = torch.empty(int(_lib.lib().spx_krylov_ws_bytes(n)), dtype=torch.uint8, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(_lib.lib().spx_krylov_cgs2(C.c_void_p(Vt.data_ptr()), n, k, C.c_void_p(wt.data_ptr()),
+                                          C.c_void_p(out.data_ptr()), C.c_void_p(ws.data_ptr()), ws.numel(), st),
+               "spx_krylov_cgs2")
+    o = out.cpu().numpy()
+    assert rel_err(o[:k], h + h2) < 1e-12
+    assert abs(o[k].real - np.linalg.norm(w2)) <= 1e-12 * np.linalg.norm(w2)
+    assert o[k].imag == 0.0
+    assert rel_err(wt.cpu().numpy(), w2) < 1e-12
+    c = rng.standard_normal(k) + 1j * rng.standard_normal(k)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    xt = torch.from_numpy(x).cuda()
+    _lib.check(_lib.lib().spx_krylov_axpy(C.c_void_p(Vt.data_ptr()), n, k,
+                                          C.c_void_p(torch.from_numpy(c).cuda().data_ptr()),
+                                          C.c_void_p(xt.data_ptr()), st), "spx_krylov_axpy")
+    assert rel_err(xt.cpu().numpy(), x + V.T @ c) < 1e-12
+
+
+@pytest.mark.gpu
+def test_krylov_rejects_bad_arguments():
+    import ctypes as C
+    import torch
+    from spectrax_gb300 import _lib
+    V = torch.zeros((2, 8), dtype=torch.complex128, device="cuda")
+    w = torch.zeros(8, dtype=torch.complex128, device="cuda")
+    out = torch.zeros(80, dtype=torch.complex128, device="cuda")
+    ws = torch.empty(int(_lib.lib().spx_krylov_ws_bytes(8)), dtype=torch.uint8, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for k in (0, 65):
+        rc = _lib.lib().spx_krylov_cgs2(C.c_void_p(V.data_ptr()), 8, k, C.c_void_p(w.data_ptr()),
+                                        C.c_void_p(out.data_ptr()), C.c_void_p(ws.data_ptr()), ws.numel(), st)
+        assert rc == _lib.SPX_E_ARG
+    rc = _lib.lib().spx_krylov_cgs2(C.c_void_p(V.data_ptr()), 8, 2, C.c_void_p(w.data_ptr()),
+                                    C.c_void_p(out.data_ptr()), C.c_void_p(ws.data_ptr()), 8, st)
+    assert rc == _lib.SPX_E_WORKSPACE
