@@ -373,6 +373,19 @@ def _extra_orszag_tang():
     torch.cuda.synchronize()
     rhs_ms, jvp_ms = ev[0].elapsed_time(ev[1]) / 10, ev[1].elapsed_time(ev[2]) / 10
     n = plan.state_len
+    # explicit Dopri8 on the same state: fixed dt = 0.01, attempts timed after a warm-up graph
+    from spectrax_gb300.dopri8 import Dopri8Solver
+    d8 = Dopri8Solver(plan, 0.0, 1e30, 0.01, adaptive=False, max_steps=1 << 40, save_states=False,
+                      masses=[1.0, 25.0])
+    d8.reset(y)
+    d8.enqueue(8)
+    torch.cuda.synchronize()
+    ev[0].record()
+    d8.enqueue(16)
+    ev[1].record()
+    torch.cuda.synchronize()
+    d8_ms = ev[0].elapsed_time(ev[1]) / 16
+    del d8
     solver = ImplicitMidpoint(rtol=1e-10, atol=1e-10, restart=30, gmres_tol=1e-10)
     # one untimed step first: the first use of each library kernel in a process is slow
     midpoint.solve(plan, y, 0.1, 0.1, [0.0, 0.1], solver, [1.0, 25.0], save_states=False)
@@ -385,7 +398,8 @@ def _extra_orszag_tang():
     return {"workload": "Orszag-Tang 2D3V Nx=Ny=64, Nn=Nm=Np=8, Ns=2 (4.2M coefficients)",
             "rhs_ms": rhs_ms, "rhs_evals_per_s": 1e3 / rhs_ms,
             "rhs_hbm_gbs": 32.0 * n / (rhs_ms * 1e-3) / 1e9,
-            "jvp_ms": jvp_ms, "midpoint_steps": info["steps"], "midpoint_s": tm,
+            "jvp_ms": jvp_ms, "dopri8_ms_per_step": d8_ms, "dopri8_rhs_evals_per_s": 13e3 / d8_ms,
+            "midpoint_steps": info["steps"], "midpoint_s": tm,
             "midpoint_steps_per_s": info["steps"] / tm, "newton_iterations": info.get("newton"),
             "jvp_matvecs": info.get("matvecs"),
             "total_energy_rel_change_3_steps": float(abs(tot[-1] - tot[0]) / abs(tot[0]))}
@@ -563,9 +577,16 @@ def main():
     ap.add_argument("--scan-t1", type=float, default=4.0, help="horizon of the batched scan extra")
     ap.add_argument("--tile", type=int, default=0, help="Hermite planes per CTA (0: autotune)")
     ap.add_argument("--threads", type=int, default=256, help="CTA width when --tile is given")
+    ap.add_argument("--only-extra", default="", choices=["", "landau", "two_stream_run", "orszag_tang"],
+                    help="run just this extra workload and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.only_extra:
+        fn = {"landau": _extra_landau, "two_stream_run": _extra_two_stream_run,
+              "orszag_tang": _extra_orszag_tang}[args.only_extra]
+        print(json.dumps(fn()))
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

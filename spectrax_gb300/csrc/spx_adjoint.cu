@@ -101,18 +101,19 @@ __device__ __forceinline__ void param_terms(const DevPlan& P, const double2* __r
     const int c = (int)(e % N);
     const int n = (int)((e / N) % Nn);
     const int s = (int)(e / ((long long)N * Nn));
-    const double a0 = P.pb.alpha_s[3 * s], u0 = P.pb.u_s[3 * s];
+    const double a0 = P.pb.alpha_s[3 * s];
     const double2 C0 = y[e];
     const double2 Cp = (n + 1 < Nn) ? y[e + N] : make_double2(0.0, 0.0);
     const double2 Cm = (n >= 1) ? y[e - N] : make_double2(0.0, 0.0);
     const double K = ktab(P, tab, 1, c).x;
+    const double* cf = P.coef + ((size_t)s * Nn + n) * COEF_1V;   // coef_1v of plane (s, n)
     // nu: -col(n) C
-    const double col = colc(Nn, n);
+    const double col = cf[4];
     loc[0] += -col * (ge.x * C0.x - ge.y * C0.y);
     // streaming -i K a0 t  with t = sqrt((n+1)/2) C+ + sqrt(n/2) C- + (u0/a0) C
-    double2 t = cscale(u0 / a0, C0);
-    t = crfma(sqrt((n + 1) * 0.5), Cp, t);
-    t = crfma(sqrt(n * 0.5), Cm, t);
+    double2 t = cscale(P.ua[s], C0);
+    t = crfma(cf[0], Cp, t);
+    t = crfma(cf[1], Cm, t);
     const double w = K * a0;
     const double2 fk = make_double2(w * t.y, -w * t.x);
     loc[1] += ge.x * fk.x - ge.y * fk.y;
@@ -123,7 +124,7 @@ __device__ __forceinline__ void param_terms(const DevPlan& P, const double2* __r
     const int f = (int)((e - nC) / N), c = (int)((e - nC) % N);
     const double K = ktab(P, tab, 1, c).x;
     const double2* F = y + nC;
-    const double iO = 1.0 / P.pb.Omega_cs[0];
+    const double iO = P.iO0;
     // curl parts with K = (Kx, 0, 0): dE_y = -i Kx B_z, dE_z = i Kx B_y, dB_y = i Kx E_z, dB_z = -i Kx E_y
     double2 fk = make_double2(0.0, 0.0);
     if (f == 1) { const double2 b = F[5 * N + c]; fk = make_double2(K * b.y, -K * b.x); }

@@ -585,6 +585,8 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   b->cluster = o->cluster;
   b->nsave = o->nsave;
   std::vector<double2> tab;
+  std::vector<double> coefs;          // every instance's coef_1v table, concatenated
+  std::vector<size_t> coef_off(n);
   std::vector<double> cost(n);
   int tab_max = 0, work_max = 0;
   long long pool = 0, yoff = 0;
@@ -613,6 +615,8 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     I.P.ntiles = ntiles;
     I.tab_off = (int)tab.size();
     tab.insert(tab.end(), tmp.tab.begin(), tmp.tab.end());
+    coef_off[i] = coefs.size();
+    coefs.insert(coefs.end(), tmp.coef.begin(), tmp.coef.end());
     tab_max = std::max(tab_max, I.P.tab_len);
     // work area: two line buffers (T+1 lines), staged planes (T+2), field lines (3);
     // the field tile reuses it for its (2 Ns + 12)-line gather + output area
@@ -690,6 +694,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   const size_t o_yin = off; off += al(sizeof(double2) * b->total_len);
   const size_t o_yout = off; off += al(sizeof(double2) * b->total_len);
   const size_t o_pool = off; off += al(sizeof(double2) * pool);
+  const size_t o_coef = off; off += al(sizeof(double) * std::max<size_t>(1, coefs.size()));
   e = cudaMalloc(&b->block, off);
   if (e != cudaSuccess) { batch_free(b); return cuda_fail(e, "cudaMalloc(batch)"); }
   char* d = static_cast<char*>(b->block);
@@ -711,7 +716,10 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   A.work_max = work_max;
   b->y_in = const_cast<double2*>(A.y_in);
   b->y_out = A.y_out;
+  for (int i = 0; i < n; ++i) b->hinst[i].P.coef = reinterpret_cast<const double*>(d + o_coef) + coef_off[i];
   e = cudaMemcpy(A.inst, b->hinst.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !coefs.empty())
+    e = cudaMemcpy(d + o_coef, coefs.data(), sizeof(double) * coefs.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !tab.empty()) e = cudaMemcpy(d + o_tab, tab.data(), sizeof(double2) * tab.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(d + o_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && o->nsave) e = cudaMemcpy(d + o_ts, o->save_ts, sizeof(double) * o->nsave, cudaMemcpyHostToDevice);

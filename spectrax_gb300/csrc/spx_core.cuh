@@ -14,13 +14,17 @@
 //    uniform branches (no lane divergence).
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include "../../include/spectrax_gb300.h"
 
 namespace spx {
 
 constexpr int MAXST = 12;      // FFT stages per axis
-constexpr int NTHREADS = 256;  // threads per CTA for every kernel of this library
+constexpr int NTHREADS = 256;  // threads per CTA of the 1D1V and helper kernels
+// CTA width of the general-path (2-D/3-D plane) kernels: one plane per CTA fills
+// most of the shared memory, so one CTA per SM runs and 16 warps hide latency
+constexpr int GEN_THREADS = 512;
 
 struct AxisPlan {
   int n;                 // length along the axis (1 = nothing to transform)
@@ -62,7 +66,19 @@ struct DevPlan {
   int ntiles;            // tiles per species on the fused path
   int prow;              // general path: shared-memory row length (Nx*Nz, odd when Ny > 1)
   int pplane;            // general path: shared-memory plane length Ny*prow
+  // fused 1D1V path: per (species, plane) coefficients, COEF_1V doubles each
+  // (coef_1v), in device memory; computed once on the host because every
+  // square root or division costs ~10 FP64 instructions per thread on the GPU
+  const double* coef;
+  double ua[SPX_MAX_SPECIES];   // u_x / alpha_x per species
+  double iO0;                   // 1 / Omega_c of species 0
 };
+
+// Coefficients of Hermite plane n of species s on the fused 1D1V path:
+//   [0] sqrt((n+1)/2), [1] sqrt(n/2)          (streaming ladder, spectrax/_model.py:193-204)
+//   [2] q Omega_c sqrt(2n) / alpha_x / Nx     (nonlinear term with the 1/N of the forward FFT)
+//   [3] nu col(Nn, n), [4] col(Nn, n)         (hypercollisions, spectrax/_initialization.py:121-130)
+constexpr int COEF_1V = 5;
 
 // ------------------------------------------------------------------ complex helpers
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
@@ -496,9 +512,19 @@ __device__ __forceinline__ bool kept(int c, int n, int cut) {
 }
 
 // hypercollision coefficient c(N, i); spectrax/_initialization.py:125-129
-__device__ __forceinline__ double colc(int N, int i) {
+__host__ __device__ __forceinline__ double colc(int N, int i) {
   if (N <= 3) return 0.0;
   return (double)i * (double)(i - 1) * (double)(i - 2) / ((double)(N - 1) * (double)(N - 2) * (double)(N - 3));
+}
+
+__host__ inline void coef_1v(const spx_problem& pb, int s, int n, double* c) {
+  const double qOc = pb.qs[s] * pb.Omega_cs[s];
+  const double a0 = pb.alpha_s[3 * s];
+  c[0] = sqrt((double)(n + 1) * 0.5);
+  c[1] = sqrt((double)n * 0.5);
+  c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)pb.Nx;
+  c[3] = pb.nu * colc(pb.Nn, n);
+  c[4] = colc(pb.Nn, n);
 }
 
 }  // namespace spx

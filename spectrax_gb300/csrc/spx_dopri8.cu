@@ -91,15 +91,14 @@ struct EpiStage {
   double2* __restrict__ Snext;
   long long len;
   int stage;
-  double h;
+  const double* hc;   // h a(stage+1, j) for j <= stage, formed once per CTA
   __device__ __forceinline__ void operator()(size_t e, double2 v) const {
     K[(size_t)stage * len + e] = v;
-    const int row = stage;   // coefficients a(stage+1, j)
-    const int mask = cMask[row];
+    const int mask = cMask[stage];   // coefficients a(stage+1, j)
     double2 acc = Y[e];
     for (int j = 0; j < stage; ++j)
-      if (mask & (1 << j)) acc = crfma(h * cCoef[row][j], K[(size_t)j * len + e], acc);
-    acc = crfma(h * cCoef[row][stage], v, acc);
+      if (mask & (1 << j)) acc = crfma(hc[j], K[(size_t)j * len + e], acc);
+    acc = crfma(hc[stage], v, acc);
     Snext[e] = acc;
   }
 };
@@ -110,7 +109,9 @@ struct EpiLast {
   const double2* __restrict__ K;
   double2* __restrict__ Ynew;
   long long len;
-  double h, rtol, atol;
+  const double* hb;   // h b_j and h e_j (j <= 12), formed once per CTA
+  const double* he;
+  double rtol, atol;
   int adaptive;
   double sq;
   int nonfinite;
@@ -123,18 +124,18 @@ struct EpiLast {
       const bool ub = mb & (1 << j), ue = me & (1 << j);
       if (ub || ue) {
         const double2 kj = K[(size_t)j * len + e];
-        if (ub) yn = crfma(h * cCoef[12][j], kj, yn);
-        if (ue) er = crfma(h * cCoef[13][j], kj, er);
+        if (ub) yn = crfma(hb[j], kj, yn);
+        if (ue) er = crfma(he[j], kj, er);
       }
     }
-    yn = crfma(h * cCoef[12][12], v, yn);
-    er = crfma(h * cCoef[13][12], v, er);
+    yn = crfma(hb[12], v, yn);
+    er = crfma(he[12], v, er);
     Ynew[e] = yn;
     if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
     if (adaptive) {
       const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
-      const double sc = fma(rtol, sqrt(fmax(m0, m1)), atol);
-      const double rx = er.x / sc, ry = er.y / sc;
+      const double inv = 1.0 / fma(rtol, sqrt(fmax(m0, m1)), atol);   // one division per entry
+      const double rx = er.x * inv, ry = er.y * inv;
       sq = fma(rx, rx, fma(ry, ry, sq));
     }
   }
@@ -254,18 +255,24 @@ __device__ void last_stage_tail(const D8Args& a, const Attempt& at, EL& el, doub
 __constant__ int cEpiN[13];
 __constant__ int cEpiJ[13][MAX_TERMS];
 
+// Called by the 32 lanes of warp 0, one term per lane (a handful of warp-level
+// FP64 multiplies instead of a serial loop in one thread).
 __device__ void fill_terms(EpiTerms& T, int stage, double h) {
   const bool last = stage == rk::S - 1;
   const int row = last ? 12 : stage;
-  T.n = cEpiN[stage];
-  for (int t = 0; t < T.n; ++t) {
-    const int j = cEpiJ[stage][t];
-    T.j[t] = j;
-    T.c[t] = h * cCoef[row][j];
-    T.e[t] = last ? h * cCoef[13][j] : 0.0;
+  const int lane = threadIdx.x & 31;
+  const int n = cEpiN[stage];
+  if (lane < n) {
+    const int j = cEpiJ[stage][lane];
+    T.j[lane] = j;
+    T.c[lane] = h * cCoef[row][j];
+    T.e[lane] = last ? h * cCoef[13][j] : 0.0;
   }
-  T.cself = h * cCoef[row][stage];
-  T.eself = last ? h * cCoef[13][stage] : 0.0;
+  if (lane == 0) {
+    T.n = n;
+    T.cself = h * cCoef[row][stage];
+    T.eself = last ? h * cCoef[13][stage] : 0.0;
+  }
 }
 
 // One stage of the fused 1D1V path (staged_stage_1v): stage inputs and
@@ -277,24 +284,28 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
   __shared__ D8Dev s;
   __shared__ double red[NTHREADS / 32];
   __shared__ EpiTerms terms;
+  __shared__ Attempt sat;
   __shared__ __align__(8) uint64_t bars[2];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   // prologue independent of the previous launch; then wait for it (PDL)
   load_plan(P, stab, a.plan, a.tab);
   pdl_wait_and_release();
+  // the attempt's scalars once per CTA (FP64 compares and products cost the
+  // same per warp whatever the number of active lanes)
   if (threadIdx.x == 0) {
     s = *a.st;
+    sat = attempt_params(s, a.save_ts);
     if (stage == 0 && blockIdx.x == 0) a.st->save_pending = 0;
   }
   __syncthreads();
-  const Attempt at = attempt_params(s, a.save_ts);
+  const Attempt at = sat;
   if (!at.go) {
     if (LAST && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING)
       a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
     return;
   }
-  if (threadIdx.x == 0) fill_terms(terms, stage, at.h);
+  if (threadIdx.x < 32) fill_terms(terms, stage, at.h);
   const long long len = a.len;
   const double2* Y = pick(a.Y, s.cur);
   double2* Ki = a.K + (size_t)stage * len;
@@ -443,7 +454,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_persist(D8Args a, int natt) 
         if (threadIdx.x == 0) atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
         return;
       }
-      if (threadIdx.x == 0) fill_terms(terms, stage, at.h);
+      if (threadIdx.x < 32) fill_terms(terms, stage, at.h);
       __syncthreads();
       const long long len = a.len;
       const double2* Y = s.cur ? a.Y[1] : a.Y[0];
@@ -506,16 +517,20 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_persist(D8Args a, int natt) 
   }
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_d8_real(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
+  __shared__ Attempt sat;
   load_plan(P, stab, a.plan, a.tab);
   pdl_wait_and_release();
-  if (threadIdx.x == 0) s = *a.st;
+  if (threadIdx.x == 0) {
+    s = *a.st;
+    sat = attempt_params(s, a.save_ts);
+  }
   __syncthreads();
-  const Attempt at = attempt_params(s, a.save_ts);
+  const Attempt at = sat;
   if (!at.go || (stage == 0 && s.k1_valid)) return;
   const double2* in = (stage == 0) ? pick(a.Y, s.cur) : pick(a.S, stage & 1);
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
@@ -524,26 +539,36 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_real(D8Args a, int stage) {
 }
 
 template <bool LAST>
-__global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stage) {
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_d8_stage_gen(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
-  __shared__ double red[NTHREADS / 32];
+  __shared__ double red[GEN_THREADS / 32];
+  __shared__ Attempt sat;
+  __shared__ double hcs[2][16];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   load_plan(P, stab, a.plan, a.tab);
   pdl_wait_and_release();
   if (threadIdx.x == 0) {
     s = *a.st;
+    sat = attempt_params(s, a.save_ts);
     if (stage == 0 && blockIdx.x == 0) a.st->save_pending = 0;
   }
   __syncthreads();
-  const Attempt at = attempt_params(s, a.save_ts);
+  const Attempt at = sat;
   if (!at.go) {
     if (stage == rk::S - 1 && blockIdx.x == 0 && threadIdx.x == 0 && s.status == SPX_ST_RUNNING) {
       a.st->status = (s.accepted + s.rejected >= s.max_steps) ? SPX_ST_MAX_STEPS : SPX_ST_DT_UNDERFLOW;
     }
     return;
   }
+  // stage coefficients times h, one lane each
+  if (threadIdx.x < rk::S) {
+    const int j = threadIdx.x;
+    hcs[0][j] = at.h * cCoef[LAST ? 12 : stage][j];
+    hcs[1][j] = LAST ? at.h * cCoef[13][j] : 0.0;
+  }
+  __syncthreads();
   const double2* Y = pick(a.Y, s.cur);
   const double2* in = (stage == 0) ? Y : pick(a.S, stage & 1);
   const int nplanes = P.pb.Ns * P.nh;
@@ -552,7 +577,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stag
   const int b = blockIdx.x;
   const double2* GB = a.ws + (size_t)nplanes * P.plane;
   if constexpr (!LAST) {
-    EpiStage epi{Y, a.K, pick(a.S, (stage + 1) & 1), a.len, stage, at.h};
+    EpiStage epi{Y, a.K, pick(a.S, (stage + 1) & 1), a.len, stage, hcs[0]};
     if (stage == 0 && s.k1_valid) {
       for_each_owned_gen(P, b, [&](size_t e) { epi(e, a.K[e]); });
     } else if (b == nplanes) {
@@ -561,7 +586,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_gen(D8Args a, int stag
       general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, epi);
     }
   } else {
-    EpiLast el{Y, a.K, pick(a.Y, s.cur ^ 1), a.len, at.h, s.rtol, s.atol, s.adaptive, 0.0, 0};
+    EpiLast el{Y, a.K, pick(a.Y, s.cur ^ 1), a.len, hcs[0], hcs[1], s.rtol, s.atol, s.adaptive, 0.0, 0};
     if (b == nplanes) maxwell_range(P, stab, in, 0, P.plane, el);
     else general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, el);
     last_stage_tail(a, at, el, red);
@@ -755,11 +780,11 @@ static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
       else
         launch_pdl(k_d8_stage_1v<true>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
     } else {
-      launch_pdl(k_d8_real, s->grid_real, s->plan->threads, s->plan->smem_gen, st, s->args, stage);
+      launch_pdl(k_d8_real, s->grid_real, GEN_THREADS, s->plan->smem_gen, st, s->args, stage);
       if (stage < rk::S - 1)
-        launch_pdl(k_d8_stage_gen<false>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
+        launch_pdl(k_d8_stage_gen<false>, s->grid_stage, GEN_THREADS, s->smem_stage, st, s->args, stage);
       else
-        launch_pdl(k_d8_stage_gen<true>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
+        launch_pdl(k_d8_stage_gen<true>, s->grid_stage, GEN_THREADS, s->smem_stage, st, s->args, stage);
     }
   }
   launch_pdl(k_d8_save, s->plan->nsm, (int)NTHREADS, (size_t)0, st, s->args);

@@ -132,8 +132,14 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
   pl->smem_tab = ((size_t)P.tab_len * sizeof(double2) + 255) / 256 * 256;
   const size_t smem_max = 227 * 1024 - 4096;
   const bool onev = (p.Ny == 1 && p.Nz == 1 && p.Nm == 1 && p.Np == 1);
+  for (int sp = 0; sp < p.Ns; ++sp) P.ua[sp] = p.u_s[3 * sp] / p.alpha_s[3 * sp];
+  P.iO0 = 1.0 / p.Omega_cs[0];
+  pl->coef.clear();
   if (onev) {
     P.path = 0;
+    pl->coef.resize((size_t)p.Ns * p.Nn * COEF_1V);
+    for (int sp = 0; sp < p.Ns; ++sp)
+      for (int n = 0; n < p.Nn; ++n) coef_1v(p, sp, n, &pl->coef[((size_t)sp * p.Nn + n) * COEF_1V]);
     const int N = p.Nx;
     const long long planes = (long long)p.Ns * p.Nn;
     int T = tile > 0 ? tile : (int)((planes + pl->nsm - 1) / pl->nsm);
@@ -196,7 +202,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_rhs1v(const DevPlan* __restrict
   rhs1v_tile(P, stab, y, s, n0, nt, sA, sB, scoef, epi);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_gen_real(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_gen_real(const DevPlan* __restrict__ gP,
                                                        const double2* __restrict__ gtab,
                                                        const double2* __restrict__ y,
                                                        double2* __restrict__ ws) {
@@ -210,7 +216,7 @@ __global__ void __launch_bounds__(NTHREADS) k_gen_real(const DevPlan* __restrict
   general_to_real(P, stab, y, id, ws + (size_t)id * P.plane, sA, sB);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_gen_nl(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_gen_nl(const DevPlan* __restrict__ gP,
                                                      const double2* __restrict__ gtab,
                                                      const double2* __restrict__ y,
                                                      const double2* __restrict__ ws,
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp1v_fields(const DevPlan* __r
   vjp1v_fields(P, stab, w, g, part, sA, sB);
 }
 
-__global__ void __launch_bounds__(NTHREADS) k_jvp_real(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_jvp_real(const DevPlan* __restrict__ gP,
                                                        const double2* __restrict__ gtab,
                                                        const double2* __restrict__ y,
                                                        const double2* __restrict__ v,
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(NTHREADS) k_jvp_real(const DevPlan* __restrict
 }
 
 // wy: real-space planes and field combinations of y; wv: the same of v
-__global__ void __launch_bounds__(NTHREADS) k_jvp_nl(const DevPlan* __restrict__ gP,
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_jvp_nl(const DevPlan* __restrict__ gP,
                                                      const double2* __restrict__ gtab,
                                                      const double2* __restrict__ v,
                                                      const double2* __restrict__ wy,
@@ -385,8 +391,8 @@ int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, c
     k_rhs1v<<<grid, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, y, dy);
   } else {
     const int nplanes = P.pb.Ns * P.nh;
-    k_gen_real<<<nplanes + 3 * P.pb.Ns + 3, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws);
-    k_gen_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws, dy);
+    k_gen_real<<<nplanes + 3 * P.pb.Ns + 3, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws);
+    k_gen_nl<<<nplanes + 1, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws, dy);
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
@@ -435,13 +441,18 @@ int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx
   // group of 8 Hermite tiles (its group-partial reduction)
   const size_t ngroups = (size_t)pb->Ns * ((pl->host.ntiles + 7) / 8 + 1);
   const size_t ticket_bytes = (256 + 4 * ngroups + 255) / 256 * 256;
-  const size_t bytes = hdr + tab_bytes + ticket_bytes;
+  const size_t coef_bytes = (pl->coef.size() * sizeof(double) + 255) / 256 * 256;
+  const size_t bytes = hdr + tab_bytes + ticket_bytes + coef_bytes;
   cudaError_t e = cudaMalloc(&pl->d_block, bytes);
   if (e != cudaSuccess) { delete pl; return cuda_fail(e, "cudaMalloc(plan)"); }
   pl->d_plan = reinterpret_cast<DevPlan*>(pl->d_block);
   pl->d_tab = reinterpret_cast<double2*>(reinterpret_cast<char*>(pl->d_block) + hdr);
   pl->d_ticket = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes);
+  double* d_coef = reinterpret_cast<double*>(reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes + ticket_bytes);
+  pl->host.coef = pl->coef.empty() ? nullptr : d_coef;
   e = cudaMemset(pl->d_ticket, 0, ticket_bytes);
+  if (e == cudaSuccess && !pl->coef.empty())
+    e = cudaMemcpy(d_coef, pl->coef.data(), pl->coef.size() * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(pl->d_plan, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !pl->tab.empty())
     e = cudaMemcpy(pl->d_tab, pl->tab.data(), pl->tab.size() * sizeof(double2), cudaMemcpyHostToDevice);
@@ -508,8 +519,8 @@ int spx_jvp(const spx_plan* pl, const void* y, const void* v, void* Jv, void* ws
   } else {
     const int nplanes = P.pb.Ns * P.nh;
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
-    k_jvp_real<<<2 * nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, vv, w);
-    k_jvp_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w,
+    k_jvp_real<<<2 * nreal, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, vv, w);
+    k_jvp_nl<<<nplanes + 1, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w,
                                                             w + (size_t)nreal * P.plane, out);
   }
   SPX_CUDA(cudaGetLastError());
@@ -535,7 +546,7 @@ int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes
     return SPX_OK;
   }
   const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
-  k_gen_real<<<nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y),
+  k_gen_real<<<nreal, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y),
                                                       static_cast<double2*>(lin));
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
@@ -556,8 +567,8 @@ int spx_jvp_lin(const spx_plan* pl, const void* lin, const void* v, void* Jv, vo
     const int nplanes = P.pb.Ns * P.nh;
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
     double2* w = static_cast<double2*>(ws);
-    k_gen_real<<<nreal, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w);
-    k_jvp_nl<<<nplanes + 1, pl->threads, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, ll, w, out);
+    k_gen_real<<<nreal, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w);
+    k_jvp_nl<<<nplanes + 1, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, ll, w, out);
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;

@@ -55,7 +55,6 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
   const double2* Fk = y + P.nc;
   const double a0 = P.pb.alpha_s[3 * s];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
   // lines: RHS  [G_y | C_{n-1}(y) x nt]
   //        JVP  [G_y | G_v | C_{n-1}(v) x nt | C_{n-1}(y) x nt]
   const int ng = JVP ? 2 : 1;
@@ -64,10 +63,8 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
   if (threadIdx.x < nt) {
     const int n = n0 + threadIdx.x;
     double* c = scoef + 4 * threadIdx.x;
-    c[0] = sqrt((double)(n + 1) * 0.5);
-    c[1] = sqrt((double)n * 0.5);
-    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
-    c[3] = P.pb.nu * colc(Nn, n);
+    const double* t = P.coef + ((size_t)s * Nn + n) * COEF_1V;
+    c[0] = t[0]; c[1] = t[1]; c[2] = t[2]; c[3] = t[3];
   }
   for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
     const int l = i / N, c = i - l * N;
@@ -100,7 +97,7 @@ __device__ void rhs1v_tile_t(const DevPlan& P, const double2* __restrict__ tab,
   }
   __syncthreads();
   double2* f = fft_axis_t<false, true>(r + ng * N, o + ng * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
-  const double ua = u0 / a0;
+  const double ua = P.ua[s];
   const double Dd = P.pb.D;
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
     const int l = i / N, c = i - l * N;
@@ -161,14 +158,11 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
   const size_t sbase = (size_t)s * Nn * N;
   const double a0 = P.pb.alpha_s[3 * s];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
   if (threadIdx.x < nt) {
     const int n = n0 + threadIdx.x;
     double* c = scoef + 4 * threadIdx.x;
-    c[0] = sqrt((double)(n + 1) * 0.5);
-    c[1] = sqrt((double)n * 0.5);
-    c[2] = qOc * sqrt(2.0 * (double)n) / a0 / (double)N;
-    c[3] = P.pb.nu * colc(Nn, n);
+    const double* t = P.coef + ((size_t)s * Nn + n) * COEF_1V;
+    c[0] = t[0]; c[1] = t[1]; c[2] = t[2]; c[3] = t[3];
   }
   // G = E_x + u_y B_z - u_z B_y at centred index c (masked)
   auto G = [&](int c) {
@@ -232,7 +226,7 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
   }
   // the epilogue's own staged operands (called by every thread; false: give up)
   if (!epi.prepare()) return;
-  const double ua = u0 / a0;
+  const double ua = P.ua[s];
   const double Dd = P.pb.D;
   // HERM: only the k <= 0 half (c <= centre) is evaluated; the epilogue's
   // pair() also writes the conjugates at the mirrored entries
@@ -307,7 +301,7 @@ __device__ void maxwell1v_g(const DevPlan& P, const double2* __restrict__ tab, c
   const double2* Fl = F + 2 * Ns * N;
   double2* Fo = F + (2 * Ns + 6) * N;
   const double rs2 = 0.70710678118654752440;
-  const double iO = 1.0 / pb.Omega_cs[0];
+  const double iO = P.iO0;
   const double2 zero = make_double2(0.0, 0.0);
   const double Ky = ktab(P, tab, 0, 0).x, Kz = ktab(P, tab, 2, 0).x;
   for (int pt = threadIdx.x; pt < N; pt += blockDim.x) {
@@ -352,7 +346,7 @@ __device__ void maxwell_range(const DevPlan& P, const double2* __restrict__ tab,
   const size_t pl = (size_t)P.plane;
   const double2* F = y + P.nc;
   const double rs2 = 0.70710678118654752440;
-  const double iO = 1.0 / pb.Omega_cs[0];
+  const double iO = P.iO0;
   for (int pt = p0 + threadIdx.x; pt < p1; pt += blockDim.x) {
     const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
     const double Kx = ktab(P, tab, 1, cx).x, Ky = ktab(P, tab, 0, cy).x, Kz = ktab(P, tab, 2, cz).x;
@@ -532,7 +526,24 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np, Ns = pb.Ns;
   const int s = id / P.nh, h = id % P.nh;
   const int n = h % Nn, m = (h / Nn) % Nm, p = h / (Nn * Nm);
-  const NlCoef cf = nl_coef(P, s, n, m, p);
+  // per-plane constants (square roots and divisions, ~300 FP64 instructions)
+  // once per CTA in shared memory instead of once per thread
+  __shared__ NlCoef s_cf;
+  __shared__ double s_lin[10];
+  if (threadIdx.x == 0) {
+    s_cf = nl_coef(P, s, n, m, p);
+    const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
+    const double rh = 0.5;
+    s_lin[0] = pb.qs[s] * pb.Omega_cs[s] / (double)pl;
+    s_lin[1] = pb.nu * (colc(Nn, n) + colc(Nm, m) + colc(Np, p));
+    s_lin[2] = sqrt((n + 1) * rh); s_lin[3] = sqrt(n * rh);
+    s_lin[4] = sqrt((m + 1) * rh); s_lin[5] = sqrt(m * rh);
+    s_lin[6] = sqrt((p + 1) * rh); s_lin[7] = sqrt(p * rh);
+    s_lin[8] = pb.u_s[3 * s] / a0;
+    s_lin[9] = pb.u_s[3 * s + 1] / a1;
+  }
+  __syncthreads();
+  const NlCoef cf = s_cf;
   const bool anyx = cf.ix[0] >= 0 || cf.ix[1] >= 0 || cf.ix[2] >= 0;
   const bool anyy = cf.iy[0] >= 0 || cf.iy[1] >= 0 || cf.iy[2] >= 0;
   const bool anyz = cf.iz[0] >= 0 || cf.iz[1] >= 0 || cf.iz[2] >= 0;
@@ -549,13 +560,9 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   double2* f = fft_planes_t<false, true>(sA, sB, P, tab);
 
   const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
-  const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
-  const double sc = pb.qs[s] * pb.Omega_cs[s] / (double)pl;
-  const double dcol = pb.nu * (colc(Nn, n) + colc(Nm, m) + colc(Np, p));
-  const double rh = 0.5;
-  const double snp = sqrt((n + 1) * rh), snm = sqrt(n * rh);
-  const double smp = sqrt((m + 1) * rh), smm = sqrt(m * rh);
-  const double spp = sqrt((p + 1) * rh), spm = sqrt(p * rh);
+  const double sc = s_lin[0], dcol = s_lin[1];
+  const double snp = s_lin[2], snm = s_lin[3], smp = s_lin[4], smm = s_lin[5], spp = s_lin[6], spm = s_lin[7];
+  const double ux = s_lin[8], uy = s_lin[9], uz = pb.u_s[3 * s + 2] / a2;
   const double2* Cp = lin + (size_t)id * pl;
   const size_t sn_ = pl, sm_ = (size_t)Nn * pl, sp_ = (size_t)Nn * Nm * pl;
   for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
@@ -565,7 +572,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     double k2 = 0.0;
     if (Nx > 1) {
       const double2 kt = ktab(P, tab, 1, cx);
-      double2 t = cscale(u0 / a0, C0);
+      double2 t = cscale(ux, C0);
       if (n + 1 < Nn) t = crfma(snp, Cp[pt + sn_], t);
       if (n >= 1) t = crfma(snm, Cp[pt - sn_], t);
       const double w = kt.x * a0;
@@ -574,7 +581,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     }
     if (Ny > 1) {
       const double2 kt = ktab(P, tab, 0, cy);
-      double2 t = cscale(u1 / a1, C0);
+      double2 t = cscale(uy, C0);
       if (m + 1 < Nm) t = crfma(smp, Cp[pt + sm_], t);
       if (m >= 1) t = crfma(smm, Cp[pt - sm_], t);
       const double w = kt.x * a1;
@@ -583,7 +590,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     }
     if (Nz > 1) {
       const double2 kt = ktab(P, tab, 2, cz);
-      double2 t = cscale(u2 / a2, C0);
+      double2 t = cscale(uz, C0);
       if (p + 1 < Np) t = crfma(spp, Cp[pt + sp_], t);
       if (p >= 1) t = crfma(spm, Cp[pt - sp_], t);
       const double w = kt.x * a2;
@@ -639,16 +646,15 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
   const double2* __restrict__ Wf = w + P.nc;
   const double a0 = P.pb.alpha_s[3 * s], a1 = P.pb.alpha_s[3 * s + 1], a2 = P.pb.alpha_s[3 * s + 2];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
   // lines: [G_y | c_m (nt) | W_{m+1} (nt)]
   const int nl = 2 * nt + 1;
   if (threadIdx.x < nt) {
     const int m = m0 + threadIdx.x;
     double* c = scoef + 4 * threadIdx.x;
-    c[0] = sqrt((double)(m + 1) * 0.5);
-    c[1] = sqrt((double)m * 0.5);
-    c[2] = (m + 1 < Nn) ? qOc * sqrt(2.0 * (double)(m + 1)) / a0 / (double)N : 0.0;   // k_{m+1}
-    c[3] = colc(Nn, m);
+    const double* t = P.coef + ((size_t)s * Nn + m) * COEF_1V;
+    c[0] = t[0]; c[1] = t[1];
+    c[2] = (m + 1 < Nn) ? t[COEF_1V + 2] : 0.0;   // k_{m+1}
+    c[3] = t[4];
   }
   for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
     const int l = i / N, c = i - l * N;
@@ -693,9 +699,9 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
   }
   __syncthreads();
   double2* q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
-  const double ua = u0 / a0;
+  const double ua = P.ua[s];
   const double Dd = P.pb.D;
-  const double iO = 1.0 / P.pb.Omega_cs[0];
+  const double iO = P.iO0;
   const double pre = P.pb.qs[s] * a0 * a1 * a2;
   double p_nu = 0.0, p_k = 0.0, p_u = 0.0;     // parameter terms of the own planes (pacc)
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
@@ -759,15 +765,14 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
   const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
   const double a0 = P.pb.alpha_s[3 * s], a1 = P.pb.alpha_s[3 * s + 1], a2 = P.pb.alpha_s[3 * s + 2];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const double qOc = P.pb.qs[s] * P.pb.Omega_cs[s];
   const int nl = 2 * nt + 1;
   if (threadIdx.x < nt) {
     const int m = m0 + threadIdx.x;
     double* c = scoef + 4 * threadIdx.x;
-    c[0] = sqrt((double)(m + 1) * 0.5);
-    c[1] = sqrt((double)m * 0.5);
-    c[2] = (m + 1 < Nn) ? qOc * sqrt(2.0 * (double)(m + 1)) / a0 / (double)N : 0.0;   // k_{m+1}
-    c[3] = colc(Nn, m);
+    const double* t = P.coef + ((size_t)s * Nn + m) * COEF_1V;
+    c[0] = t[0]; c[1] = t[1];
+    c[2] = (m + 1 < Nn) ? t[COEF_1V + 2] : 0.0;   // k_{m+1}
+    c[3] = t[4];
   }
   // lines: [G_y | c_m (nt) | W_{m+1} (nt)], masked, transform order (U line l = plane m0-1+l)
   for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
@@ -815,9 +820,9 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
   double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
   for (int c = threadIdx.x; c < N; c += blockDim.x)
     Rp[c] = kept(c, N, cut) ? q[nt * N + std_index(c, N)] : make_double2(0.0, 0.0);
-  const double ua = u0 / a0;
+  const double ua = P.ua[s];
   const double Dd = P.pb.D;
-  const double iO = 1.0 / P.pb.Omega_cs[0];
+  const double iO = P.iO0;
   const double pre = P.pb.qs[s] * a0 * a1 * a2;
   double p_nu = 0.0, p_k = 0.0, p_u = 0.0;
   for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
