@@ -87,20 +87,24 @@ struct BTerms {
   double cself, eself;
 };
 
+// Called by the 32 lanes of warp 0: lane j < stage fills the term of K_j (terms
+// in ascending j), so the products cost one warp-level multiply each.
 __device__ void fill_bterms(BTerms& T, int stage, double h) {
   const bool last = stage == rk::S - 1;
   const int row = last ? 12 : stage;
-  const int mask = last ? (bMask[12] | bMask[13]) : bMask[row];
-  T.n = 0;
-  for (int j = 0; j < stage; ++j)
-    if (mask & (1 << j)) {
-      T.j[T.n] = j;
-      T.c[T.n] = h * bCoef[row][j];
-      T.e[T.n] = last ? h * bCoef[13][j] : 0.0;
-      ++T.n;
-    }
-  T.cself = h * bCoef[row][stage];
-  T.eself = last ? h * bCoef[13][stage] : 0.0;
+  const unsigned mask = (unsigned)(last ? (bMask[12] | bMask[13]) : bMask[row]) & ((1u << stage) - 1u);
+  const int l = threadIdx.x & 31;
+  if (l < stage && (mask & (1u << l))) {
+    const int t = __popc(mask & ((1u << l) - 1u));
+    T.j[t] = l;
+    T.c[t] = h * bCoef[row][l];
+    T.e[t] = last ? h * bCoef[13][l] : 0.0;
+  }
+  if (l == 0) {
+    T.n = __popc(mask);
+    T.cself = h * bCoef[row][stage];
+    T.eself = last ? h * bCoef[13][stage] : 0.0;
+  }
 }
 
 // Source of a tile's stage input written earlier in this launch (L2-coherent loads).
@@ -361,7 +365,7 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
       const bool herm = ctl.herm != 0;
       for (int stage = 0; stage < rk::S; ++stage) {
         const double2* in = (stage == 0) ? Y : Sb[stage & 1];
-        if (threadIdx.x == 0) fill_bterms(terms, stage, h);
+        if (threadIdx.x < 32) fill_bterms(terms, stage, h);
         __syncthreads();
         double2* Ki = K + (size_t)stage * len;
         // one tile of this stage: the field tile (Maxwell + current) or Hermite

@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
     return;
   }
   if (threadIdx.x < 32) fill_terms(terms, stage, at.h);
+  __syncthreads();   // every thread reads terms.n when it sizes the staged operands
   const long long len = a.len;
   const double2* Y = pick(a.Y, s.cur);
   double2* Ki = a.K + (size_t)stage * len;
