@@ -147,8 +147,8 @@ struct EpiNextB {
     Ki[e] = v;
     Snext[e] = sn;
     if (two) {
-      Ki[e2] = make_double2(v.x, -v.y);
-      Snext[e2] = make_double2(sn.x, -sn.y);
+      Ki[e2] = conj_bits(v);
+      Snext[e2] = conj_bits(sn);
     }
   }
 };
@@ -206,8 +206,8 @@ struct EpiFinalB {
     Ki[e] = v;
     Ynew[e] = yn;
     if (two) {
-      Ki[e2] = make_double2(v.x, -v.y);
-      Ynew[e2] = make_double2(yn.x, -yn.y);
+      Ki[e2] = conj_bits(v);
+      Ynew[e2] = conj_bits(yn);
     }
   }
 };

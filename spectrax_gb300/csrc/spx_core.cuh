@@ -103,6 +103,11 @@ template <bool INV>
 __device__ __forceinline__ double2 twiddle(double2 v, double2 w) {
   return INV ? cmulc(v, w) : cmul(v, w);
 }
+// complex conjugate by flipping the sign bit with an integer instruction (the
+// result of -x, bit for bit, without spending an FP64 issue slot)
+__device__ __forceinline__ double2 conj_bits(double2 a) {
+  return make_double2(a.x, __longlong_as_double(__double_as_longlong(a.y) ^ (long long)0x8000000000000000ULL));
+}
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
 __device__ __forceinline__ double2 rot90(double2 a) {

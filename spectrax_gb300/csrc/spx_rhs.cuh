@@ -162,7 +162,8 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
     const int n = n0 + threadIdx.x;
     double* c = scoef + 4 * threadIdx.x;
     const double* t = P.coef + ((size_t)s * Nn + n) * COEF_1V;
-    c[0] = t[0]; c[1] = t[1]; c[2] = t[2]; c[3] = t[3];
+    // HERM: the 1/2 of the packed-spectrum split is folded into the coefficient (exact)
+    c[0] = t[0]; c[1] = t[1]; c[2] = HERM ? 0.5 * t[2] : t[2]; c[3] = t[3];
   }
   // G = E_x + u_y B_z - u_z B_y at centred index c (masked)
   auto G = [&](int c) {
@@ -252,8 +253,8 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
       } else {
         const double2* fl = f + (l >> 1) * N;
         const double2 W = fl[std_index(c, N)], Wm = fl[std_index(N - 1 - c, N)];
-        if ((l & 1) == 0) nl2 = make_double2(0.5 * (W.x + Wm.x), 0.5 * (W.y - Wm.y));
-        else nl2 = make_double2(0.5 * (W.y + Wm.y), -0.5 * (W.x - Wm.x));
+        if ((l & 1) == 0) nl2 = make_double2(W.x + Wm.x, W.y - Wm.y);
+        else nl2 = make_double2(W.y + Wm.y, Wm.x - W.x);
       }
       re = fma(cf[2], nl2.x, re);
       im = fma(cf[2], nl2.y, im);

@@ -63,8 +63,8 @@ struct EpiNext {
     Ki[e] = v;
     Snext[e] = sn;
     if (two) {
-      Ki[e2] = make_double2(v.x, -v.y);
-      Snext[e2] = make_double2(sn.x, -sn.y);
+      Ki[e2] = conj_bits(v);
+      Snext[e2] = conj_bits(sn);
     }
   }
   __device__ __forceinline__ double2 next(size_t e, int il, double2 v) const {
@@ -165,8 +165,8 @@ struct EpiFinal {
   __device__ __forceinline__ void pair(size_t e, int il, size_t e2, int il2, double2 v, bool two) {
     (*this)(e, il, v);
     if (two) {
-      Ki[e2] = make_double2(v.x, -v.y);
-      Ynew[e2] = make_double2(last_yn.x, -last_yn.y);
+      Ki[e2] = conj_bits(v);
+      Ynew[e2] = conj_bits(last_yn);
       if (adaptive) sq += last_sq;
     }
   }
