@@ -308,21 +308,27 @@ __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __r
     // over G lanes (G a power of two, G * rem <= 32) and reduced by shuffles, so
     // that a nearly empty warp does not cost a full task loop.  FP64 issue is
     // per warp instruction, whatever the number of active lanes.
+    // When the whole task list fits the CTA at least twice over, every task is
+    // split over GA lanes instead (one round): the four SM sub-partitions (warp
+    // w runs on sub-partition w % 4) then each carry a shorter loop, rather than
+    // warp 0 carrying full-length loops while the others idle.
     const int nfw = ntask >> 5;
     const int rem = ntask - (nfw << 5);
+    int GA = 1;
+    while (GA < 8 && ntask * GA * 2 <= (int)blockDim.x) GA *= 2;
     int G = 1;
-    if (rem > 0 && rem <= 16) {
+    if (GA == 1 && rem > 0 && rem <= 16) {
       G = 32 / rem;
       while (G & (G - 1)) G &= G - 1;
     }
-    const int units = nfw + (rem > 0 ? 1 : 0);
+    const int units = GA > 1 ? (ntask * GA + 31) >> 5 : nfw + (rem > 0 ? 1 : 0);
     const int lane = threadIdx.x & 31;
     for (int u = threadIdx.x >> 5; u < units; u += blockDim.x >> 5) {
-      const bool split = u == nfw;                     // the remainder warp
-      const int Gu = split ? G : 1;
-      const int t = split ? (nfw << 5) + lane / Gu : (u << 5) + lane;
-      const int g = split ? lane % Gu : 0;
-      const bool active = split ? (lane / Gu) < rem : true;
+      const bool split = GA == 1 && u == nfw;          // the remainder warp
+      const int Gu = GA > 1 ? GA : (split ? G : 1);
+      const int t = GA > 1 ? ((u << 5) + lane) / GA : (split ? (nfw << 5) + lane / Gu : (u << 5) + lane);
+      const int g = GA > 1 ? lane % GA : (split ? lane % Gu : 0);
+      const bool active = GA > 1 ? t < ntask : (split ? (lane / Gu) < rem : true);
       double2 A0 = make_double2(0.0, 0.0), A1 = A0, B0 = A0, B1 = A0;
       int l = 0, j = 0, kk0 = 0, kk1 = 0;
       bool two = false;
