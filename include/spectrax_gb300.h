@@ -174,6 +174,12 @@ int spx_vjp_noalloc(const spx_plan* plan, const void* y, const void* w, void* g,
  */
 int spx_rk_step_store(const spx_plan* plan, const void* y, double h, void* Ystages, void* Kstages,
                       void* ynext, void* stream);
+/* The same with `hermitian` = 1 for an exactly Hermitian y (C(-k) == conj C(k) on
+ * every line; odd Nx): packed real transforms, as the Dopri8 solver's
+ * `hermitian` option uses, so the stage inputs match its forward solve.  Fails
+ * with SPX_E_ARG on a plan whose wavenumber grid does not allow it. */
+int spx_rk_step_store_ex(const spx_plan* plan, const void* y, double h, void* Ystages, void* Kstages,
+                         void* ynext, int32_t hermitian, void* stream);
 /* Status word of spx_rk_step_store since the last call (SPX_ST_RUNNING = 0: no
  * problem; SPX_ST_WAIT_TIMEOUT: a bounded wait for staged data gave up and the
  * outputs are invalid); reading it resets it.  Synchronises `stream`. */
@@ -196,6 +202,11 @@ int spx_param_dots(const spx_plan* plan, const void* y, const void* g, double* a
  * concurrently (the plan holds the kernel's completion ticket). */
 int spx_vjp_param(const spx_plan* plan, const void* y, const void* w, void* g, double* acc, void* ws,
                   size_t ws_bytes, void* stream);
+/* The same with `hermitian` = 1 for exactly Hermitian y and w: every real-space
+ * line is real, two share one complex transform, only the k <= 0 half of each
+ * output plane is evaluated and g is written exactly Hermitian. */
+int spx_vjp_param_ex(const spx_plan* plan, const void* y, const void* w, void* g, double* acc, void* ws,
+                     size_t ws_bytes, int32_t hermitian, void* stream);
 
 /* ------------------------------------------------------------------ Dopri8 */
 typedef struct spx_dopri8_opts {

@@ -130,8 +130,10 @@ _PROTOS = {
     "spx_batch_run": (C.c_int, [_VP, _VP, _VP, _VP]),
     "spx_batch_results": (C.c_int, [_VP, C.POINTER(spx_batch_stats), C.POINTER(C.c_double), _VP]),
     "spx_rk_step_store": (C.c_int, [_VP, _VP, C.c_double, _VP, _VP, _VP, _VP]),
+    "spx_rk_step_store_ex": (C.c_int, [_VP, _VP, C.c_double, _VP, _VP, _VP, C.c_int32, _VP]),
     "spx_rk_status": (C.c_int, [C.POINTER(C.c_int32), _VP]),
     "spx_vjp_param": (C.c_int, [_VP, _VP, _VP, _VP, C.POINTER(C.c_double), _VP, C.c_size_t, _VP]),
+    "spx_vjp_param_ex": (C.c_int, [_VP, _VP, _VP, _VP, C.POINTER(C.c_double), _VP, C.c_size_t, C.c_int32, _VP]),
     "spx_lincomb": (C.c_int, [C.c_int64, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_double), _VP, _VP]),
     "spx_param_dots": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "spx_probe_fp64": (C.c_int, [_VP, C.c_int, C.c_int, _VP]),

@@ -7,15 +7,18 @@ history is computed exactly for the discrete solution:
 * forward: the fused device stepper (``Dopri8Solver``), keeping every
   m-th state (m = ceil(sqrt(N))) and the field energy of every step;
 * backward, segment by segment in reverse: recompute the segment's steps with
-  ``spx_rk_step_store`` (keeping the 13 stage inputs of each step), then sweep
+  ``spx_rk_step_store_ex`` (keeping the 13 stage inputs of each step), then sweep
   back through the steps with the Runge-Kutta adjoint recursion
       gk_j = h b_j lam + sum_{i>j} h a_ij gY_i ,   gY_j = J(Y_j)^H gk_j ,
       lam_n = lam_{n+1} + sum_j gY_j ,
-  using ``spx_vjp`` (plain transpose) on conjugated adjoints:
+  using ``spx_vjp_param_ex`` (plain transpose, plus the parameter sums) on
+  conjugated adjoints:
   conj(J^H lam) = J^T conj(lam), so every adjoint vector is stored conjugated;
 * parameter gradients accumulate Re sum conj(gk_j) . df/dtheta(Y_j) on the device
-  (``spx_param_dots``) for theta = (nu, k, u_x per species), plus the initial-state
-  terms for k and the perturbation amplitude.
+  (in the same launch) for theta = (nu, k, u_x per species), plus the
+  initial-state terms for k and the perturbation amplitude;
+* an exactly Hermitian trajectory (odd Nx, the spectrum of real fields) runs all
+  three on packed real transforms (``hermitian=True``, the default).
 
 ``TwoStreamLoss`` puts this behind ``torch.autograd.Function`` for the adjoint
 workload (1D1V two-stream, loss = LSQ slope of log E over t in [10, 40] plus
@@ -54,10 +57,16 @@ def lincomb(out: torch.Tensor, terms):
 class Dopri8Adjoint:
     """Fixed-step Dopri8 trajectory with its discrete adjoint."""
 
-    def __init__(self, plan: Plan, dt: float, nsteps: int, ckpt_every: int | None = None, masses=None):
+    def __init__(self, plan: Plan, dt: float, nsteps: int, ckpt_every: int | None = None, masses=None,
+                 hermitian=True):
         if plan.problem.Ny != 1 or plan.problem.Nz != 1 or plan.problem.Nm != 1 or plan.problem.Np != 1:
             raise ValueError("the adjoint is implemented for the 1D1V layout")
         self.plan, self.dt, self.N = plan, float(dt), int(nsteps)
+        # exactly Hermitian trajectories (the spectra of real fields) run the
+        # forward, the recomputation and the adjoint sweep on packed transforms;
+        # the adjoint of a Hermitian state stays exactly Hermitian
+        self.hermitian = bool(hermitian)
+        self.herm = False
         self.m = int(ckpt_every or math.ceil(math.sqrt(self.N)))
         self.masses = masses
         self.n = plan.state_len
@@ -68,9 +77,11 @@ class Dopri8Adjoint:
 
     # ------------------------------------------------------------------ forward
     def forward(self, y0: torch.Tensor):
-        # general (complex-transform) stages, the same kernels as the recomputation
+        # the stage kernels the recomputation uses too: packed real transforms when
+        # y0 is exactly Hermitian (odd Nx), general complex transforms otherwise
         s = Dopri8Solver(self.plan, 0.0, self.ts[-1], self.dt, ts=self.ts, adaptive=False,
-                         save_states=False, masses=self.masses, max_steps=self.N + 10, hermitian=False)
+                         save_states=False, masses=self.masses, max_steps=self.N + 10,
+                         hermitian=self.hermitian)
         s.reset(y0)
         ckpts = [y0.clone()]
         done = 0
@@ -84,6 +95,7 @@ class Dopri8Adjoint:
             raise RuntimeError(f"forward solve failed: {st}")
         E = s.energies()[:, 0].clone()
         self.ckpts = ckpts
+        self.herm = bool(st["hermitian"])
         return E, ckpts[-1]
 
     # ------------------------------------------------------------------ backward
@@ -107,9 +119,9 @@ class Dopri8Adjoint:
         B = self._buffers()
         L = _lib.lib()
         for q in range(steps):
-            _lib.check(L.spx_rk_step_store(self.plan.handle, _ptr(B["Ys"][q, 0]), C.c_double(self.dt),
-                                           _ptr(B["Ys"][q]), _ptr(B["Kb"]), _ptr(B["Ys"][q + 1, 0]),
-                                           _stream_ptr()), "spx_rk_step_store")
+            _lib.check(L.spx_rk_step_store_ex(self.plan.handle, _ptr(B["Ys"][q, 0]), C.c_double(self.dt),
+                                              _ptr(B["Ys"][q]), _ptr(B["Kb"]), _ptr(B["Ys"][q + 1, 0]),
+                                              int(self.herm), _stream_ptr()), "spx_rk_step_store_ex")
 
     def _sweep(self, steps):
         """Adjoint sweep back over `steps` steps (stage inputs in Ys), seeding the
@@ -129,8 +141,8 @@ class Dopri8Adjoint:
                     if aij != 0.0:
                         terms.append((h * aij, gY[i]))
                 lincomb(gk, terms)
-                _lib.check(L.spx_vjp_param(self.plan.handle, _ptr(Yq[j]), _ptr(gk), _ptr(gY[j]), accp, ws, wsb,
-                                           _stream_ptr()), "spx_vjp_param")
+                _lib.check(L.spx_vjp_param_ex(self.plan.handle, _ptr(Yq[j]), _ptr(gk), _ptr(gY[j]), accp, ws, wsb,
+                                              int(self.herm), _stream_ptr()), "spx_vjp_param_ex")
             lincomb(mu, [(1.0, mu)] + [(1.0, gY[j]) for j in range(S)])
             mu[nc:].add_((B["coef"][q] * c2) * Yq[0, nc:].conj())
 
@@ -243,15 +255,18 @@ def loss_from_energy(E, w):
 class TwoStreamProblem:
     """Forward loss and adjoint gradients of the two-stream adjoint workload."""
 
-    def __init__(self, Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0, ckpt_every=None, window=(10.0, 40.0)):
+    def __init__(self, Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0, ckpt_every=None, window=(10.0, 40.0),
+                 hermitian=True):
         self.Nx, self.Nn, self.dt, self.N, self.seed = Nx, Nn, dt, nsteps, seed
+        self.hermitian = hermitian
         self.ckpt_every = ckpt_every
         self.window = window
 
     def _build(self, k, nu, u, amp):
         p, bg, delta, ddk = two_stream_setup(k, nu, u, amp, self.Nx, self.Nn, seed=self.seed)
         plan = plan_for_params(p, "divide")
-        adj = Dopri8Adjoint(plan, self.dt, self.N, self.ckpt_every, masses=[1.0, 1.0, 1836.0])
+        adj = Dopri8Adjoint(plan, self.dt, self.N, self.ckpt_every, masses=[1.0, 1.0, 1836.0],
+                            hermitian=self.hermitian)
         y0 = torch.from_numpy(bg + amp * delta).to(plan.device)
         return p, plan, adj, y0, delta, ddk
 

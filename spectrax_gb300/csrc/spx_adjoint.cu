@@ -41,7 +41,7 @@ __device__ void fill_terms_fixed(EpiTerms& T, int stage, double h) {
   T.eself = 0.0;
 }
 
-template <bool LAST>
+template <bool LAST, bool HERM>
 __global__ void __launch_bounds__(NTHREADS, 2) k_rk_stage_st(const DevPlan* __restrict__ gP,
                                                             const double2* __restrict__ gtab,
                                                             const double2* y, double2* Yb, double2* Kb,
@@ -64,12 +64,12 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_rk_stage_st(const DevPlan* __re
   io.Ki = Kb + (size_t)stage * len;
   io.out = LAST ? ynext : Yb + (size_t)(stage + 1) * len;
   io.npf = npf;
-  io.herm = false;
+  io.herm = HERM;
   io.rtol = io.atol = 0.0;
   io.adaptive = 0;
   io.timeout_status = &g_rk_status;
   io.persistent = false;
-  staged_stage_1v<LAST>(P, stab, io, terms, bars, [](auto&) {});
+  staged_stage_1v<LAST, HERM ? 1 : 0>(P, stab, io, terms, bars, [](auto&) {});
 }
 
 struct LinTerms {
@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(NTHREADS) k_param_dots_1v(const DevPlan* __res
 // ws: part (Ns * ntiles * N double2) | pp (grid x (2 + SPX_MAX_SPECIES) doubles) |
 // gpart (Ns * groups * N double2); the tickets live in the plan (calls on one
 // plan are serialised, as its workspace is).
+template <bool HERM>
 __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __restrict__ gP,
                                                               const double2* __restrict__ gtab,
                                                               const double2* __restrict__ y,
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
         timed_out = true;
       } else {
         double pacc[3] = {0.0, 0.0, 0.0};
-        vjp1v_tile_u(P, stab, Uy, Uw, yF3, wE, g, part, s, tile, m0, nt, sA, sB, scoef, pacc);
+        vjp1v_tile_u<HERM>(P, stab, Uy, Uw, yF3, wE, g, part, s, tile, m0, nt, sA, sB, scoef, pacc);
 #pragma unroll
         for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k)
           loc[k] = (k == 0) ? pacc[0] : (k == 1) ? pacc[1] : (k == 2 + s) ? pacc[2] : 0.0;
@@ -336,12 +337,19 @@ static int adj_setup() {
   SPX_CUDA(cudaMemcpyToSymbol(aMask, m, sizeof(m)));
   const int optin = smem_optin();
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<false>));
-  SPX_CUDA(cudaFuncSetAttribute(k_rk_stage_st<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<true>));
-  SPX_CUDA(cudaFuncSetAttribute(k_rk_stage_st<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v));
-  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+#define SPX_RK_ATTR(L, H)                                                                              \
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<L, H>));                                           \
+  SPX_CUDA(cudaFuncSetAttribute(k_rk_stage_st<L, H>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                optin - (int)fa.sharedSizeBytes));
+  SPX_RK_ATTR(false, false)
+  SPX_RK_ATTR(true, false)
+  SPX_RK_ATTR(false, true)
+  SPX_RK_ATTR(true, true)
+#undef SPX_RK_ATTR
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v<false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v<true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_param_dots_1v));
   SPX_CUDA(cudaFuncSetAttribute(k_param_dots_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   done = true;
@@ -356,11 +364,21 @@ extern "C" {
 
 int spx_rk_step_store(const spx_plan* pl, const void* y, double h, void* Ystages, void* Kstages, void* ynext,
                       void* stream) {
+  return spx_rk_step_store_ex(pl, y, h, Ystages, Kstages, ynext, 0, stream);
+}
+
+int spx_rk_step_store_ex(const spx_plan* pl, const void* y, double h, void* Ystages, void* Kstages, void* ynext,
+                         int32_t hermitian, void* stream) {
   if (!pl || !y || !Ystages || !Kstages || !ynext) { set_error("spx_rk_step_store: null argument"); return SPX_E_ARG; }
   if (pl->host.path != 0) {
     set_error("spx_rk_step_store: only the 1D1V layout (Ny = Nz = Nm = Np = 1) is supported");
     return SPX_E_UNSUPPORTED;
   }
+  if (hermitian && !pl->herm_ok) {
+    set_error("spx_rk_step_store_ex: packed transforms need an odd Nx with an antisymmetric wavenumber grid");
+    return SPX_E_ARG;
+  }
+  const int herm = hermitian ? 1 : 0;
   int rc = adj_setup();
   if (rc != SPX_OK) return rc;
   const DevPlan& P = pl->host;
@@ -370,7 +388,12 @@ int spx_rk_step_store(const spx_plan* pl, const void* y, double h, void* Ystages
   if (static_cast<const void*>(Yb) != y)
     SPX_CUDA(cudaMemcpyAsync(Yb, y, sizeof(double2) * len, cudaMemcpyDeviceToDevice, st));
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<true>));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_rk_stage_st<true, false>));
+  {
+    cudaFuncAttributes fh;
+    SPX_CUDA(cudaFuncGetAttributes(&fh, k_rk_stage_st<true, true>));
+    if (fh.sharedSizeBytes > fa.sharedSizeBytes) fa = fh;
+  }
   int npf = 0;
   const size_t smem = stage_smem_1v(pl, fa.sharedSizeBytes, &npf);
   if (npf < 1) { set_error("spx_rk_step_store: Nx / tile too large for the stage kernel"); return SPX_E_UNSUPPORTED; }
@@ -381,10 +404,13 @@ int spx_rk_step_store(const spx_plan* pl, const void* y, double h, void* Ystages
     const double2* yb = Yb;
     double2* kb = static_cast<double2*>(Kstages);
     double2* yn = static_cast<double2*>(ynext);
-    if (stage < rk::S - 1)
-      SPX_CUDA(launch_pdl(k_rk_stage_st<false>, grid, pl->threads, smem, st, dp, dt, yb, Yb, kb, yn, h, stage, npf));
+    const bool last = stage == rk::S - 1;
+    if (herm)
+      SPX_CUDA(launch_pdl(last ? k_rk_stage_st<true, true> : k_rk_stage_st<false, true>, grid, pl->threads, smem,
+                          st, dp, dt, yb, Yb, kb, yn, h, stage, npf));
     else
-      SPX_CUDA(launch_pdl(k_rk_stage_st<true>, grid, pl->threads, smem, st, dp, dt, yb, Yb, kb, yn, h, stage, npf));
+      SPX_CUDA(launch_pdl(last ? k_rk_stage_st<true, false> : k_rk_stage_st<false, false>, grid, pl->threads, smem,
+                          st, dp, dt, yb, Yb, kb, yn, h, stage, npf));
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
@@ -443,10 +469,19 @@ int spx_param_dots(const spx_plan* pl, const void* y, const void* g, double* acc
 
 int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, double* acc, void* ws,
                   size_t ws_bytes, void* stream) {
+  return spx_vjp_param_ex(pl, y, w, g, acc, ws, ws_bytes, 0, stream);
+}
+
+int spx_vjp_param_ex(const spx_plan* pl, const void* y, const void* w, void* g, double* acc, void* ws,
+                     size_t ws_bytes, int32_t hermitian, void* stream) {
   if (!pl || !y || !w || !g || !acc || !ws) { set_error("spx_vjp_param: null argument"); return SPX_E_ARG; }
   if (pl->host.path != 0) {
     set_error("spx_vjp_param: only the 1D1V layout is supported");
     return SPX_E_UNSUPPORTED;
+  }
+  if (hermitian && !pl->herm_ok) {
+    set_error("spx_vjp_param_ex: packed transforms need an odd Nx with an antisymmetric wavenumber grid");
+    return SPX_E_ARG;
   }
   if (ws_bytes < pl->ws_bytes || (reinterpret_cast<uintptr_t>(ws) & 255)) {
     set_error("spx_vjp_param: workspace too small or not 256-byte aligned");
@@ -469,9 +504,10 @@ int spx_vjp_param(const spx_plan* pl, const void* y, const void* w, void* g, dou
   const double2* dt = pl->d_tab;
   // a plain launch: with a programmatic early start the CTAs of this small grid
   // (one per SM) were placed less evenly and the kernel ran longer
-  k_vjp_param_1v<<<grid, pl->threads, smem, st>>>(dp, dt, static_cast<const double2*>(y),
-                                                  static_cast<const double2*>(w), static_cast<double2*>(g),
-                                                  reinterpret_cast<double2*>(wsb), pp, gpart, ticket, acc);
+  auto kern = hermitian ? k_vjp_param_1v<true> : k_vjp_param_1v<false>;
+  kern<<<grid, pl->threads, smem, st>>>(dp, dt, static_cast<const double2*>(y), static_cast<const double2*>(w),
+                                        static_cast<double2*>(g), reinterpret_cast<double2*>(wsb), pp, gpart,
+                                        ticket, acc);
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
 }

@@ -20,6 +20,7 @@ struct spx_plan {
   size_t smem_gen = 0;          // dynamic smem of the general kernels
   size_t ws_bytes = 0;          // scratch of spx_rhs
   int threads = 256;            // CTA width of the right-hand-side kernels (<= 256)
+  bool herm_ok = false;         // fused 1D1V path, odd Nx, antisymmetric k table: packed transforms valid
 };
 
 namespace spx {

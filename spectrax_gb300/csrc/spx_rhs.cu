@@ -433,6 +433,14 @@ int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx
   pl->threads = threads > 0 ? threads : NTHREADS;
   int rc = build_plan_host(pb, nsm, pl, tile);
   if (rc != SPX_OK) { delete pl; return rc; }
+  {
+    // streaming and Maxwell terms keep C(-k) = conj C(k) only if k(N-1-c) == -k(c) exactly
+    const DevPlan& H = pl->host;
+    bool anti = H.path == 0 && (H.ax[1].n & 1);
+    for (int c = 0; anti && c < H.ax[1].n; ++c)
+      if (!(pl->tab[H.ax[1].kofs + c].x == -pl->tab[H.ax[1].kofs + H.ax[1].n - 1 - c].x)) anti = false;
+    pl->herm_ok = anti;
+  }
   rc = set_attrs();
   if (rc != SPX_OK) { delete pl; return rc; }
   const size_t hdr = (sizeof(DevPlan) + 255) / 256 * 256;

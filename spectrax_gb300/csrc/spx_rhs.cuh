@@ -758,6 +758,7 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
 // ((nt+2)*N each, zero outside [0, Nn)); yF3: y's E_x, B_z, B_y lines; wE: w's
 // E_x, E_y, E_z lines (3*N each).  pacc (3 doubles) accumulates the parameter
 // terms of the own planes: Re w . (-col C), Re w . f_K, Re w . (-i K C).
+template <bool HERM>
 __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict__ tab,
                                     const double2* Uy, const double2* Uw, const double2* yF3,
                                     const double2* wE, double2* __restrict__ g,
@@ -766,7 +767,6 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
   const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
   const double a0 = P.pb.alpha_s[3 * s], a1 = P.pb.alpha_s[3 * s + 1], a2 = P.pb.alpha_s[3 * s + 2];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-  const int nl = 2 * nt + 1;
   if (threadIdx.x < nt) {
     const int m = m0 + threadIdx.x;
     double* c = scoef + 4 * threadIdx.x;
@@ -775,71 +775,130 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
     c[2] = (m + 1 < Nn) ? t[COEF_1V + 2] : 0.0;   // k_{m+1}
     c[3] = t[4];
   }
-  // lines: [G_y | c_m (nt) | W_{m+1} (nt)], masked, transform order (U line l = plane m0-1+l)
-  for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
-    double2 v = make_double2(0.0, 0.0);
-    if (kept(c, N, cut)) {
-      if (l == 0) {
-        v = yF3[c];
-        v = crfma(u1, yF3[N + c], v);
-        v = crfma(-u2, yF3[2 * N + c], v);
-      } else if (l <= nt) {
-        v = Uy[(size_t)l * N + c];                    // plane m0 + l - 1
-      } else {
-        // forward transform of W as conj(inverse transform of conj W), so that all
-        // 2 nt + 1 lines go through one transform pass
-        const double2 wv = Uw[(size_t)(l - nt + 1) * N + c];   // plane m0 + (l - 1 - nt) + 1
-        v = make_double2(wv.x, -wv.y);
-      }
+  // spectrum (masked, centred index c) of line q of [G_y | c_m (nt) | conj W_{m+1} (nt)]
+  // (U line l = plane m0-1+l); the inverse transform of conj W is conj(FFT W), so
+  // every line goes through one inverse pass
+  auto spec = [&](int q, int c) -> double2 {
+    if (q == 0) {
+      double2 v = yF3[c];
+      v = crfma(u1, yF3[N + c], v);
+      return crfma(-u2, yF3[2 * N + c], v);
     }
-    sA[l * N + std_index(c, N)] = v;
-  }
-  __syncthreads();
-  double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
-  double2* o = (r == sA) ? sB : sA;
-  // this tile's share of the field sum R_s(x) = sum_n k_n c_{n-1}(x) W_n(x), as an
-  // extra line after the nt product lines: its inverse transform (masked) goes
-  // through the same pass, and the tile stores the kept modes as its partial
-  for (int x = threadIdx.x; x < N; x += blockDim.x) {
-    double2 acc = make_double2(0.0, 0.0);
-    for (int l = 0; l < nt; ++l) {
-      const double k = scoef[4 * l + 2];
-      const double2 wt = r[(1 + nt + l) * N + x];
-      acc = cfma(cscale(k, r[(1 + l) * N + x]), make_double2(wt.x, -wt.y), acc);
-    }
-    r[(1 + 2 * nt) * N + x] = acc;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-    const int x = i % N;
-    const double2 wt = r[(1 + nt) * N + i];
-    r[(1 + nt) * N + i] = cmul(r[x], make_double2(wt.x, -wt.y));
-  }
-  __syncthreads();
-  double2* q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
+    if (q <= nt) return Uy[(size_t)q * N + c];                     // plane m0 + q - 1
+    const double2 wv = Uw[(size_t)(q - nt + 1) * N + c];           // plane m0 + (q - 1 - nt) + 1
+    return make_double2(wv.x, -wv.y);
+  };
+  const double2* q;                     // inverse transforms of the products (and R) by line
   double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
-  for (int c = threadIdx.x; c < N; c += blockDim.x)
-    Rp[c] = kept(c, N, cut) ? q[nt * N + std_index(c, N)] : make_double2(0.0, 0.0);
+  if constexpr (!HERM) {
+    const int nl = 2 * nt + 1;
+    for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
+      const int l = i / N, c = i - l * N;
+      sA[l * N + std_index(c, N)] = kept(c, N, cut) ? spec(l, c) : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
+    double2* o = (r == sA) ? sB : sA;
+    // this tile's share of the field sum R_s(x) = sum_n k_n c_{n-1}(x) W_n(x), as an
+    // extra line after the nt product lines: its inverse transform (masked) goes
+    // through the same pass, and the tile stores the kept modes as its partial
+    for (int x = threadIdx.x; x < N; x += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int l = 0; l < nt; ++l) {
+        const double k = scoef[4 * l + 2];
+        const double2 wt = r[(1 + nt + l) * N + x];
+        acc = cfma(cscale(k, r[(1 + l) * N + x]), make_double2(wt.x, -wt.y), acc);
+      }
+      r[(1 + 2 * nt) * N + x] = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
+      const int x = i % N;
+      const double2 wt = r[(1 + nt) * N + i];
+      r[(1 + nt) * N + i] = cmul(r[x], make_double2(wt.x, -wt.y));
+    }
+    __syncthreads();
+    q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
+    for (int c = threadIdx.x; c < N; c += blockDim.x)
+      Rp[c] = kept(c, N, cut) ? q[nt * N + std_index(c, N)] : make_double2(0.0, 0.0);
+  } else {
+    // Exactly Hermitian y and w: every real-space line is real, so two lines share
+    // one complex transform (inverse of X_a + i X_b is x_a + i x_b).
+    const int nreal = 2 * nt + 1, nin = nt + 1;
+    for (int i = threadIdx.x; i < nin * N; i += blockDim.x) {
+      const int j = i / N, c = i - j * N;
+      double2 z = make_double2(0.0, 0.0);
+      if (kept(c, N, cut)) {
+        const double2 xa = spec(2 * j, c);
+        const double2 xb = (2 * j + 1 < nreal) ? spec(2 * j + 1, c) : make_double2(0.0, 0.0);
+        z = make_double2(xa.x - xb.y, xa.y + xb.x);
+      }
+      sA[j * N + std_index(c, N)] = z;
+    }
+    __syncthreads();
+    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nin, 1, 1, N, 0}, cut);
+    double2* o = (r == sA) ? sB : sA;
+    auto rl = [&](int ql, int x) -> double {
+      const double2 z = r[(ql >> 1) * N + x];
+      return (ql & 1) ? z.y : z.x;
+    };
+    // real lines p_l = G W_l (l < nt) and R = sum_l k_{m0+l+1} c_l W_l, in pairs
+    const int nprod = nt + 1, nout = (nprod + 1) / 2;
+    for (int i = threadIdx.x; i < nout * N; i += blockDim.x) {
+      const int j = i / N, x = i - j * N;
+      double pv[2];
+#pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2) {
+        const int l = 2 * j + h2;
+        double v = 0.0;
+        if (l < nt) {
+          v = rl(0, x) * rl(1 + nt + l, x);
+        } else if (l == nt) {
+          for (int ll = 0; ll < nt; ++ll) v = fma(scoef[4 * ll + 2] * rl(1 + ll, x), rl(1 + nt + ll, x), v);
+        }
+        pv[h2] = v;
+      }
+      o[j * N + x] = make_double2(pv[0], pv[1]);
+    }
+    __syncthreads();
+    double2* qq = fft_axis_t<true, true>(o, r, P.ax[1], tab, Lines{nout, 1, 1, N, 0}, cut);
+    q = qq;
+    // R's spectrum: P_b of a pair (nt odd) or P_a (nt even), at every kept mode
+    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+      double2 v = make_double2(0.0, 0.0);
+      if (kept(c, N, cut)) {
+        const double2* fl = qq + (nt >> 1) * N;
+        const double2 W = fl[std_index(c, N)], Wm = fl[std_index(N - 1 - c, N)];
+        v = (nt & 1) ? make_double2(0.5 * (W.y + Wm.y), 0.5 * (Wm.x - W.x))
+                     : make_double2(0.5 * (W.x + Wm.x), 0.5 * (W.y - Wm.y));
+      }
+      Rp[c] = v;
+    }
+  }
   const double ua = P.ua[s];
   const double Dd = P.pb.D;
   const double iO = P.iO0;
   const double pre = P.pb.qs[s] * a0 * a1 * a2;
   double p_nu = 0.0, p_k = 0.0, p_u = 0.0;
-  for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-    const int l = i / N, c = i - l * N;
+  // HERM: only the k <= 0 half; the mirrored entry gets the conjugate and the
+  // same parameter contributions
+  const int Nc = HERM ? (N + 1) / 2 : N;
+  for (int i = threadIdx.x; i < nt * Nc; i += blockDim.x) {
+    const int l = i / Nc, c = i - l * Nc;
     const int m = m0 + l;
     const double* cf = scoef + 4 * l;
     const double2 kt = ktab(P, tab, 1, c);
     const double wk = kt.x * a0;
     const double2 Wm = Uw[(size_t)l * N + c], W0 = Uw[(size_t)(l + 1) * N + c], Wp = Uw[(size_t)(l + 2) * N + c];
     const double2 Cm = Uy[(size_t)l * N + c], C0 = Uy[(size_t)(l + 1) * N + c], Cp = Uy[(size_t)(l + 2) * N + c];
-    p_nu += -cf[3] * (W0.x * C0.x - W0.y * C0.y);
+    const int c2 = N - 1 - c;
+    const double mult = (HERM && c2 != c) ? 2.0 : 1.0;
     double2 tc = cscale(ua, C0);
     tc = crfma(cf[0], Cp, tc);
     tc = crfma(cf[1], Cm, tc);
-    p_k += W0.x * (wk * tc.y) - W0.y * (-wk * tc.x);
-    p_u += W0.x * (kt.x * C0.y) - W0.y * (-kt.x * C0.x);
+    p_nu = fma(mult, -cf[3] * (W0.x * C0.x - W0.y * C0.y), p_nu);
+    p_k = fma(mult, W0.x * (wk * tc.y) - W0.y * (-wk * tc.x), p_k);
+    p_u = fma(mult, W0.x * (kt.x * C0.y) - W0.y * (-kt.x * C0.x), p_u);
     double2 t = cscale(ua, W0);
     t = crfma(cf[0], Wp, t);
     t = crfma(cf[1], Wm, t);
@@ -848,7 +907,15 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
     double re = fma(wk, t.y, -d * W0.x);
     double im = fma(-wk, t.x, -d * W0.y);
     if (m + 1 < Nn && kept(c, N, cut)) {
-      const double2 v = q[l * N + std_index(c, N)];
+      double2 v;
+      if constexpr (!HERM) {
+        v = q[l * N + std_index(c, N)];
+      } else {
+        const double2* fl = q + (l >> 1) * N;
+        const double2 W = fl[std_index(c, N)], Wn = fl[std_index(c2, N)];
+        v = (l & 1) ? make_double2(0.5 * (W.y + Wn.y), 0.5 * (Wn.x - W.x))
+                    : make_double2(0.5 * (W.x + Wn.x), 0.5 * (W.y - Wn.y));
+      }
       re = fma(cf[2], v.x, re);
       im = fma(cf[2], v.y, im);
     }
@@ -863,6 +930,7 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
       im = fma(co, wE[c].y, im);
     }
     g[(size_t)(s * Nn + m) * N + c] = make_double2(re, im);
+    if (HERM && c2 != c) g[(size_t)(s * Nn + m) * N + c2] = conj_bits(make_double2(re, im));
   }
   pacc[0] += p_nu; pacc[1] += p_k; pacc[2] += p_u;
 }

@@ -225,7 +225,9 @@ struct SrcL2 {
 // field CTA).  `terms` must be visible to every thread; bars / red are the
 // caller's shared scratch.  LAST: `tail(el)` is called by every thread of every
 // CTA with the stage's EpiFinal (or an empty accumulator) for the error reduction.
-template <bool LAST, class Tail>
+// HM: 0 general transforms only, 1 packed transforms only, 2 chosen by io.herm
+// at run time (both variants compiled into the caller).
+template <bool LAST, int HM = 2, class Tail>
 __device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ stab, const StageIO& io,
                                 const EpiTerms& terms, uint64_t* bars, Tail&& tail) {
   const long long len = io.len;
@@ -305,12 +307,12 @@ __device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
   }
   if constexpr (!LAST) {
     EpiNext epi{io.Ki, io.out, io.Y, io.K, len, &terms, pf, own, npf, &bars[1]};
-    if (io.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
+    if (HM == 1 || (HM == 2 && io.herm)) rhs1v_tile_u<HM != 0>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
     else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
   } else {
     EpiFinal el{io.Ki, io.out, io.Y, io.K, len, &terms, pf, own, npf, &bars[1],
                 io.rtol, io.atol, io.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
-    if (io.herm) rhs1v_tile_u<true>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
+    if (HM == 1 || (HM == 2 && io.herm)) rhs1v_tile_u<HM != 0>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
     else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
     tail(el);
   }

@@ -98,3 +98,74 @@ def test_fused_vjp_param_matches_separate_kernels():
     # same algebra; the fused kernel forms the forward transform of w as conj(inverse(conj w))
     assert (torch.linalg.vector_norm(g1 - g2) / torch.linalg.vector_norm(g1)).item() < 1e-13
     np.testing.assert_allclose((a2.cpu().numpy() - 0.25) / 2, a1.cpu().numpy(), rtol=1e-12, atol=1e-300)
+
+
+def _hermitian(v, N):
+    L = v.reshape(-1, N).copy()
+    c0 = N // 2
+    L[:, c0] = L[:, c0].real
+    L[:, :c0] = np.conj(L[:, ::-1][:, :c0])
+    return L.ravel()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("Nx,Nn", [(17, 24), (65, 40), (9, 5)])
+def test_packed_vjp_param_matches_general(Nx, Nn):
+    # exactly Hermitian y and w: the packed-transform VJP agrees with the general
+    # one to rounding, writes an exactly Hermitian g, and the parameter sums agree
+    import ctypes as C
+    import torch
+    from spectrax_gb300 import _lib
+    from spectrax_gb300.adjoint import two_stream_setup
+    from spectrax_gb300.vector_field import plan_for_params
+    p, bg, delta, _ = two_stream_setup(0.3, 1.2, 0.5, 1e-3, Nx, Nn, seed=2)
+    plan = plan_for_params(p, "divide")
+    n = plan.state_len
+    rng = np.random.default_rng(7)
+    y = torch.from_numpy(_hermitian(bg + 1e-2 * (rng.standard_normal(n) + 1j * rng.standard_normal(n)), Nx)).cuda()
+    w = torch.from_numpy(_hermitian(rng.standard_normal(n) + 1j * rng.standard_normal(n), Nx)).cuda()
+    g1, g2 = torch.empty_like(y), torch.empty_like(y)
+    a1 = torch.zeros(5, dtype=torch.float64, device="cuda")
+    a2 = torch.zeros(5, dtype=torch.float64, device="cuda")
+    L = _lib.lib()
+    ws, wsb = plan.ws_ptr()
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+    _lib.check(L.spx_vjp_param_ex(plan.handle, ptr(y), ptr(w), ptr(g1), dp(a1), ws, wsb, 0, None), "general")
+    _lib.check(L.spx_vjp_param_ex(plan.handle, ptr(y), ptr(w), ptr(g2), dp(a2), ws, wsb, 1, None), "packed")
+    torch.cuda.synchronize()
+    G2 = g2.cpu().numpy().reshape(-1, Nx)
+    assert np.array_equal(G2, np.conj(G2[:, ::-1]))
+    assert (torch.linalg.vector_norm(g1 - g2) / torch.linalg.vector_norm(g1)).item() < 1e-13
+    np.testing.assert_allclose(a2.cpu().numpy(), a1.cpu().numpy(), rtol=1e-12, atol=1e-14 * float(a1.abs().max()))
+
+
+@pytest.mark.gpu
+def test_packed_entry_points_reject_even_nx():
+    import ctypes as C
+    import torch
+    from spectrax_gb300 import _lib
+    from spectrax_gb300.adjoint import two_stream_setup
+    from spectrax_gb300.vector_field import plan_for_params
+    p, bg, _, _ = two_stream_setup(0.3, 1.2, 0.5, 1e-3, 16, 8, seed=2)
+    plan = plan_for_params(p, "divide")
+    y = torch.from_numpy(bg).cuda()
+    Ys = torch.empty((13, plan.state_len), dtype=torch.complex128, device="cuda")
+    K = torch.empty_like(Ys)
+    yn = torch.empty_like(y)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    rc = _lib.lib().spx_rk_step_store_ex(plan.handle, ptr(y), C.c_double(0.05), ptr(Ys), ptr(K), ptr(yn), 1, None)
+    assert rc == _lib.SPX_E_ARG
+    acc = torch.zeros(5, dtype=torch.float64, device="cuda")
+    ws, wsb = plan.ws_ptr()
+    rc = _lib.lib().spx_vjp_param_ex(plan.handle, ptr(y), ptr(y), ptr(yn),
+                                     C.cast(C.c_void_p(acc.data_ptr()), C.POINTER(C.c_double)), ws, wsb, 1, None)
+    assert rc == _lib.SPX_E_ARG
+
+
+@pytest.mark.gpu
+def test_adjoint_runs_packed_transforms_for_hermitian_states():
+    prob = _problem(nsteps=20)
+    p, plan, adj, y0, _, _ = prob._build(0.35, 1.0, 0.5, 1e-3)
+    adj.forward(y0)
+    assert adj.herm
