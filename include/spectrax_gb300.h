@@ -249,7 +249,8 @@ typedef struct spx_dopri8_stats {
  */
 int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* opts, spx_dopri8** out);
 int spx_dopri8_destroy(spx_dopri8* s);
-/* Copy y0 (device) in and reset the clock/controller. */
+/* Copy y0 in (device memory or page-locked host memory) and reset the
+ * clock/controller; stream-ordered, the host does not wait. */
 int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream);
 /* Replay up to `max_attempts` step attempts (accepted or rejected); returns
  * after the solve ends or the attempts are used.  *status_out gets the status. */

@@ -594,6 +594,15 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_d8_stage_gen(D8Args a, int s
   }
 }
 
+// Copy the current state (Y[st->cur], chosen on the device) to dst: device
+// memory or page-locked host memory (written through the mapped address), so
+// reading the state out needs no host round trip for the buffer index.
+__global__ void __launch_bounds__(NTHREADS) k_d8_export(D8Args a, double2* __restrict__ dst) {
+  const double2* Y = pick(a.Y, a.st->cur);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.len; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = Y[i];
+}
+
 // Exact Hermitian test of a fused-1D1V state (odd Nx): every line of Nx entries
 // (Hermite planes and field components) must satisfy y(N-1-c) == conj y(c).
 // Any violation clears *flag (set to 1 by the caller).
@@ -693,6 +702,7 @@ struct spx_dopri8 {
   std::vector<double> ts;
   bool herm_allowed = false;  // requested, fused 1D1V path, odd Nx, antisymmetric k table
   bool persistent = false;    // attempts run by k_d8_persist (one cooperative launch per replay)
+  D8Dev* d_init = nullptr;    // the reset record, in device memory (reset copies it without a host wait)
 };
 
 static bool g_d8_consts = false;
@@ -859,6 +869,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   const size_t vec = al((size_t)len * sizeof(double2));
   size_t off = 0;
   const size_t o_st = off; off += al(sizeof(D8Dev));
+  const size_t o_init = off; off += al(sizeof(D8Dev));
   const size_t o_part = off; off += al(2 * (size_t)nparts * sizeof(double));
   const size_t o_ts = off; off += al(std::max(1, o->nsave) * sizeof(double));
   const size_t o_m = off; off += al(SPX_MAX_SPECIES * sizeof(double));
@@ -875,6 +886,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   A.plan = plan->d_plan;
   A.tab = plan->d_tab;
   A.st = reinterpret_cast<D8Dev*>(b + o_st);
+  s->d_init = reinterpret_cast<D8Dev*>(b + o_init);
   A.part = reinterpret_cast<double*>(b + o_part);
   A.save_ts = reinterpret_cast<const double*>(b + o_ts);
   A.masses = reinterpret_cast<const double*>(b + o_m);
@@ -908,6 +920,18 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
       if (!(plan->tab[P.ax[1].kofs + c].x == -plan->tab[P.ax[1].kofs + N - 1 - c].x)) anti = false;
     s->herm_allowed = anti;
   }
+  {
+    // the reset record: a save time at (or before) t0 is taken from y0
+    D8Dev R = I;
+    R.cur = 0;
+    int hi = 0;
+    while (hi < s->nsave && s->ts[hi] <= R.t0) ++hi;
+    if (hi > 0) { R.save_pending = 1; R.save_lo = 0; R.save_hi = hi; R.isave = hi; }
+    if (R.t0 >= R.t1) R.status = SPX_ST_DONE;
+    R.herm = s->herm_allowed ? 1 : 0;
+    e = cudaMemcpy(s->d_init, &R, sizeof(R), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "dopri8 reset record"); }
+  }
   e = cudaMallocHost(&s->h_status, sizeof(int) * 4);
   if (e == cudaSuccess && o->nsave > 0)
     e = cudaMemcpy(b + o_ts, o->save_ts, o->nsave * sizeof(double), cudaMemcpyHostToDevice);
@@ -940,16 +964,12 @@ int spx_dopri8_destroy(spx_dopri8* s) { return d8_free(s); }
 int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
   if (!s || !y0) { set_error("spx_dopri8_reset: null argument"); return SPX_E_ARG; }
   cudaStream_t st = (cudaStream_t)stream;
-  D8Dev I = s->init;
-  I.cur = 0;
-  // a save time at (or before) t0 is taken from y0
   int hi = 0;
-  while (hi < s->nsave && s->ts[hi] <= I.t0) ++hi;
-  if (hi > 0) { I.save_pending = 1; I.save_lo = 0; I.save_hi = hi; I.isave = hi; }
-  if (I.t0 >= I.t1) I.status = SPX_ST_DONE;
-  I.herm = s->herm_allowed ? 1 : 0;
-  SPX_CUDA(cudaMemcpyAsync(s->args.st, &I, sizeof(I), cudaMemcpyHostToDevice, st));
-  SPX_CUDA(cudaMemcpyAsync(s->args.Y[0], y0, (size_t)s->args.len * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  while (hi < s->nsave && s->ts[hi] <= s->init.t0) ++hi;
+  // everything stream-ordered, no host wait: the reset record lives on the device,
+  // y0 may be device memory or page-locked host memory
+  SPX_CUDA(cudaMemcpyAsync(s->args.st, s->d_init, sizeof(D8Dev), cudaMemcpyDeviceToDevice, st));
+  SPX_CUDA(cudaMemcpyAsync(s->args.Y[0], y0, (size_t)s->args.len * sizeof(double2), cudaMemcpyDefault, st));
   SPX_CUDA(cudaMemsetAsync(s->args.done, 0, sizeof(unsigned int) * (size_t)s->grid_stage, st));
   if (s->herm_allowed) {
     const int N = s->plan->host.ax[1].n;
@@ -959,8 +979,6 @@ int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
   }
   if (hi > 0) k_d8_save<<<s->plan->nsm, NTHREADS, 0, st>>>(s->args);
   SPX_CUDA(cudaGetLastError());
-  // the init struct lives on the host stack: make the copy complete before returning
-  SPX_CUDA(cudaStreamSynchronize(st));
   return SPX_OK;
 }
 
@@ -1038,11 +1056,27 @@ int spx_dopri8_copy(spx_dopri8* s, int32_t what, void* dst, size_t bytes, void* 
   const void* src = nullptr;
   size_t want = 0;
   if (what == 0) {
-    D8Dev d;
-    SPX_CUDA(cudaMemcpyAsync(&d, s->args.st, sizeof(d), cudaMemcpyDeviceToHost, st));
-    SPX_CUDA(cudaStreamSynchronize(st));
-    src = s->args.Y[d.cur];
-    want = vec;
+    if (bytes != vec) { set_error("spx_dopri8_copy: size mismatch"); return SPX_E_ARG; }
+    // the address this device dereferences for dst (device memory, or page-locked
+    // host memory mapped into the device's address space); NULL otherwise
+    cudaPointerAttributes pa;
+    void* target = nullptr;
+    if (cudaPointerGetAttributes(&pa, dst) == cudaSuccess &&
+        (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeManaged))
+      target = pa.devicePointer;
+    cudaGetLastError();
+    if (!target) {
+      // pageable host memory: read the buffer index first, then copy
+      D8Dev d;
+      SPX_CUDA(cudaMemcpyAsync(&d, s->args.st, sizeof(d), cudaMemcpyDeviceToHost, st));
+      SPX_CUDA(cudaStreamSynchronize(st));
+      SPX_CUDA(cudaMemcpyAsync(dst, s->args.Y[d.cur], vec, cudaMemcpyDefault, st));
+      return SPX_OK;
+    }
+    const int grid = (int)std::min<long long>(4LL * s->plan->nsm, (s->args.len + NTHREADS - 1) / NTHREADS);
+    k_d8_export<<<grid, NTHREADS, 0, st>>>(s->args, static_cast<double2*>(target));
+    SPX_CUDA(cudaGetLastError());
+    return SPX_OK;
   } else if (what == 1) {
     if (!s->args.saved) { set_error("spx_dopri8_copy: states were not kept (save_states = 0)"); return SPX_E_ARG; }
     src = s->args.saved;

@@ -63,9 +63,18 @@ class Dopri8Solver:
         self.handle = h
 
     def reset(self, y0, stream=None):
-        y0 = torch.as_tensor(y0).to(self.plan.device, torch.complex128).contiguous()
-        self.plan.check_state(y0, "y0")
-        _lib.check(_lib.lib().spx_dopri8_reset(self.handle, C.c_void_p(y0.data_ptr()), _stream_ptr(stream)),
+        """Start a new solve from y0 (stream-ordered; a page-locked complex128 host
+        tensor is copied straight from host memory and must not change until the
+        stream has consumed it)."""
+        t = torch.as_tensor(y0)
+        if t.device.type == "cpu" and t.is_pinned() and t.dtype == torch.complex128 and t.is_contiguous():
+            if t.numel() != self.plan.state_len:
+                raise ValueError(f"y0 must have {self.plan.state_len} entries")
+        else:
+            t = t.to(self.plan.device, torch.complex128).contiguous()
+            self.plan.check_state(t, "y0")
+        self._y0 = t                     # alive until the copy has run (next reset at the earliest)
+        _lib.check(_lib.lib().spx_dopri8_reset(self.handle, C.c_void_p(t.data_ptr()), _stream_ptr(stream)),
                    "spx_dopri8_reset")
         return self
 

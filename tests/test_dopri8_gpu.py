@@ -135,3 +135,33 @@ def test_host_driven_dopri8_matches_oracle():
     assert st["status_name"] == "DONE"
     assert st["accepted"] == ref["accepted"] and st["rejected"] == ref["rejected"], (st, ref)
     assert rel_err(ys.cpu().numpy(), ref["ys"]) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(17, 1, 1, 12, 1, 1, 2), (6, 5, 1, 2, 2, 2, 2)], ids=["1v", "general"])
+def test_reset_and_export_through_host_memory(shape):
+    # reset from page-locked host memory, from a device tensor and from a NumPy
+    # array give the same solve; the state read back into page-locked, pageable
+    # and device memory is the same (no host round trip for the buffer index)
+    import torch
+    from spectrax_gb300 import dopri8, vector_field
+    p = _params(shape)
+    y0 = _y0(shape)
+    plan = vector_field.plan_for_params(p, "divide")
+    outs = []
+    for src in ("pinned", "device", "numpy"):
+        s = dopri8.Dopri8Solver(plan, 0.0, 1e9, 0.01, adaptive=True, max_steps=1 << 30, save_states=False)
+        y = {"pinned": torch.from_numpy(y0).pin_memory(), "device": torch.from_numpy(y0).cuda(), "numpy": y0}[src]
+        for _ in range(2):                          # a second reset starts over
+            s.reset(y)
+            s.enqueue(5)
+        pinned = torch.empty(plan.state_len, dtype=torch.complex128).pin_memory()
+        pageable = torch.empty(plan.state_len, dtype=torch.complex128)
+        s._copy(0, pinned)
+        s._copy(0, pageable)
+        dev = s.state()
+        torch.cuda.synchronize()
+        assert torch.equal(pinned, pageable) and torch.equal(pinned, dev.cpu())
+        outs.append(pinned.numpy().copy())
+        assert s.stats()["accepted"] + s.stats()["rejected"] == 5
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
