@@ -122,6 +122,14 @@ int spx_jvp_lin(const spx_plan* plan, const void* lin, const void* v, void* Jv, 
                 size_t ws_bytes, void* stream);
 
 /*
+ * out[n * nv + j] = H_n(xi[j]) / (sqrt(pi) 2^(n/2) sqrt(n!)) for n < N: the
+ * per-axis Hermite basis of the f(x, v) reconstruction in
+ * spectrax/_inverse_transform.py:79-84 (xi and out device arrays), by the
+ * recurrence of the normalised Hermite functions (finite for every n).
+ */
+int spx_hermite_basis(int32_t N, const double* xi, int64_t nv, double* out, void* stream);
+
+/*
  * Krylov-basis kernels of the implicit midpoint's restarted GMRES (the reference
  * uses jax.scipy's GMRES, spectrax/midpoint_solver.py:37-98).  V: device basis of
  * rows of n complex128 entries (row i at V + i*n); only rows i < k are read.

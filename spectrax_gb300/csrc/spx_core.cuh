@@ -308,23 +308,24 @@ __device__ __forceinline__ void stage_odd(double2* __restrict__ in, double2* __r
     // over G lanes (G a power of two, G * rem <= 32) and reduced by shuffles, so
     // that a nearly empty warp does not cost a full task loop.  FP64 issue is
     // per warp instruction, whatever the number of active lanes.
-    // When the whole task list fits the CTA at least twice over, every task is
-    // split over GA lanes instead (one round): the four SM sub-partitions (warp
-    // w runs on sub-partition w % 4) then each carry a shorter loop, rather than
-    // warp 0 carrying full-length loops while the others idle.
+    // Alternatively, when the task list fits the CTA at least twice over, every
+    // task is split over GA lanes (the largest power of two <= 8 that still
+    // fits): a warp issues at most one FP64 instruction per ~68 cycles, so
+    // shorter loops on more warps shorten the phase.  Chosen by measurement
+    // over the tile shapes the autotuner tries.
     const int nfw = ntask >> 5;
     const int rem = ntask - (nfw << 5);
-    int GA = 1;
-    while (GA < 8 && ntask * GA * 2 <= (int)blockDim.x) GA *= 2;
     int G = 1;
-    if (GA == 1 && rem > 0 && rem <= 16) {
+    if (rem > 0 && rem <= 16) {
       G = 32 / rem;
       while (G & (G - 1)) G &= G - 1;
     }
+    int GA = 1;
+    while (GA < 8 && ntask * GA * 2 <= (int)blockDim.x) GA *= 2;
     const int units = GA > 1 ? (ntask * GA + 31) >> 5 : nfw + (rem > 0 ? 1 : 0);
     const int lane = threadIdx.x & 31;
     for (int u = threadIdx.x >> 5; u < units; u += blockDim.x >> 5) {
-      const bool split = GA == 1 && u == nfw;          // the remainder warp
+      const bool split = GA == 1 && u == nfw;          // the remainder warp (G lanes per task)
       const int Gu = GA > 1 ? GA : (split ? G : 1);
       const int t = GA > 1 ? ((u << 5) + lane) / GA : (split ? (nfw << 5) + lane / Gu : (u << 5) + lane);
       const int g = GA > 1 ? lane % GA : (split ? lane % Gu : 0);

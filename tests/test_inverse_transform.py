@@ -1,0 +1,59 @@
+"""f(x, v) reconstruction (spectrax/_inverse_transform.py) against the oracle restatement."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import inverse_transform as oinv
+
+
+def _normalised(N, x):
+    H = oinv.hermite_basis(N, x)
+    norm = np.array([math.sqrt(math.pi) * 2.0 ** (n / 2.0) * math.sqrt(math.factorial(n)) for n in range(N)])
+    return H / norm.reshape((-1,) + (1,) * np.ndim(x))
+
+
+def test_oracle_basis_is_orthonormal_under_the_gaussian():
+    # Gauss-Hermite quadrature: int e^{-x^2} b_n b_m dx = delta_nm / sqrt(pi)
+    x, w = np.polynomial.hermite.hermgauss(40)
+    b = _normalised(16, x)
+    G = (b * w) @ b.T
+    np.testing.assert_allclose(G, np.eye(16) / math.sqrt(math.pi), atol=1e-13)
+
+
+@pytest.mark.gpu
+def test_basis_kernel_matches_oracle():
+    from spectrax_gb300.inverse_transform import hermite_basis
+    x = np.linspace(-5.0, 5.0, 301)
+    ref = _normalised(48, x)
+    got = hermite_basis(48, x).cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.gpu
+def test_basis_kernel_is_finite_where_the_polynomials_overflow():
+    from spectrax_gb300.inverse_transform import hermite_basis
+    x = np.linspace(-30.0, 30.0, 61)
+    got = hermite_basis(400, x).cpu().numpy()
+    assert np.all(np.isfinite(got))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("Nn,Nm,Np,Ny,Nx,Nz,V", [
+    (16, 1, 1, 1, 9, 1, (1, 20, 1)),
+    (3, 3, 3, 4, 5, 1, (3, 4, 2)),
+    (2, 3, 2, 1, 6, 3, (2, 2, 3)),
+])
+def test_inverse_transform_matches_oracle(Nn, Nm, Np, Ny, Nx, Nz, V):
+    from spectrax_gb300.inverse_transform import inverse_HF_transform
+    rng = np.random.default_rng(Nn * 100 + Nx)
+    Ck = rng.standard_normal((2, Nn * Nm * Np, Ny, Nx, Nz)) + 1j * rng.standard_normal((2, Nn * Nm * Np, Ny, Nx, Nz))
+    vy = np.linspace(-2.0, 2.0, V[0])
+    vx = np.linspace(-3.0, 3.0, V[1])
+    vz = np.linspace(-1.5, 1.5, V[2])
+    xi_y, xi_x, xi_z = np.meshgrid(vy, vx, vz, indexing="ij")
+    ref = oinv.inverse_HF_transform(Ck, Nn, Nm, Np, xi_x, xi_y, xi_z)
+    got = inverse_HF_transform(Ck, Nn, Nm, Np, xi_x, xi_y, xi_z).cpu().numpy()
+    assert got.shape == ref.shape == (2, Ny, Nx, Nz) + V
+    assert rel_err(got, ref) < 1e-12
