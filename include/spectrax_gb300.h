@@ -130,6 +130,21 @@ int spx_jvp_lin(const spx_plan* plan, const void* lin, const void* v, void* Jv, 
 int spx_hermite_basis(int32_t N, const double* xi, int64_t nv, double* out, void* stream);
 
 /*
+ * Initial Hermite-Fourier coefficients of drifting Maxwellians on the device
+ * (spectrax/_initialize_maxwellian.py:15-66): for every species s and Hermite
+ * mode (n, m, p) of the plan, fftshift(fftn(C, norm="forward")) over (y, x, z) of
+ *   C(x) = sqrt(2^(n+m+p) / (n! m! p!)) / (a_x^(n+1) a_y^(m+1) a_z^(p+1))
+ *          (U_x - u_x)^n (U_y - u_y)^m (U_z - u_z)^p,
+ * with a, u the plan's alpha_s, u_s and Us (device, Ns x 3 x Ny x Nx x Nz
+ * doubles) the sampled bulk velocities; then the same transform of `nreal`
+ * extra real planes xreal (device, nreal x plane; e.g. the fields E, B).
+ * out (device) gets Ns*Nn*Nm*Np + nreal planes of complex128 in the state's
+ * order.  The plan must keep every Fourier mode (cut >= N/2 on every axis).
+ */
+int spx_maxwellian(const spx_plan* plan, const double* Us, const double* xreal, int32_t nreal, void* out,
+                   void* stream);
+
+/*
  * Krylov-basis kernels of the implicit midpoint's restarted GMRES (the reference
  * uses jax.scipy's GMRES, spectrax/midpoint_solver.py:37-98).  V: device basis of
  * rows of n complex128 entries (row i at V + i*n); only rows i < k are read.

@@ -4,7 +4,9 @@ and the 2D3V Orszag-Tang-like initial state (Examples/2D_Orszag_Tang.py:40-77).
 C_nmp(x) = sqrt(2^(n+m+p) / (n! m! p!)) / (a_x^(n+1) a_y^(m+1) a_z^(p+1))
            * (U_x - u_x)^n (U_y - u_y)^m (U_z - u_z)^p
 sampled on the real-space grid, then fftn(norm="forward") and fftshift over
-(y, x, z).  Host-side (NumPy): it runs once per simulation.
+(y, x, z).  `compute_C_nmp` is the host (NumPy) version; `compute_C_nmp_device`
+runs the same on the GPU (`spx_maxwellian`: one CTA per mode plane, samples
+formed in shared memory and transformed in place) for large initial states.
 """
 from __future__ import annotations
 
@@ -31,6 +33,39 @@ def compute_C_nmp(Us_grid, alpha_s, u_s, Nn, Nm, Np, Ns):
          * (Ux - ux) ** n * (Uy - uy) ** m * (Uz - uz) ** p)
     ax3 = (-3, -2, -1)
     return np.fft.fftshift(np.fft.fftn(C, axes=ax3, norm="forward"), axes=ax3)
+
+
+def compute_C_nmp_device(Us_grid, alpha_s, u_s, Nn, Nm, Np, Ns, extra_real=None, device=None):
+    """The GPU version of compute_C_nmp: Us_grid (Ns, 3, Ny, Nx, Nz) -> Ck (Ns, Np, Nm,
+    Nn, Ny, Nx, Nz) complex128 on the device; `extra_real` (k, Ny, Nx, Nz) real planes
+    are transformed the same way and returned second (else None)."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib
+    from .params import make_problem
+    from .vector_field import _stream_ptr, get_plan
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    Us = torch.as_tensor(np.asarray(Us_grid, np.float64)).to(dev).contiguous()
+    _, _, Ny, Nx, Nz = Us.shape
+    pb = make_problem(Nx, Ny, Nz, Nn, Nm, Np, Ns, [-1.0] * Ns, 0.0, 0.0, [1.0] * Ns, alpha_s, u_s,
+                      1.0, 1.0, 1.0)
+    pb.cut_x, pb.cut_y, pb.cut_z = Nx, Ny, Nz           # keep every mode: no 2/3 mask here
+    plan = get_plan(pb, dev.index)
+    X = None
+    nreal = 0
+    if extra_real is not None:
+        X = torch.as_tensor(np.asarray(extra_real, np.float64)).to(dev).contiguous()
+        nreal = X.shape[0]
+    plane = Nx * Ny * Nz
+    out = torch.empty((Ns * Nn * Nm * Np + nreal) * plane, dtype=torch.complex128, device=dev)
+    _lib.check(_lib.lib().spx_maxwellian(plan.handle, C.c_void_p(Us.data_ptr()),
+                                         C.c_void_p(X.data_ptr()) if X is not None else None, nreal,
+                                         C.c_void_p(out.data_ptr()), _stream_ptr()), "spx_maxwellian")
+    nc = Ns * Nn * Nm * Np * plane
+    Ck = out[:nc].reshape(Ns, Np, Nm, Nn, Ny, Nx, Nz)
+    return Ck, (out[nc:].reshape(nreal, Ny, Nx, Nz) if X is not None else None)
 
 
 def orszag_tang_state(Nx=64, Ny=64, Nz=1, Nn=8, Nm=8, Np=8, L=50.0, alpha_e=0.25, mi_me=25.0,

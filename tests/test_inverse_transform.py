@@ -57,3 +57,22 @@ def test_inverse_transform_matches_oracle(Nn, Nm, Np, Ny, Nx, Nz, V):
     got = inverse_HF_transform(Ck, Nn, Nm, Np, xi_x, xi_y, xi_z).cpu().numpy()
     assert got.shape == ref.shape == (2, Ny, Nx, Nz) + V
     assert rel_err(got, ref) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("Ns,Nn,Nm,Np,Ny,Nx,Nz", [(2, 8, 1, 1, 1, 33, 1), (2, 3, 3, 3, 8, 8, 1), (1, 2, 2, 3, 4, 5, 3)])
+def test_device_maxwellian_matches_host(Ns, Nn, Nm, Np, Ny, Nx, Nz):
+    # spectrax/_initialize_maxwellian.py on the GPU against the NumPy version,
+    # plus the same transform of extra real planes (the fields)
+    from spectrax_gb300.maxwellian import compute_C_nmp, compute_C_nmp_device
+    rng = np.random.default_rng(Nx * 7 + Nn)
+    Us = 0.3 * rng.standard_normal((Ns, 3, Ny, Nx, Nz))
+    alpha = rng.uniform(0.3, 1.5, 3 * Ns)
+    u = rng.uniform(-0.2, 0.2, 3 * Ns)
+    ref = compute_C_nmp(Us, alpha, u, Nn, Nm, Np, Ns)
+    F = rng.standard_normal((6, Ny, Nx, Nz))
+    got, Fk = compute_C_nmp_device(Us, alpha, u, Nn, Nm, Np, Ns, extra_real=F)
+    assert tuple(got.shape) == ref.shape
+    assert rel_err(got.cpu().numpy(), ref) < 1e-13
+    Fref = np.fft.fftshift(np.fft.fftn(F, axes=(-3, -2, -1), norm="forward"), axes=(-3, -2, -1))
+    assert rel_err(Fk.cpu().numpy(), Fref) < 1e-13
