@@ -549,7 +549,10 @@ def run_ours(args):
                      "kernel": "k_d8_stage_1v (duration = step time / 13)"},
         "fp64": {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
                  "frac": achieved_tf / fp64_peak, "peak_source": "live FMA probe (spx_probe_fp64)",
-                 "note": "the binding ceiling of this path on GB300"},
+                 "note": "FP64 work of the complex-transform formulation of the step (pruned transforms, "
+                         "products, streaming, stage combinations) per unit time; the packed real transforms "
+                         "used for this exactly Hermitian state execute fewer instructions (ncu: 6.7 M FP64 "
+                         "instructions per stage launch). FP64 issue is the binding ceiling of this path on GB300"},
         "clocks": clk.summary(),
     }
     if world == 1:
