@@ -87,3 +87,14 @@ def test_fits_on_synthetic_signals():
     E2 = 1e-8 * np.exp(2 * 0.2 * t)
     assert abs(fits.growth_rate(t, E2, 300) - 0.2) < 1e-10
     assert abs(fits.window_slope(t, E2, 10, 40) - 0.4) < 1e-10
+
+
+def test_physics_curve_fixture():
+    # the copied reference curves: damping at k = 0.5 (the Landau workload) and
+    # a positive two-stream growth rate somewhere on the curve
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "physics_curves.npz"))
+    assert d["damping_k"].shape == d["damping_rate"].shape == (200,)
+    g = float(np.interp(0.5, d["damping_k"], d["damping_rate"]))
+    assert -0.16 < g < -0.15
+    assert np.max(d["growth_rate"]) > 0

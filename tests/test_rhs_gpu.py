@@ -122,3 +122,30 @@ def test_rhs_rejects_bad_inputs():
         plan.rhs(torch.zeros(plan.state_len + 1, dtype=torch.complex128, device="cuda"))
     with pytest.raises(ValueError):
         sg.make_problem(300, 1, 1, 2, 1, 1, 1, [-1], 1, 0, [1], [1, 1, 1], [0, 0, 0], 1, 1, 1)
+
+
+@pytest.mark.gpu
+def test_oversized_planes_are_refused_not_launched():
+    # a general-path plane whose two shared-memory buffers exceed a CTA's
+    # shared memory is refused at plan creation (SPX_E_UNSUPPORTED), before
+    # any launch
+    import spectrax_gb300 as sg
+    from spectrax_gb300 import SpectraxError, vector_field
+    pb = sg.make_problem(64, 64, 8, 2, 2, 1, 1, [-1], 1, 0, [1], [1, 1, 1], [0, 0, 0], 1, 1, 1)
+    with pytest.raises(SpectraxError):
+        vector_field.get_plan(pb)
+
+
+@pytest.mark.gpu
+def test_maxwellian_builder_refuses_a_masked_plan():
+    import ctypes as C
+    import torch
+    import spectrax_gb300 as sg
+    from spectrax_gb300 import _lib, vector_field
+    pb = sg.make_problem(9, 1, 1, 3, 1, 1, 1, [-1], 1, 0, [1], [1, 1, 1], [0, 0, 0], 1, 1, 1)   # 2/3 mask on
+    plan = vector_field.get_plan(pb)
+    Us = torch.zeros(3 * 9, dtype=torch.float64, device="cuda")
+    out = torch.empty(3 * 9, dtype=torch.complex128, device="cuda")
+    rc = _lib.lib().spx_maxwellian(plan.handle, C.c_void_p(Us.data_ptr()), None, 0, C.c_void_p(out.data_ptr()),
+                                   None)
+    assert rc == _lib.SPX_E_ARG
