@@ -7,10 +7,10 @@
 // with one re-orthogonalisation pass:
 //     h = V[:k]^H w;  w -= V[:k]^T h;  h2 = V[:k]^H w;  w -= V[:k]^T h2
 // and the host receives h + h2 and ||w|| in one copy.  Only the k rows built so
-// far are read (no work on the unused rows of the basis), every pass streams
-// the rows once, and the block partial sums are reduced in a fixed order, so
-// results do not depend on scheduling.  The kernels are HBM-bound: one pass
-// moves k*n*16 bytes (plus w).
+// far are read (no work on the unused rows of the basis), the middle update and
+// projection share one pass (three streaming passes in all for k <= 32), and
+// the block partial sums are reduced in a fixed order, so results do not depend
+// on scheduling.  The kernels are HBM-bound: one pass moves k*n*16 bytes (plus w).
 #include <algorithm>
 #include <cuda_runtime.h>
 
@@ -72,13 +72,21 @@ __global__ void __launch_bounds__(NTHREADS) k_kry_dots(const double2* __restrict
   }
 }
 
-// out[i] = sum_b part[b*SPX_KRYLOV_MAX_ROWS + i] in block order, i < k
-__global__ void k_kry_reduce(const double2* __restrict__ part, int nb, int k, double2* __restrict__ out) {
-  const int i = threadIdx.x;
-  if (i >= k) return;
-  double2 s = make_double2(0.0, 0.0);
-  for (int b = 0; b < nb; ++b) s = cadd(s, part[(size_t)b * SPX_KRYLOV_MAX_ROWS + i]);
-  out[i] = s;
+// out[i] = sum_b part[b*SPX_KRYLOV_MAX_ROWS + i], i < k: warp i sums its column, lane
+// l the blocks b = l, l + 32, ... in order, then a fixed shuffle tree (deterministic)
+constexpr int KRY_RED_THREADS = 1024;
+__global__ void __launch_bounds__(KRY_RED_THREADS) k_kry_reduce(const double2* __restrict__ part, int nb, int k,
+                                                                double2* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  for (int i = threadIdx.x >> 5; i < k; i += blockDim.x >> 5) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int b = lane; b < nb; b += 32) s = cadd(s, part[(size_t)b * SPX_KRYLOV_MAX_ROWS + i]);
+    for (int off = 16; off > 0; off >>= 1) {
+      s.x += __shfl_down_sync(0xffffffffu, s.x, off);
+      s.y += __shfl_down_sync(0xffffffffu, s.y, off);
+    }
+    if (lane == 0) out[i] = s;
+  }
 }
 
 // x[e] += sign * sum_{i<k} c[i] V_i[e]; npart[b] = block b's sum of |x_new|^2 when npart != nullptr
@@ -116,15 +124,80 @@ __global__ void __launch_bounds__(NTHREADS) k_kry_update(const double2* __restri
   }
 }
 
-// out[i] = h[i] + h2[i] (i < k), out[k] = (||w||, 0)
+// The middle two passes of CGS2 in one: x[e] -= sum_{i<k} c[i] V_i[e], then
+// part[b*SPX_KRYLOV_MAX_ROWS + i] = block b's sum of conj(V_i[e]) x_new[e].  Each
+// thread re-reads its own rows right after the update (L1), so the rows stream
+// from memory once for both.  k <= 32 (four unrolled groups of eight rows).
+__global__ void __launch_bounds__(NTHREADS) k_kry_update_dots(const double2* __restrict__ V, long long n, int k,
+                                                              const double2* __restrict__ c,
+                                                              double2* __restrict__ x, double2* __restrict__ part) {
+  __shared__ double2 sc[32];
+  __shared__ double2 red[NTHREADS / 32][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x < 32) sc[threadIdx.x] = threadIdx.x < k ? cscale(-1.0, c[threadIdx.x]) : make_double2(0.0, 0.0);
+  __syncthreads();
+  double2 acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) acc[i] = make_double2(0.0, 0.0);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += stride) {
+    double2 a = x[e];
+#pragma unroll
+    for (int g0 = 0; g0 < 32; g0 += KRY_GROUP) {
+      if (g0 < k) {
+        double2 v[KRY_GROUP];
+#pragma unroll
+        for (int r = 0; r < KRY_GROUP; ++r)
+          v[r] = (g0 + r < k) ? V[(size_t)(g0 + r) * n + e] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int r = 0; r < KRY_GROUP; ++r)
+          if (g0 + r < k) a = cfma(v[r], sc[g0 + r], a);
+      }
+    }
+    x[e] = a;
+#pragma unroll
+    for (int g0 = 0; g0 < 32; g0 += KRY_GROUP) {
+      if (g0 < k) {
+#pragma unroll
+        for (int r = 0; r < KRY_GROUP; ++r) {
+          if (g0 + r < k) {
+            const double2 v = __ldcs(V + (size_t)(g0 + r) * n + e);
+            acc[g0 + r].x = fma(v.x, a.x, fma(v.y, a.y, acc[g0 + r].x));
+            acc[g0 + r].y = fma(v.x, a.y, fma(-v.y, a.x, acc[g0 + r].y));
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    if (i < k) {
+      for (int off = 16; off > 0; off >>= 1) {
+        acc[i].x += __shfl_down_sync(0xffffffffu, acc[i].x, off);
+        acc[i].y += __shfl_down_sync(0xffffffffu, acc[i].y, off);
+      }
+      if (lane == 0) red[wid][i] = acc[i];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double2 sum = make_double2(0.0, 0.0);
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum = cadd(sum, red[q][threadIdx.x]);
+    part[(size_t)blockIdx.x * SPX_KRYLOV_MAX_ROWS + threadIdx.x] = sum;
+  }
+}
+
+// out[i] = h[i] + h2[i] (i < k), out[k] = (||w||, 0); warp 0 sums the norm
+// partials (lane l: b = l, l + 32, ... in order, then a fixed shuffle tree)
 __global__ void k_kry_finish(const double2* __restrict__ h, const double2* __restrict__ h2,
                              const double* __restrict__ npart, int nb, int k, double2* __restrict__ out) {
   const int i = threadIdx.x;
   if (i < k) out[i] = cadd(h[i], h2[i]);
-  if (i == 0) {
+  if (i < 32) {
     double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += npart[b];
-    out[k] = make_double2(sqrt(s), 0.0);
+    for (int b = i; b < nb; b += 32) s += npart[b];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (i == 0) out[k] = make_double2(sqrt(s), 0.0);
   }
 }
 
@@ -157,10 +230,14 @@ int spx_krylov_cgs2(const void* V, int64_t n, int32_t k, void* w, void* out, voi
   double2* h2 = h + SPX_KRYLOV_MAX_ROWS;
   double* npart = reinterpret_cast<double*>(h2 + SPX_KRYLOV_MAX_ROWS);
   k_kry_dots<<<nb, NTHREADS, 0, st>>>(Vp, n, k, wp, part);
-  k_kry_reduce<<<1, SPX_KRYLOV_MAX_ROWS, 0, st>>>(part, nb, k, h);
-  k_kry_update<<<nb, NTHREADS, 0, st>>>(Vp, n, k, h, -1.0, wp, nullptr);
-  k_kry_dots<<<nb, NTHREADS, 0, st>>>(Vp, n, k, wp, part);
-  k_kry_reduce<<<1, SPX_KRYLOV_MAX_ROWS, 0, st>>>(part, nb, k, h2);
+  k_kry_reduce<<<1, KRY_RED_THREADS, 0, st>>>(part, nb, k, h);
+  if (k <= 32) {
+    k_kry_update_dots<<<nb, NTHREADS, 0, st>>>(Vp, n, k, h, wp, part);
+  } else {
+    k_kry_update<<<nb, NTHREADS, 0, st>>>(Vp, n, k, h, -1.0, wp, nullptr);
+    k_kry_dots<<<nb, NTHREADS, 0, st>>>(Vp, n, k, wp, part);
+  }
+  k_kry_reduce<<<1, KRY_RED_THREADS, 0, st>>>(part, nb, k, h2);
   k_kry_update<<<nb, NTHREADS, 0, st>>>(Vp, n, k, h2, -1.0, wp, npart);
   k_kry_finish<<<1, SPX_KRYLOV_MAX_ROWS, 0, st>>>(h, h2, npart, nb, k, static_cast<double2*>(out));
   SPX_CUDA(cudaGetLastError());
