@@ -111,9 +111,10 @@ int spx_jvp(const spx_plan* plan, const void* y, const void* v, void* Jv, void* 
  * (spectrax/midpoint_solver.py:75: linearise once per Newton iteration, then one
  * product per GMRES iteration).  spx_linearize stores in `lin`
  * (spx_linearize_bytes() bytes, 16-byte aligned) what J(y) v needs from y: the
- * real-space Hermite planes and field combinations of y on the general layout
- * (saving one inverse transform per plane in every later product), a copy of y
- * on the 1D1V layout.  `lin` no longer refers to y.  spx_jvp_lin then returns
+ * real-space Hermite planes and field combinations of y and the six bracket sums
+ * of every plane on the general layout (saving one inverse transform per plane
+ * and half of the bracket arithmetic in every later product), a copy of y on
+ * the 1D1V layout.  `lin` no longer refers to y.  spx_jvp_lin then returns
  * J(y) v bit for bit as spx_jvp(y, v) would; `ws` as for spx_jvp.
  */
 size_t spx_linearize_bytes(const spx_plan* plan);

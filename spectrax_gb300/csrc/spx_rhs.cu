@@ -345,7 +345,42 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_jvp_nl(const DevPlan* __rest
   const double2* Gy = wy + (size_t)nplanes * pl;
   const double2* Cv = wv;
   const double2* Gv = wv + (size_t)nplanes * pl;
-  general_nl_plane_t<true>(P, stab, v, Cv, Gy, Cy, Gv, blockIdx.x, sA, sB, epi);
+  general_nl_plane_t<1>(P, stab, v, Cv, Gy, Cy, Gv, blockIdx.x, sA, sB, epi);
+}
+
+// Linearised JVP, pass 2: Gy = y's real-space field combinations, Sy = y's
+// bracket sums (6 planes per Hermite plane), wv = v's real-space planes and fields.
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_jvp_nl_lin(const DevPlan* __restrict__ gP,
+                                                              const double2* __restrict__ gtab,
+                                                              const double2* __restrict__ v,
+                                                              const double2* __restrict__ Gy,
+                                                              const double2* __restrict__ Sy,
+                                                              const double2* __restrict__ wv,
+                                                              double2* __restrict__ out) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  EpiStore epi{out};
+  const int nplanes = P.pb.Ns * P.nh;
+  if ((int)blockIdx.x == nplanes) {
+    maxwell_range(P, stab, v, 0, P.plane, epi);
+    return;
+  }
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.pplane;
+  const double2* Gv = wv + (size_t)nplanes * P.plane;
+  general_nl_plane_t<2>(P, stab, v, wv, Gy, Sy, Gv, blockIdx.x, sA, sB, epi);
+}
+
+// The bracket sums of every Hermite plane of y (real-space planes R) into S.
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_lin_sums(const DevPlan* __restrict__ gP,
+                                                            const double2* __restrict__ R,
+                                                            double2* __restrict__ S) {
+  __shared__ DevPlan P;
+  if (threadIdx.x == 0) P = *gP;
+  __syncthreads();
+  lin_bracket_sums(P, R, blockIdx.x, S + (size_t)blockIdx.x * 6 * P.plane);
 }
 
 static bool g_attr_done = false;
@@ -380,6 +415,7 @@ static int set_attrs() {
   if ((rc = allow_smem(k_vjp1v_fields, optin)) != SPX_OK) return rc;
   if ((rc = allow_smem(k_jvp_real, optin)) != SPX_OK) return rc;
   if ((rc = allow_smem(k_jvp_nl, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_jvp_nl_lin, optin)) != SPX_OK) return rc;
   g_attr_done = true;
   return SPX_OK;
 }
@@ -539,8 +575,10 @@ size_t spx_linearize_bytes(const spx_plan* pl) {
   if (!pl) return 0;
   const DevPlan& P = pl->host;
   if (P.path == 0) return (size_t)(P.nc + 6LL * P.plane) * sizeof(double2);
-  const size_t nreal = (size_t)P.pb.Ns * P.nh + 3 * (size_t)P.pb.Ns + 3;
-  return nreal * (size_t)P.plane * sizeof(double2);
+  // real-space planes and field combinations of y, then 6 bracket sums per plane
+  const size_t nplanes = (size_t)P.pb.Ns * P.nh;
+  const size_t nreal = nplanes + 3 * (size_t)P.pb.Ns + 3;
+  return (nreal + 6 * nplanes) * (size_t)P.plane * sizeof(double2);
 }
 
 int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes, void* stream) {
@@ -553,9 +591,11 @@ int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes
     SPX_CUDA(cudaMemcpyAsync(lin, y, spx_linearize_bytes(pl), cudaMemcpyDeviceToDevice, st));
     return SPX_OK;
   }
-  const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
-  k_gen_real<<<nreal, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y),
-                                                      static_cast<double2*>(lin));
+  const int nplanes = P.pb.Ns * P.nh;
+  const int nreal = nplanes + 3 * P.pb.Ns + 3;
+  double2* L = static_cast<double2*>(lin);
+  k_gen_real<<<nreal, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, static_cast<const double2*>(y), L);
+  k_lin_sums<<<nplanes, GEN_THREADS, 0, st>>>(pl->d_plan, L, L + (size_t)nreal * P.plane);
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
 }
@@ -576,7 +616,8 @@ int spx_jvp_lin(const spx_plan* pl, const void* lin, const void* v, void* Jv, vo
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
     double2* w = static_cast<double2*>(ws);
     k_gen_real<<<nreal, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, w);
-    k_jvp_nl<<<nplanes + 1, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, vv, ll, w, out);
+    k_jvp_nl_lin<<<nplanes + 1, GEN_THREADS, pl->smem_gen, st>>>(
+        pl->d_plan, pl->d_tab, vv, ll + (size_t)nplanes * P.plane, ll + (size_t)nreal * P.plane, w, out);
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;

@@ -514,8 +514,11 @@ __device__ __forceinline__ double2 bracket_point(const NlCoef& cf, const double2
 //   JVP: bracket(C_v, G_y) + bracket(C_y, G_v), lin = v
 // RA/GA: real-space Hermite planes and field combinations of the first
 // operand; RB/GB2 of the second (JVP only).
+// MODE 0: RHS; 1: JVP (two brackets); 2: linearised JVP, where RB holds the
+// six precomputed bracket sums of y for this plane (lin_bracket_sums), so the
+// second bracket is six complex products with v's fields GB2.
 // ------------------------------------------------------------------------
-template <bool JVP, class Epi>
+template <int MODE, class Epi>
 __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__ tab,
                                    const double2* __restrict__ lin,
                                    const double2* __restrict__ RA, const double2* __restrict__ GA,
@@ -530,7 +533,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   // per-plane constants (square roots and divisions, ~300 FP64 instructions)
   // once per CTA in shared memory instead of once per thread
   __shared__ NlCoef s_cf;
-  __shared__ double s_lin[10];
+  __shared__ double s_lin[11];
   if (threadIdx.x == 0) {
     s_cf = nl_coef(P, s, n, m, p);
     const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
@@ -542,19 +545,30 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     s_lin[6] = sqrt((p + 1) * rh); s_lin[7] = sqrt(p * rh);
     s_lin[8] = pb.u_s[3 * s] / a0;
     s_lin[9] = pb.u_s[3 * s + 1] / a1;
+    s_lin[10] = pb.u_s[3 * s + 2] / a2;
   }
   __syncthreads();
   const NlCoef cf = s_cf;
   const bool anyx = cf.ix[0] >= 0 || cf.ix[1] >= 0 || cf.ix[2] >= 0;
   const bool anyy = cf.iy[0] >= 0 || cf.iy[1] >= 0 || cf.iy[2] >= 0;
   const bool anyz = cf.iz[0] >= 0 || cf.iz[1] >= 0 || cf.iz[2] >= 0;
-  // RHS: (RA = C_y, GA = G_y).  JVP: RA = C_v, GA = G_y, RB = C_y, GB2 = G_v.
+  // RHS: (RA = C_y, GA = G_y).  JVP: RA = C_v, GA = G_y, RB = C_y (MODE 2: the
+  // bracket sums of y), GB2 = G_v.
   const FieldPlanes FA = field_planes(GA, s, Ns, pl);
   FieldPlanes FB;
-  if (JVP) FB = field_planes(GB2, s, Ns, pl);
+  if (MODE != 0) FB = field_planes(GB2, s, Ns, pl);
+  const double2* Sy = (MODE == 2) ? RB + (size_t)id * 6 * pl : nullptr;
   for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
     double2 acc = bracket_point(cf, RA, FA, pl, pt, anyx, anyy, anyz, make_double2(0.0, 0.0));
-    if (JVP) acc = bracket_point(cf, RB, FB, pl, pt, anyx, anyy, anyz, acc);
+    if (MODE == 1) acc = bracket_point(cf, RB, FB, pl, pt, anyx, anyy, anyz, acc);
+    if (MODE == 2) {
+      if (cf.in_ >= 0) acc = cfma(FB.Gx[pt], Sy[pt], acc);
+      if (cf.im_ >= 0) acc = cfma(FB.Gy[pt], Sy[pl + pt], acc);
+      if (cf.ip_ >= 0) acc = cfma(FB.Gz[pt], Sy[2 * pl + pt], acc);
+      if (anyx) acc = cfma(FB.Bx[pt], Sy[3 * pl + pt], acc);
+      if (anyy) acc = cfma(FB.By[pt], Sy[4 * pl + pt], acc);
+      if (anyz) acc = cfma(FB.Bz[pt], Sy[5 * pl + pt], acc);
+    }
     sA[padded(P, (int)pt)] = acc;
   }
   __syncthreads();
@@ -563,7 +577,7 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
   const double sc = s_lin[0], dcol = s_lin[1];
   const double snp = s_lin[2], snm = s_lin[3], smp = s_lin[4], smm = s_lin[5], spp = s_lin[6], spm = s_lin[7];
-  const double ux = s_lin[8], uy = s_lin[9], uz = pb.u_s[3 * s + 2] / a2;
+  const double ux = s_lin[8], uy = s_lin[9], uz = s_lin[10];
   const double2* Cp = lin + (size_t)id * pl;
   const size_t sn_ = pl, sm_ = (size_t)Nn * pl, sp_ = (size_t)Nn * Nm * pl;
   for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
@@ -617,7 +631,32 @@ __device__ __forceinline__ void general_nl_plane(const DevPlan& P, const double2
                                                  const double2* __restrict__ Creal,
                                                  const double2* __restrict__ GB, int id,
                                                  double2* sA, double2* sB, Epi& epi) {
-  general_nl_plane_t<false>(P, tab, y, Creal, GB, nullptr, nullptr, id, sA, sB, epi);
+  general_nl_plane_t<0>(P, tab, y, Creal, GB, nullptr, nullptr, id, sA, sB, epi);
+}
+
+// The six bracket sums of plane `id` for the real-space planes R of a state y
+// (the part of N(F_v, C_y) that does not depend on v): S_0..2 = g_x C_{n-1},
+// g_y C_{m-1}, g_z C_{p-1}; S_3..5 = the B_x, B_y, B_z neighbour combinations;
+// absent terms are zero.  Written to S (6 planes).
+__device__ inline void lin_bracket_sums(const DevPlan& P, const double2* __restrict__ R, int id,
+                                        double2* __restrict__ S) {
+  const spx_problem& pb = P.pb;
+  const size_t pl = (size_t)P.plane;
+  const int s = id / P.nh, h = id % P.nh;
+  const int n = h % pb.Nn, m = (h / pb.Nn) % pb.Nm, p = h / (pb.Nn * pb.Nm);
+  __shared__ NlCoef s_cf;
+  if (threadIdx.x == 0) s_cf = nl_coef(P, s, n, m, p);
+  __syncthreads();
+  const NlCoef cf = s_cf;
+  const double2 zero = make_double2(0.0, 0.0);
+  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+    S[pt] = cf.in_ >= 0 ? cscale(cf.gx, R[(size_t)cf.in_ * pl + pt]) : zero;
+    S[pl + pt] = cf.im_ >= 0 ? cscale(cf.gy, R[(size_t)cf.im_ * pl + pt]) : zero;
+    S[2 * pl + pt] = cf.ip_ >= 0 ? cscale(cf.gz, R[(size_t)cf.ip_ * pl + pt]) : zero;
+    S[3 * pl + pt] = combo3(R, pl, cf.ix, cf.bx, pt);
+    S[4 * pl + pt] = combo3(R, pl, cf.iy, cf.by, pt);
+    S[5 * pl + pt] = combo3(R, pl, cf.iz, cf.bz, pt);
+  }
 }
 
 // ------------------------------------------------------------------------
