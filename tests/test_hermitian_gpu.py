@@ -106,3 +106,30 @@ def test_even_nx_never_uses_packed_transforms():
     y0 = 1e-2 * (rng.standard_normal((2 * 8 + 6, 32)) + 1j * rng.standard_normal((2 * 8 + 6, 32)))
     s = _solve(p, y0.ravel(), 0.2, 0.05, np.linspace(0.0, 0.2, 2), False, hermitian=True)
     assert not s.stats()["hermitian"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tile,threads", [(6, 256), (3, 128), (3, 256), (0, 0)])
+def test_benchmark_configuration_matches_oracle(tile, threads):
+    # the exact two-stream workload of the benchmark (Nx=129, Nn=256, Ns=3), with
+    # the tile shapes the autotuner chooses between: a few adaptive steps against
+    # the oracle stepper (same tableau, same controller)
+    import os
+    import sys
+    import torch
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    from spectrax_gb300 import dopri8, vector_field
+    p, y0 = bench.two_stream_params(seed=0)
+    ts = np.array([0.0, 0.05, 0.1])
+    ref = od.solve(lambda t, y: orhs.rhs(p, y, "divide"), 0.0, 0.1, y0, 0.02, ts=ts, adaptive=True,
+                   rtol=1e-10, atol=1e-12)
+    plan = vector_field.get_plan(vector_field.problem_from_params(p, "divide"), None, tile, threads)
+    s = dopri8.Dopri8Solver(plan, 0.0, 0.1, 0.02, ts=ts, adaptive=True, rtol=1e-10, atol=1e-12,
+                            masses=[1.0, 1.0, 1836.0])
+    s.reset(torch.from_numpy(y0))
+    assert s.run() == 1
+    info = s.stats()
+    assert info["hermitian"]
+    assert info["accepted"] == ref["accepted"] and info["rejected"] == ref["rejected"], (info, ref)
+    assert rel_err(s.saved_states().cpu().numpy(), ref["ys"]) < 1e-11
