@@ -72,6 +72,7 @@ struct DevPlan {
   const double* coef;
   double ua[SPX_MAX_SPECIES];   // u_x / alpha_x per species
   double iO0;                   // 1 / Omega_c of species 0
+  const void* gen;              // general path: per-plane constants (GenPlane[Ns * nh]), device memory
 };
 
 // Coefficients of Hermite plane n of species s on the fused 1D1V path:

@@ -8,6 +8,7 @@ struct spx_plan {
   spx::DevPlan host;            // host copy of the device header
   std::vector<double2> tab;     // host copy of the table
   std::vector<double> coef;     // fused 1D1V path: coef_1v for every (species, plane)
+  std::vector<unsigned char> gen;   // general path: GenPlane for every (species, plane), as bytes
   spx::DevPlan* d_plan = nullptr;
   double2* d_tab = nullptr;
   void* d_block = nullptr;      // single allocation holding d_plan, d_tab and d_ticket

@@ -135,6 +135,7 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
   for (int sp = 0; sp < p.Ns; ++sp) P.ua[sp] = p.u_s[3 * sp] / p.alpha_s[3 * sp];
   P.iO0 = 1.0 / p.Omega_cs[0];
   pl->coef.clear();
+  pl->gen.clear();
   if (onev) {
     P.path = 0;
     pl->coef.resize((size_t)p.Ns * p.Nn * COEF_1V);
@@ -167,6 +168,12 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
     if (pl->smem_gen > smem_max) {
       set_error("a Fourier plane of this size does not fit in shared memory");
       return SPX_E_UNSUPPORTED;
+    }
+    const int nplanes = p.Ns * P.nh;
+    pl->gen.resize((size_t)nplanes * sizeof(GenPlane));
+    for (int id = 0; id < nplanes; ++id) {
+      const GenPlane g = gen_plane(P, id);
+      std::memcpy(pl->gen.data() + (size_t)id * sizeof(GenPlane), &g, sizeof(GenPlane));
     }
     // real-space planes of y (RHS) and of y and v (JVP)
     const size_t nreal = (size_t)p.Ns * P.nh + 3 * (size_t)p.Ns + 3;
@@ -486,7 +493,8 @@ int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx
   const size_t ngroups = (size_t)pb->Ns * ((pl->host.ntiles + 7) / 8 + 1);
   const size_t ticket_bytes = (256 + 4 * ngroups + 255) / 256 * 256;
   const size_t coef_bytes = (pl->coef.size() * sizeof(double) + 255) / 256 * 256;
-  const size_t bytes = hdr + tab_bytes + ticket_bytes + coef_bytes;
+  const size_t gen_bytes = (pl->gen.size() + 255) / 256 * 256;
+  const size_t bytes = hdr + tab_bytes + ticket_bytes + coef_bytes + gen_bytes;
   cudaError_t e = cudaMalloc(&pl->d_block, bytes);
   if (e != cudaSuccess) { delete pl; return cuda_fail(e, "cudaMalloc(plan)"); }
   pl->d_plan = reinterpret_cast<DevPlan*>(pl->d_block);
@@ -494,9 +502,13 @@ int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx
   pl->d_ticket = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes);
   double* d_coef = reinterpret_cast<double*>(reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes + ticket_bytes);
   pl->host.coef = pl->coef.empty() ? nullptr : d_coef;
+  char* d_gen = reinterpret_cast<char*>(pl->d_block) + hdr + tab_bytes + ticket_bytes + coef_bytes;
+  pl->host.gen = pl->gen.empty() ? nullptr : d_gen;
   e = cudaMemset(pl->d_ticket, 0, ticket_bytes);
   if (e == cudaSuccess && !pl->coef.empty())
     e = cudaMemcpy(d_coef, pl->coef.data(), pl->coef.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !pl->gen.empty())
+    e = cudaMemcpy(d_gen, pl->gen.data(), pl->gen.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(pl->d_plan, &pl->host, sizeof(DevPlan), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !pl->tab.empty())
     e = cudaMemcpy(pl->d_tab, pl->tab.data(), pl->tab.size() * sizeof(double2), cudaMemcpyHostToDevice);

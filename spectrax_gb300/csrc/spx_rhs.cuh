@@ -431,7 +431,7 @@ struct NlCoef {
   int in_, im_, ip_;           // plane ids of C_{n-1}, C_{m-1}, C_{p-1} (-1 when absent)
 };
 
-__device__ __forceinline__ NlCoef nl_coef(const DevPlan& P, int s, int n, int m, int p) {
+__host__ __device__ inline NlCoef nl_coef(const DevPlan& P, int s, int n, int m, int p) {
   const spx_problem& pb = P.pb;
   const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np;
   const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
@@ -466,6 +466,35 @@ __device__ __forceinline__ NlCoef nl_coef(const DevPlan& P, int s, int n, int m,
     if (c.iz[k] < 0) c.bz[k] = 0.0;
   }
   return c;
+}
+
+// General path: every constant of one Hermite plane's bracket and linear terms,
+// built once on the host (one table entry per (species, mode)) so that no CTA
+// spends serial FP64 work on square roots and divisions.
+struct GenPlane {
+  NlCoef cf;
+  // q Omega / N, nu col, sqrt((n+1)/2), sqrt(n/2), sqrt((m+1)/2), sqrt(m/2),
+  // sqrt((p+1)/2), sqrt(p/2), u_x/a_x, u_y/a_y, u_z/a_z
+  double lin[11];
+};
+
+__host__ inline GenPlane gen_plane(const DevPlan& P, int id) {
+  const spx_problem& pb = P.pb;
+  const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np;
+  const int s = id / P.nh, h = id % P.nh;
+  const int n = h % Nn, m = (h / Nn) % Nm, p = h / (Nn * Nm);
+  GenPlane g;
+  g.cf = nl_coef(P, s, n, m, p);
+  const double rh = 0.5;
+  g.lin[0] = pb.qs[s] * pb.Omega_cs[s] / (double)P.plane;
+  g.lin[1] = pb.nu * (colc(Nn, n) + colc(Nm, m) + colc(Np, p));
+  g.lin[2] = sqrt((n + 1) * rh); g.lin[3] = sqrt(n * rh);
+  g.lin[4] = sqrt((m + 1) * rh); g.lin[5] = sqrt(m * rh);
+  g.lin[6] = sqrt((p + 1) * rh); g.lin[7] = sqrt(p * rh);
+  g.lin[8] = pb.u_s[3 * s] / pb.alpha_s[3 * s];
+  g.lin[9] = pb.u_s[3 * s + 1] / pb.alpha_s[3 * s + 1];
+  g.lin[10] = pb.u_s[3 * s + 2] / pb.alpha_s[3 * s + 2];
+  return g;
 }
 
 // sum_k w[k] * R[ids[k]][pt] over the present neighbours
@@ -530,25 +559,10 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np, Ns = pb.Ns;
   const int s = id / P.nh, h = id % P.nh;
   const int n = h % Nn, m = (h / Nn) % Nm, p = h / (Nn * Nm);
-  // per-plane constants (square roots and divisions, ~300 FP64 instructions)
-  // once per CTA in shared memory instead of once per thread
-  __shared__ NlCoef s_cf;
-  __shared__ double s_lin[11];
-  if (threadIdx.x == 0) {
-    s_cf = nl_coef(P, s, n, m, p);
-    const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
-    const double rh = 0.5;
-    s_lin[0] = pb.qs[s] * pb.Omega_cs[s] / (double)pl;
-    s_lin[1] = pb.nu * (colc(Nn, n) + colc(Nm, m) + colc(Np, p));
-    s_lin[2] = sqrt((n + 1) * rh); s_lin[3] = sqrt(n * rh);
-    s_lin[4] = sqrt((m + 1) * rh); s_lin[5] = sqrt(m * rh);
-    s_lin[6] = sqrt((p + 1) * rh); s_lin[7] = sqrt(p * rh);
-    s_lin[8] = pb.u_s[3 * s] / a0;
-    s_lin[9] = pb.u_s[3 * s + 1] / a1;
-    s_lin[10] = pb.u_s[3 * s + 2] / a2;
-  }
-  __syncthreads();
-  const NlCoef cf = s_cf;
+  // per-plane constants from the host-built table (no square roots or divisions here)
+  const GenPlane* gp = static_cast<const GenPlane*>(P.gen) + id;
+  const NlCoef cf = gp->cf;
+  const double* s_lin = gp->lin;
   const bool anyx = cf.ix[0] >= 0 || cf.ix[1] >= 0 || cf.ix[2] >= 0;
   const bool anyy = cf.iy[0] >= 0 || cf.iy[1] >= 0 || cf.iy[2] >= 0;
   const bool anyz = cf.iz[0] >= 0 || cf.iz[1] >= 0 || cf.iz[2] >= 0;
@@ -644,10 +658,7 @@ __device__ inline void lin_bracket_sums(const DevPlan& P, const double2* __restr
   const size_t pl = (size_t)P.plane;
   const int s = id / P.nh, h = id % P.nh;
   const int n = h % pb.Nn, m = (h / pb.Nn) % pb.Nm, p = h / (pb.Nn * pb.Nm);
-  __shared__ NlCoef s_cf;
-  if (threadIdx.x == 0) s_cf = nl_coef(P, s, n, m, p);
-  __syncthreads();
-  const NlCoef cf = s_cf;
+  const NlCoef cf = (static_cast<const GenPlane*>(P.gen) + id)->cf;
   const double2 zero = make_double2(0.0, 0.0);
   for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
     S[pt] = cf.in_ >= 0 ? cscale(cf.gx, R[(size_t)cf.in_ * pl + pt]) : zero;
