@@ -165,7 +165,11 @@ int spx_krylov_axpy(const void* V, int64_t n, int32_t k, const void* c, void* x,
 /*
  * g = J(y)^T w (plain transpose, no conjugation): the vector-Jacobian product of
  * the holomorphic right-hand side.  conj(J^T conj(w)) = J^H w is what
- * torch autograd needs; the Python layer applies the conjugations.
+ * torch autograd needs; the Python layer applies the conjugations.  Every
+ * layout: 1D1V (two launches) and the general 2-D / 3-D one (three launches:
+ * real-space planes of y and forward transforms of w, the real-space field
+ * gradients, then one block per Hermite plane and per field component).
+ * ws as for spx_rhs (spx_rhs_workspace_bytes).
  */
 int spx_vjp(const spx_plan* plan, const void* y, const void* w, void* g, void* ws,
             size_t ws_bytes, void* stream);

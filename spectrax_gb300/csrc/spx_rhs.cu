@@ -170,11 +170,18 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
       return SPX_E_UNSUPPORTED;
     }
     const int nplanes = p.Ns * P.nh;
-    pl->gen.resize((size_t)nplanes * sizeof(GenPlane));
-    for (int id = 0; id < nplanes; ++id) {
-      const GenPlane g = gen_plane(P, id);
-      std::memcpy(pl->gen.data() + (size_t)id * sizeof(GenPlane), &g, sizeof(GenPlane));
+    // forward table (GenPlane per plane), then the transposed bracket (GenPlaneT per plane)
+    std::vector<GenPlane> fwd((size_t)nplanes);
+    for (int id = 0; id < nplanes; ++id) fwd[id] = gen_plane(P, id);
+    std::vector<GenPlaneT> tr((size_t)nplanes);
+    if (!gen_plane_t(fwd.data(), nplanes, tr.data())) {
+      set_error("internal: a Hermite plane has too many transposed bracket terms");
+      return SPX_E_UNSUPPORTED;
     }
+    pl->gen.resize((size_t)nplanes * (sizeof(GenPlane) + sizeof(GenPlaneT)));
+    std::memcpy(pl->gen.data(), fwd.data(), (size_t)nplanes * sizeof(GenPlane));
+    std::memcpy(pl->gen.data() + (size_t)nplanes * sizeof(GenPlane), tr.data(),
+                (size_t)nplanes * sizeof(GenPlaneT));
     // real-space planes of y (RHS) and of y and v (JVP)
     const size_t nreal = (size_t)p.Ns * P.nh + 3 * (size_t)p.Ns + 3;
     pl->ws_bytes = 2 * nreal * P.plane * sizeof(double2);
@@ -390,6 +397,65 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_lin_sums(const DevPlan* __re
   lin_bracket_sums(P, R, blockIdx.x, S + (size_t)blockIdx.x * 6 * P.plane);
 }
 
+// General-path VJP, pass 1: y's real-space planes and field combinations
+// (blocks [0, nreal)), then W_r of w (blocks [nreal, nreal + nplanes)).
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_real(const DevPlan* __restrict__ gP,
+                                                            const double2* __restrict__ gtab,
+                                                            const double2* __restrict__ y,
+                                                            const double2* __restrict__ w,
+                                                            double2* __restrict__ ws) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.pplane;
+  const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
+  const int b = blockIdx.x;
+  if (b < nreal) general_to_real(P, stab, y, b, ws + (size_t)b * P.plane, sA, sB);
+  else general_w_real(P, stab, w, b - nreal, ws + (size_t)b * P.plane, sA, sB);
+}
+
+// Pass 2: the six real-space field gradients, one thread per point.
+__global__ void __launch_bounds__(NTHREADS) k_vjp_fsum(const DevPlan* __restrict__ gP,
+                                                      const double2* __restrict__ ws,
+                                                      double2* __restrict__ gF) {
+  __shared__ DevPlan P;
+  if (threadIdx.x == 0) P = *gP;
+  __syncthreads();
+  const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
+  const double2* W = ws + (size_t)nreal * P.plane;
+  for (size_t pt = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pt < (size_t)P.plane;
+       pt += (size_t)gridDim.x * blockDim.x)
+    vjp_field_point(P, ws, W, pt, gF);
+}
+
+// Pass 3: blocks [0, nplanes) the Hermite planes of g, then six field blocks.
+__global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_gen(const DevPlan* __restrict__ gP,
+                                                           const double2* __restrict__ gtab,
+                                                           const double2* __restrict__ w,
+                                                           const double2* __restrict__ ws,
+                                                           const double2* __restrict__ gF,
+                                                           double2* __restrict__ g) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  EpiStore epi{g};
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + P.pplane;
+  const int nplanes = P.pb.Ns * P.nh;
+  const int nreal = nplanes + 3 * P.pb.Ns + 3;
+  const int b = blockIdx.x;
+  if (b >= nplanes) {
+    vjp_field_plane(P, stab, w + P.nc, gF + (size_t)(b - nplanes) * P.plane, b - nplanes, sA, sB, epi);
+    return;
+  }
+  const double2* GB = ws + (size_t)nplanes * P.plane;
+  const double2* W = ws + (size_t)nreal * P.plane;
+  general_nl_plane_t<3>(P, stab, w, W, GB, nullptr, nullptr, b, sA, sB, epi);
+}
+
 static bool g_attr_done = false;
 
 // Allow each kernel the opt-in shared memory minus its static part.
@@ -423,6 +489,8 @@ static int set_attrs() {
   if ((rc = allow_smem(k_jvp_real, optin)) != SPX_OK) return rc;
   if ((rc = allow_smem(k_jvp_nl, optin)) != SPX_OK) return rc;
   if ((rc = allow_smem(k_jvp_nl_lin, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_vjp_real, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_vjp_gen, optin)) != SPX_OK) return rc;
   g_attr_done = true;
   return SPX_OK;
 }
@@ -640,11 +708,24 @@ int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws
   int rc = check_vec_args(pl, y, wv, g, ws, ws_bytes, "spx_vjp");
   if (rc != SPX_OK) return rc;
   const DevPlan& P = pl->host;
-  if (P.path != 0) {
-    set_error("spx_vjp: only the 1D1V layout (Ny = Nz = Nm = Np = 1) has a transpose kernel");
-    return SPX_E_UNSUPPORTED;
-  }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (P.path != 0) {
+    // workspace: y's real planes (nreal), W (nplanes), 6 field gradients;
+    // nreal + nplanes + 6 <= 2 nreal for Ns >= 1, inside spx_rhs_workspace_bytes
+    const int nplanes = P.pb.Ns * P.nh;
+    const int nreal = nplanes + 3 * P.pb.Ns + 3;
+    const double2* yy = static_cast<const double2*>(y);
+    const double2* ww = static_cast<const double2*>(wv);
+    double2* W = static_cast<double2*>(ws);
+    double2* gF = W + (size_t)(nreal + nplanes) * P.plane;
+    k_vjp_real<<<nreal + nplanes, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, ww, W);
+    const int fgrid = (int)std::min<long long>((P.plane + NTHREADS - 1) / NTHREADS, 4LL * 152);
+    k_vjp_fsum<<<fgrid, NTHREADS, 0, st>>>(pl->d_plan, W, gF);
+    k_vjp_gen<<<nplanes + 6, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, ww, W, gF,
+                                                              static_cast<double2*>(g));
+    SPX_CUDA(cudaGetLastError());
+    return SPX_OK;
+  }
   double2* part = static_cast<double2*>(ws);
   k_vjp1v<<<P.pb.Ns * P.ntiles, pl->threads, pl->smem_1v, st>>>(
       pl->d_plan, pl->d_tab, static_cast<const double2*>(y), static_cast<const double2*>(wv),

@@ -497,6 +497,47 @@ __host__ inline GenPlane gen_plane(const DevPlan& P, int id) {
   return g;
 }
 
+// Transposed bracket of one Hermite plane q: the (output plane r, field j,
+// weight c) of every bracket term of r that reads C_q (field j: 0..2 = the
+// species combinations G_x, G_y, G_z, 3..5 = B_x, B_y, B_z).  At most 3 + 9
+// entries (one per E term, three per B term).  Stored after the GenPlane table.
+constexpr int GENT_MAX = 12;
+struct GenPlaneT {
+  int cnt;
+  int r[GENT_MAX];
+  int j[GENT_MAX];
+  double c[GENT_MAX];
+};
+
+static_assert(sizeof(GenPlane) % alignof(GenPlaneT) == 0, "GenPlaneT entries follow the GenPlane table");
+
+__host__ __device__ inline const GenPlaneT* gen_t(const DevPlan& P) {
+  return reinterpret_cast<const GenPlaneT*>(static_cast<const char*>(P.gen) +
+                                            (size_t)P.pb.Ns * P.nh * sizeof(GenPlane));
+}
+
+// Builds the transposed table from the forward entries (r ascending, so the
+// device sums run in a fixed order).  Returns false if a plane has more than
+// GENT_MAX entries (cannot happen for the bracket of spectrax/_model.py:168-184).
+__host__ inline bool gen_plane_t(const GenPlane* fwd, int nplanes, GenPlaneT* T) {
+  for (int q = 0; q < nplanes; ++q) T[q] = GenPlaneT{};
+  auto add = [&](int q, int r, int j, double c) {
+    if (q < 0) return true;
+    GenPlaneT& t = T[q];
+    if (t.cnt >= GENT_MAX) return false;
+    t.r[t.cnt] = r; t.j[t.cnt] = j; t.c[t.cnt] = c; ++t.cnt;
+    return true;
+  };
+  for (int r = 0; r < nplanes; ++r) {
+    const NlCoef& cf = fwd[r].cf;
+    bool ok = add(cf.in_, r, 0, cf.gx) && add(cf.im_, r, 1, cf.gy) && add(cf.ip_, r, 2, cf.gz);
+    for (int k = 0; k < 3; ++k)
+      ok = ok && add(cf.ix[k], r, 3, cf.bx[k]) && add(cf.iy[k], r, 4, cf.by[k]) && add(cf.iz[k], r, 5, cf.bz[k]);
+    if (!ok) return false;
+  }
+  return true;
+}
+
 // sum_k w[k] * R[ids[k]][pt] over the present neighbours
 __device__ __forceinline__ double2 combo3(const double2* __restrict__ R, size_t pl, const int* ids,
                                           const double* w, size_t pt) {
@@ -546,6 +587,14 @@ __device__ __forceinline__ double2 bracket_point(const NlCoef& cf, const double2
 // MODE 0: RHS; 1: JVP (two brackets); 2: linearised JVP, where RB holds the
 // six precomputed bracket sums of y for this plane (lin_bracket_sums), so the
 // second bracket is six complex products with v's fields GB2.
+// MODE 3: VJP (plain transpose J^T w) of Hermite plane `id`: lin = w, RA = the
+// planes W_r = (q Omega / N)_r FFT(P_i M w_r) (general_w_real), GA = y's field
+// combinations.  The transposed bracket sum_e c_e F_{j_e}(x) W_{r_e}(x) goes
+// through the inverse transform (the transpose of the forward one, the DFT
+// matrix being symmetric), is masked, and the streaming/collision/diffusion
+// terms are the forward formula applied to w (the Hermite streaming matrix is
+// symmetric, the rest diagonal); the current's transpose adds the -J/Omega_0
+// weights of w_E to the (0,0,0), (1,0,0), (0,1,0), (0,0,1) planes.
 // ------------------------------------------------------------------------
 template <int MODE, class Epi>
 __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__ tab,
@@ -570,9 +619,22 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
   // bracket sums of y), GB2 = G_v.
   const FieldPlanes FA = field_planes(GA, s, Ns, pl);
   FieldPlanes FB;
-  if (MODE != 0) FB = field_planes(GB2, s, Ns, pl);
+  if (MODE == 1 || MODE == 2) FB = field_planes(GB2, s, Ns, pl);
   const double2* Sy = (MODE == 2) ? RB + (size_t)id * 6 * pl : nullptr;
-  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+  if (MODE == 3) {
+    const GenPlaneT* tq = gen_t(P) + id;
+    const int ne = tq->cnt;
+    for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int e = 0; e < ne; ++e) {
+        const int j = tq->j[e];
+        const double2* Fj = j < 3 ? FA.Gx + (size_t)j * pl : FA.Bx + (size_t)(j - 3) * pl;
+        acc = cfma(Fj[pt], cscale(tq->c[e], RA[(size_t)tq->r[e] * pl + pt]), acc);
+      }
+      sA[padded(P, (int)pt)] = acc;
+    }
+  }
+  for (size_t pt = threadIdx.x; MODE != 3 && pt < pl; pt += blockDim.x) {
     double2 acc = bracket_point(cf, RA, FA, pl, pt, anyx, anyy, anyz, make_double2(0.0, 0.0));
     if (MODE == 1) acc = bracket_point(cf, RB, FB, pl, pt, anyx, anyy, anyz, acc);
     if (MODE == 2) {
@@ -586,10 +648,27 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
     sA[padded(P, (int)pt)] = acc;
   }
   __syncthreads();
-  double2* f = fft_planes_t<false, true>(sA, sB, P, tab);
+  double2* f = fft_planes_t<MODE == 3, true>(sA, sB, P, tab);
 
   const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
-  const double sc = s_lin[0], dcol = s_lin[1];
+  const double sc = MODE == 3 ? 1.0 : s_lin[0], dcol = s_lin[1];
+  // MODE 3: transposed current weights on w_E (spectrax/_model.py:15-72 and
+  // dE = -J / Omega_0 of spectrax/_simulation.py:103-106)
+  double cjx = 0.0, cjy = 0.0, cjz = 0.0;
+  if (MODE == 3) {
+    const double w0 = -P.iO0 * pb.qs[s] * a0 * a1 * a2;
+    const double rs2 = 0.70710678118654752440;
+    if (n == 0 && m == 0 && p == 0) {
+      cjx = w0 * pb.u_s[3 * s]; cjy = w0 * pb.u_s[3 * s + 1]; cjz = w0 * pb.u_s[3 * s + 2];
+    } else if (n == 1 && m == 0 && p == 0) {
+      cjx = w0 * a0 * rs2;
+    } else if (n == 0 && m == 1 && p == 0) {
+      cjy = w0 * a1 * rs2;
+    } else if (n == 0 && m == 0 && p == 1) {
+      cjz = w0 * a2 * rs2;
+    }
+  }
+  const bool hasJ = MODE == 3 && (cjx != 0.0 || cjy != 0.0 || cjz != 0.0);
   const double snp = s_lin[2], snm = s_lin[3], smp = s_lin[4], smm = s_lin[5], spp = s_lin[6], spm = s_lin[7];
   const double ux = s_lin[8], uy = s_lin[9], uz = s_lin[10];
   const double2* Cp = lin + (size_t)id * pl;
@@ -635,6 +714,12 @@ __device__ void general_nl_plane_t(const DevPlan& P, const double2* __restrict__
       re = fma(sc, v.x, re);
       im = fma(sc, v.y, im);
     }
+    if (hasJ) {
+      const double2* wE = lin + P.nc;
+      const double2 ex = wE[pt], ey = wE[pl + pt], ez = wE[2 * pl + pt];
+      re = fma(cjx, ex.x, fma(cjy, ey.x, fma(cjz, ez.x, re)));
+      im = fma(cjx, ex.y, fma(cjy, ey.y, fma(cjz, ez.y, im)));
+    }
     epi((size_t)id * pl + pt, make_double2(re, im));
   }
 }
@@ -667,6 +752,99 @@ __device__ inline void lin_bracket_sums(const DevPlan& P, const double2* __restr
     S[3 * pl + pt] = combo3(R, pl, cf.ix, cf.bx, pt);
     S[4 * pl + pt] = combo3(R, pl, cf.iy, cf.by, pt);
     S[5 * pl + pt] = combo3(R, pl, cf.iz, cf.bz, pt);
+  }
+}
+
+// ------------------------------------------------------------------------
+// General-path VJP.  The nonlinear term of output plane r is
+//   sc_r M P_f FFT( sum_j F_j(x) S_{r,j}(x) ),  S_{r,j} = sum_q c_{r,j,q} IFFT(P_i M C_q),
+// F_j the real-space field combinations (G_s = E + u_s x B, then B), so its
+// transpose needs, per plane r, W_r = sc_r FFT(P_i M w_r) (the forward DFT
+// matrix is symmetric, so the transpose of "mask, shift, forward" applied to
+// w_r is "mask, shift, forward" of w_r): general_w_real.
+// ------------------------------------------------------------------------
+__device__ inline void general_w_real(const DevPlan& P, const double2* __restrict__ tab,
+                                      const double2* __restrict__ w, int id, double2* __restrict__ out,
+                                      double2* sA, double2* sB) {
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const int pl = P.plane;
+  const double sc = (static_cast<const GenPlane*>(P.gen) + id)->lin[0];
+  for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+    const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
+    double2 v = make_double2(0.0, 0.0);
+    if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut))
+      v = w[(size_t)id * pl + pt];
+    sA[std_index(cy, Ny) * P.prow + std_index(cx, Nx) * Nz + std_index(cz, Nz)] = v;
+  }
+  __syncthreads();
+  double2* r = fft_planes_t<false, false>(sA, sB, P, tab);
+  for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) out[pt] = cscale(sc, r[padded(P, pt)]);
+}
+
+// Field part of the transpose at real-space point pt: with R_{s,j} = sum_{r in s}
+// W_r S_{r,j} (j = 0..2) and R_{B,j} = sum_r W_r S_{r,3+j}, the gradient of the
+// real-space fields is g_E = sum_s R_s and g_B = R_B + sum_s (R_s x u_s)-terms
+// (the chain through G_s = E + u_s x B).  Sums in plane order.  Writes the six
+// real-space planes (Ex, Ey, Ez, Bx, By, Bz) to gF.
+__device__ inline void vjp_field_point(const DevPlan& P, const double2* __restrict__ Cr,
+                                       const double2* __restrict__ W, size_t pt,
+                                       double2* __restrict__ gF) {
+  const spx_problem& pb = P.pb;
+  const size_t pl = (size_t)P.plane;
+  const GenPlane* gp = static_cast<const GenPlane*>(P.gen);
+  const double2 z = make_double2(0.0, 0.0);
+  double2 E0 = z, E1 = z, E2 = z, B0 = z, B1 = z, B2 = z;
+  for (int s = 0; s < pb.Ns; ++s) {
+    double2 R0 = z, R1 = z, R2 = z;
+    for (int h = 0; h < P.nh; ++h) {
+      const int r = s * P.nh + h;
+      const NlCoef& cf = gp[r].cf;
+      const double2 Wr = W[(size_t)r * pl + pt];
+      if (cf.in_ >= 0) R0 = cfma(Wr, cscale(cf.gx, Cr[(size_t)cf.in_ * pl + pt]), R0);
+      if (cf.im_ >= 0) R1 = cfma(Wr, cscale(cf.gy, Cr[(size_t)cf.im_ * pl + pt]), R1);
+      if (cf.ip_ >= 0) R2 = cfma(Wr, cscale(cf.gz, Cr[(size_t)cf.ip_ * pl + pt]), R2);
+      B0 = cfma(Wr, combo3(Cr, pl, cf.ix, cf.bx, pt), B0);
+      B1 = cfma(Wr, combo3(Cr, pl, cf.iy, cf.by, pt), B1);
+      B2 = cfma(Wr, combo3(Cr, pl, cf.iz, cf.bz, pt), B2);
+    }
+    const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
+    E0 = cadd(E0, R0); E1 = cadd(E1, R1); E2 = cadd(E2, R2);
+    // G_x = E_x + u_y B_z - u_z B_y, G_y = E_y + u_z B_x - u_x B_z, G_z = E_z + u_x B_y - u_y B_x
+    B2 = crfma(u1, R0, B2); B1 = crfma(-u2, R0, B1);
+    B0 = crfma(u2, R1, B0); B2 = crfma(-u0, R1, B2);
+    B1 = crfma(u0, R2, B1); B0 = crfma(-u1, R2, B0);
+  }
+  gF[pt] = E0; gF[pl + pt] = E1; gF[2 * pl + pt] = E2;
+  gF[3 * pl + pt] = B0; gF[4 * pl + pt] = B1; gF[5 * pl + pt] = B2;
+}
+
+// Field component c (0..5 = Ex..Bz) of the transpose: the masked inverse
+// transform of its real-space gradient gr, plus the curl's transpose
+// (dE = i K x B, dB = -i K x E give g_E += i K x w_B, g_B += -i K x w_E).
+template <class Epi>
+__device__ inline void vjp_field_plane(const DevPlan& P, const double2* __restrict__ tab,
+                                       const double2* __restrict__ wF, const double2* __restrict__ gr,
+                                       int c, double2* sA, double2* sB, Epi& epi) {
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const size_t pl = (size_t)P.plane;
+  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) sA[padded(P, (int)pt)] = gr[pt];
+  __syncthreads();
+  double2* f = fft_planes_t<true, true>(sA, sB, P, tab);
+  const double2* wO = wF + (size_t)(c < 3 ? 3 : 0) * pl;   // w_B for E, w_E for B
+  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) {
+    const int cz = pt % Nz, cx = (pt / Nz) % Nx, cy = pt / (Nz * Nx);
+    const double Kx = ktab(P, tab, 1, cx).x, Ky = ktab(P, tab, 0, cy).x, Kz = ktab(P, tab, 2, cz).x;
+    const double2 o0 = wO[pt], o1 = wO[pl + pt], o2 = wO[2 * pl + pt];
+    const int k = c % 3;
+    const double2 kx = k == 0 ? csub(cscale(Ky, o2), cscale(Kz, o1))
+                     : k == 1 ? csub(cscale(Kz, o0), cscale(Kx, o2))
+                              : csub(cscale(Kx, o1), cscale(Ky, o0));
+    double2 v = c < 3 ? make_double2(-kx.y, kx.x) : make_double2(kx.y, -kx.x);
+    if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut)) {
+      const int sidx = std_index(cy, Ny) * P.prow + std_index(cx, Nx) * Nz + std_index(cz, Nz);
+      v = cadd(v, f[sidx]);
+    }
+    epi((size_t)P.nc + (size_t)c * pl + pt, v);
   }
 }
 
