@@ -347,7 +347,7 @@ def _extra_two_stream_run():
 
 
 def _extra_orszag_tang():
-    """2D3V Orszag-Tang-like state (64x64, 8^3 Hermite, 2 species, 67.5 MB): RHS and JVP rates,
+    """2D3V Orszag-Tang-like state (64x64, 8^3 Hermite, 2 species, 67.5 MB): RHS, JVP and VJP rates,
     three implicit-midpoint steps (Newton-GMRES, restart 30) and the energy change over them."""
     import torch
     from spectrax_gb300 import midpoint
@@ -362,7 +362,8 @@ def _extra_orszag_tang():
     for _ in range(2):
         plan.rhs_into(y, dy)
         plan.jvp_into(y, v, dy)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    plan.vjp_into(y, v, dy)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record()
     for _ in range(10):
         plan.rhs_into(y, dy)
@@ -370,8 +371,12 @@ def _extra_orszag_tang():
     for _ in range(10):
         plan.jvp_into(y, v, dy)
     ev[2].record()
+    for _ in range(10):
+        plan.vjp_into(y, v, dy)
+    ev[3].record()
     torch.cuda.synchronize()
     rhs_ms, jvp_ms = ev[0].elapsed_time(ev[1]) / 10, ev[1].elapsed_time(ev[2]) / 10
+    vjp_ms = ev[2].elapsed_time(ev[3]) / 10
     n = plan.state_len
     # explicit Dopri8 on the same state: fixed dt = 0.01, attempts timed after a warm-up graph
     from spectrax_gb300.dopri8 import Dopri8Solver
@@ -398,7 +403,7 @@ def _extra_orszag_tang():
     return {"workload": "Orszag-Tang 2D3V Nx=Ny=64, Nn=Nm=Np=8, Ns=2 (4.2M coefficients)",
             "rhs_ms": rhs_ms, "rhs_evals_per_s": 1e3 / rhs_ms,
             "rhs_hbm_gbs": 32.0 * n / (rhs_ms * 1e-3) / 1e9,
-            "jvp_ms": jvp_ms, "dopri8_ms_per_step": d8_ms, "dopri8_rhs_evals_per_s": 13e3 / d8_ms,
+            "jvp_ms": jvp_ms, "vjp_ms": vjp_ms, "dopri8_ms_per_step": d8_ms, "dopri8_rhs_evals_per_s": 13e3 / d8_ms,
             "midpoint_steps": info["steps"], "midpoint_s": tm,
             "midpoint_steps_per_s": info["steps"] / tm, "newton_iterations": info.get("newton"),
             "jvp_matvecs": info.get("matvecs"),

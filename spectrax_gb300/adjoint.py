@@ -18,7 +18,10 @@ history is computed exactly for the discrete solution:
   (in the same launch) for theta = (nu, k, u_x per species), plus the
   initial-state terms for k and the perturbation amplitude;
 * an exactly Hermitian trajectory (odd Nx, the spectrum of real fields) runs all
-  three on packed real transforms (``hermitian=True``, the default).
+  three on packed real transforms (``hermitian=True``, the default);
+* 2-D / 3-D layouts: the same recursion for the state gradient, the steps
+  recomputed with ``spx_rhs`` and device linear combinations, the sweep on
+  ``spx_vjp`` (no parameter sums).
 
 ``TwoStreamLoss`` puts this behind ``torch.autograd.Function`` for the adjoint
 workload (1D1V two-stream, loss = LSQ slope of log E over t in [10, 40] plus
@@ -59,18 +62,20 @@ class Dopri8Adjoint:
 
     def __init__(self, plan: Plan, dt: float, nsteps: int, ckpt_every: int | None = None, masses=None,
                  hermitian=True):
-        if plan.problem.Ny != 1 or plan.problem.Nz != 1 or plan.problem.Nm != 1 or plan.problem.Np != 1:
-            raise ValueError("the adjoint is implemented for the 1D1V layout")
+        pb = plan.problem
+        # 2-D / 3-D layouts: the state gradient only (no parameter sums), with
+        # the steps recomputed through spx_rhs and the sweep through spx_vjp
+        self.general = not (pb.Ny == 1 and pb.Nz == 1 and pb.Nm == 1 and pb.Np == 1)
         self.plan, self.dt, self.N = plan, float(dt), int(nsteps)
         # exactly Hermitian trajectories (the spectra of real fields) run the
         # forward, the recomputation and the adjoint sweep on packed transforms;
         # the adjoint of a Hermitian state stays exactly Hermitian
-        self.hermitian = bool(hermitian)
+        self.hermitian = bool(hermitian) and not self.general
         self.herm = False
         self.m = int(ckpt_every or math.ceil(math.sqrt(self.N)))
         self.masses = masses
         self.n = plan.state_len
-        self.nc = self.n - 6 * plan.problem.Nx
+        self.nc = self.n - 6 * pb.Nx * pb.Ny * pb.Nz
         self.O0 = float(plan.problem.Omega_cs[0])
         dev = plan.device
         self.ts = np.arange(self.N + 1) * self.dt
@@ -118,6 +123,17 @@ class Dopri8Adjoint:
         """Recompute `steps` steps from Ys[0, 0], keeping the stage inputs Ys[q]."""
         B = self._buffers()
         L = _lib.lib()
+        if self.general:
+            # stage inputs Y_j = y + h sum_{i<j} a_ji K_i, K_j = f(Y_j); y' = y + h sum_j b_j K_j
+            h, Kb = self.dt, B["Kb"]
+            for q in range(steps):
+                Yq, y = B["Ys"][q], B["Ys"][q, 0]
+                for j in range(S):
+                    if j > 0:
+                        lincomb(Yq[j], [(1.0, y)] + [(h * _A.get(j, {}).get(i, 0.0), Kb[i]) for i in range(j)])
+                    self.plan.rhs_into(Yq[j], Kb[j])
+                lincomb(B["Ys"][q + 1, 0], [(1.0, y)] + [(h * _B[j], Kb[j]) for j in range(S)])
+            return
         for q in range(steps):
             _lib.check(L.spx_rk_step_store_ex(self.plan.handle, _ptr(B["Ys"][q, 0]), C.c_double(self.dt),
                                               _ptr(B["Ys"][q]), _ptr(B["Kb"]), _ptr(B["Ys"][q + 1, 0]),
@@ -141,6 +157,9 @@ class Dopri8Adjoint:
                     if aij != 0.0:
                         terms.append((h * aij, gY[i]))
                 lincomb(gk, terms)
+                if self.general:
+                    self.plan.vjp_into(Yq[j], gk, gY[j])
+                    continue
                 _lib.check(L.spx_vjp_param_ex(self.plan.handle, _ptr(Yq[j]), _ptr(gk), _ptr(gY[j]), accp, ws, wsb,
                                               int(self.herm), _stream_ptr()), "spx_vjp_param_ex")
             lincomb(mu, [(1.0, mu)] + [(1.0, gY[j]) for j in range(S)])
@@ -168,7 +187,8 @@ class Dopri8Adjoint:
 
     def backward(self, dLdE: torch.Tensor, mu_final=None, use_graphs=True):
         """dLdE: (N+1,) field-energy sensitivities.  Returns (conj of dL/dy0, param dots
-        (2 + Ns): [nu, k d/dk, u_x per species])."""
+        (2 + Ns): [nu, k d/dk, u_x per species]); the param dots are None on the
+        2-D / 3-D layouts."""
         B = self._buffers()
         dev = self.plan.device
         dLdE = dLdE.to(dev, torch.float64)
@@ -193,7 +213,7 @@ class Dopri8Adjoint:
         _lib.check(_lib.lib().spx_rk_status(C.byref(st), _stream_ptr()), "spx_rk_status")
         if st.value != 0:
             raise RuntimeError(f"step recomputation failed: status {_lib.STATUS_NAMES.get(st.value, st.value)}")
-        return mu.clone(), acc.clone()
+        return mu.clone(), (None if self.general else acc.clone())
 
 
 # ----------------------------------------------------------------- two-stream workload

@@ -182,9 +182,11 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
     std::memcpy(pl->gen.data(), fwd.data(), (size_t)nplanes * sizeof(GenPlane));
     std::memcpy(pl->gen.data() + (size_t)nplanes * sizeof(GenPlane), tr.data(),
                 (size_t)nplanes * sizeof(GenPlaneT));
-    // real-space planes of y (RHS) and of y and v (JVP)
+    // real-space planes of y (RHS), of y and v (JVP); of y, the forward
+    // transforms of w and 6 Ns per-species field sums (VJP)
     const size_t nreal = (size_t)p.Ns * P.nh + 3 * (size_t)p.Ns + 3;
-    pl->ws_bytes = 2 * nreal * P.plane * sizeof(double2);
+    const size_t nws = std::max(2 * nreal, nreal + (size_t)nplanes + 6 * (size_t)p.Ns);
+    pl->ws_bytes = nws * P.plane * sizeof(double2);
   }
   if (pl->smem_1v > smem_max) { set_error("Nx too large for the fused path"); return SPX_E_UNSUPPORTED; }
   return SPX_OK;
@@ -416,18 +418,21 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_real(const DevPlan* __re
   else general_w_real(P, stab, w, b - nreal, ws + (size_t)b * P.plane, sA, sB);
 }
 
-// Pass 2: the six real-space field gradients, one thread per point.
+// Pass 2: the per-species field sums, one thread per (point, species,
+// component): blockIdx.y = s * 6 + j, written to plane blockIdx.y of S.
 __global__ void __launch_bounds__(NTHREADS) k_vjp_fsum(const DevPlan* __restrict__ gP,
                                                       const double2* __restrict__ ws,
-                                                      double2* __restrict__ gF) {
+                                                      double2* __restrict__ S) {
   __shared__ DevPlan P;
   if (threadIdx.x == 0) P = *gP;
   __syncthreads();
   const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
   const double2* W = ws + (size_t)nreal * P.plane;
+  const int s = blockIdx.y / 6, j = blockIdx.y % 6;
+  double2* out = S + (size_t)blockIdx.y * P.plane;
   for (size_t pt = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pt < (size_t)P.plane;
        pt += (size_t)gridDim.x * blockDim.x)
-    vjp_field_point(P, ws, W, pt, gF);
+    out[pt] = vjp_field_sum(P, ws, W, pt, s, j);
 }
 
 // Pass 3: blocks [0, nplanes) the Hermite planes of g, then six field blocks.
@@ -435,7 +440,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_gen(const DevPlan* __res
                                                            const double2* __restrict__ gtab,
                                                            const double2* __restrict__ w,
                                                            const double2* __restrict__ ws,
-                                                           const double2* __restrict__ gF,
+                                                           const double2* __restrict__ S,
                                                            double2* __restrict__ g) {
   __shared__ DevPlan P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -448,7 +453,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_gen(const DevPlan* __res
   const int nreal = nplanes + 3 * P.pb.Ns + 3;
   const int b = blockIdx.x;
   if (b >= nplanes) {
-    vjp_field_plane(P, stab, w + P.nc, gF + (size_t)(b - nplanes) * P.plane, b - nplanes, sA, sB, epi);
+    vjp_field_plane(P, stab, w + P.nc, S, b - nplanes, sA, sB, epi);
     return;
   }
   const double2* GB = ws + (size_t)nplanes * P.plane;
@@ -710,18 +715,17 @@ int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws
   const DevPlan& P = pl->host;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (P.path != 0) {
-    // workspace: y's real planes (nreal), W (nplanes), 6 field gradients;
-    // nreal + nplanes + 6 <= 2 nreal for Ns >= 1, inside spx_rhs_workspace_bytes
+    // workspace: y's real planes (nreal), W (nplanes), 6 Ns per-species field sums
     const int nplanes = P.pb.Ns * P.nh;
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
     const double2* yy = static_cast<const double2*>(y);
     const double2* ww = static_cast<const double2*>(wv);
     double2* W = static_cast<double2*>(ws);
-    double2* gF = W + (size_t)(nreal + nplanes) * P.plane;
+    double2* S = W + (size_t)(nreal + nplanes) * P.plane;
     k_vjp_real<<<nreal + nplanes, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, ww, W);
-    const int fgrid = (int)std::min<long long>((P.plane + NTHREADS - 1) / NTHREADS, 4LL * 152);
-    k_vjp_fsum<<<fgrid, NTHREADS, 0, st>>>(pl->d_plan, W, gF);
-    k_vjp_gen<<<nplanes + 6, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, ww, W, gF,
+    const int fx = (int)std::min<long long>((P.plane + NTHREADS - 1) / NTHREADS, 65535LL);
+    k_vjp_fsum<<<dim3(fx, 6 * P.pb.Ns), NTHREADS, 0, st>>>(pl->d_plan, W, S);
+    k_vjp_gen<<<nplanes + 6, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, ww, W, S,
                                                               static_cast<double2*>(g));
     SPX_CUDA(cudaGetLastError());
     return SPX_OK;

@@ -781,53 +781,66 @@ __device__ inline void general_w_real(const DevPlan& P, const double2* __restric
   for (int pt = threadIdx.x; pt < pl; pt += blockDim.x) out[pt] = cscale(sc, r[padded(P, pt)]);
 }
 
-// Field part of the transpose at real-space point pt: with R_{s,j} = sum_{r in s}
-// W_r S_{r,j} (j = 0..2) and R_{B,j} = sum_r W_r S_{r,3+j}, the gradient of the
-// real-space fields is g_E = sum_s R_s and g_B = R_B + sum_s (R_s x u_s)-terms
-// (the chain through G_s = E + u_s x B).  Sums in plane order.  Writes the six
-// real-space planes (Ex, Ey, Ez, Bx, By, Bz) to gF.
-__device__ inline void vjp_field_point(const DevPlan& P, const double2* __restrict__ Cr,
-                                       const double2* __restrict__ W, size_t pt,
-                                       double2* __restrict__ gF) {
-  const spx_problem& pb = P.pb;
+// Field part of the transpose, per species s and bracket component j at
+// real-space point pt: R_{s,j} = sum_{r in s} W_r S_{r,j} (j = 0..2: the G_s
+// terms; j = 3..5: the species' share of the B terms), summed in plane order.
+__device__ inline double2 vjp_field_sum(const DevPlan& P, const double2* __restrict__ Cr,
+                                        const double2* __restrict__ W, size_t pt, int s, int j) {
   const size_t pl = (size_t)P.plane;
   const GenPlane* gp = static_cast<const GenPlane*>(P.gen);
-  const double2 z = make_double2(0.0, 0.0);
-  double2 E0 = z, E1 = z, E2 = z, B0 = z, B1 = z, B2 = z;
-  for (int s = 0; s < pb.Ns; ++s) {
-    double2 R0 = z, R1 = z, R2 = z;
-    for (int h = 0; h < P.nh; ++h) {
-      const int r = s * P.nh + h;
-      const NlCoef& cf = gp[r].cf;
-      const double2 Wr = W[(size_t)r * pl + pt];
-      if (cf.in_ >= 0) R0 = cfma(Wr, cscale(cf.gx, Cr[(size_t)cf.in_ * pl + pt]), R0);
-      if (cf.im_ >= 0) R1 = cfma(Wr, cscale(cf.gy, Cr[(size_t)cf.im_ * pl + pt]), R1);
-      if (cf.ip_ >= 0) R2 = cfma(Wr, cscale(cf.gz, Cr[(size_t)cf.ip_ * pl + pt]), R2);
-      B0 = cfma(Wr, combo3(Cr, pl, cf.ix, cf.bx, pt), B0);
-      B1 = cfma(Wr, combo3(Cr, pl, cf.iy, cf.by, pt), B1);
-      B2 = cfma(Wr, combo3(Cr, pl, cf.iz, cf.bz, pt), B2);
+  double2 R = make_double2(0.0, 0.0);
+  for (int h = 0; h < P.nh; ++h) {
+    const int r = s * P.nh + h;
+    const NlCoef& cf = gp[r].cf;
+    double2 t;
+    if (j < 3) {
+      const int q = j == 0 ? cf.in_ : j == 1 ? cf.im_ : cf.ip_;
+      if (q < 0) continue;
+      t = cscale(j == 0 ? cf.gx : j == 1 ? cf.gy : cf.gz, Cr[(size_t)q * pl + pt]);
+    } else {
+      t = j == 3 ? combo3(Cr, pl, cf.ix, cf.bx, pt) : j == 4 ? combo3(Cr, pl, cf.iy, cf.by, pt)
+                                                     : combo3(Cr, pl, cf.iz, cf.bz, pt);
     }
-    const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
-    E0 = cadd(E0, R0); E1 = cadd(E1, R1); E2 = cadd(E2, R2);
-    // G_x = E_x + u_y B_z - u_z B_y, G_y = E_y + u_z B_x - u_x B_z, G_z = E_z + u_x B_y - u_y B_x
-    B2 = crfma(u1, R0, B2); B1 = crfma(-u2, R0, B1);
-    B0 = crfma(u2, R1, B0); B2 = crfma(-u0, R1, B2);
-    B1 = crfma(u0, R2, B1); B0 = crfma(-u1, R2, B0);
+    R = cfma(W[(size_t)r * pl + pt], t, R);
   }
-  gF[pt] = E0; gF[pl + pt] = E1; gF[2 * pl + pt] = E2;
-  gF[3 * pl + pt] = B0; gF[4 * pl + pt] = B1; gF[5 * pl + pt] = B2;
+  return R;
+}
+
+// Real-space gradient of field component c (0..5 = Ex..Bz) at pt from the
+// per-species sums S (plane s*6 + j): g_E = sum_s R_{s,0..2}, g_B = sum_s
+// (R_{s,3..5} + the chain through G_s = E + u_s x B).
+__device__ __forceinline__ double2 vjp_field_grad(const DevPlan& P, const double2* __restrict__ S, int c,
+                                                  size_t pt) {
+  const size_t pl = (size_t)P.plane;
+  double2 g = make_double2(0.0, 0.0);
+  for (int s = 0; s < P.pb.Ns; ++s) {
+    const double2* Ss = S + (size_t)s * 6 * pl + pt;
+    if (c < 3) {
+      g = cadd(g, Ss[(size_t)c * pl]);
+      continue;
+    }
+    const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
+    const double2 R0 = Ss[0], R1 = Ss[pl], R2 = Ss[2 * pl];
+    g = cadd(g, Ss[(size_t)c * pl]);
+    // G_x = E_x + u_y B_z - u_z B_y, G_y = E_y + u_z B_x - u_x B_z, G_z = E_z + u_x B_y - u_y B_x
+    if (c == 3) { g = crfma(u2, R1, g); g = crfma(-u1, R2, g); }
+    else if (c == 4) { g = crfma(-u2, R0, g); g = crfma(u0, R2, g); }
+    else { g = crfma(u1, R0, g); g = crfma(-u0, R1, g); }
+  }
+  return g;
 }
 
 // Field component c (0..5 = Ex..Bz) of the transpose: the masked inverse
-// transform of its real-space gradient gr, plus the curl's transpose
-// (dE = i K x B, dB = -i K x E give g_E += i K x w_B, g_B += -i K x w_E).
+// transform of its real-space gradient (vjp_field_grad of the per-species sums
+// S), plus the curl's transpose (dE = i K x B, dB = -i K x E give
+// g_E += i K x w_B, g_B += -i K x w_E).
 template <class Epi>
 __device__ inline void vjp_field_plane(const DevPlan& P, const double2* __restrict__ tab,
-                                       const double2* __restrict__ wF, const double2* __restrict__ gr,
+                                       const double2* __restrict__ wF, const double2* __restrict__ S,
                                        int c, double2* sA, double2* sB, Epi& epi) {
   const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
   const size_t pl = (size_t)P.plane;
-  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) sA[padded(P, (int)pt)] = gr[pt];
+  for (size_t pt = threadIdx.x; pt < pl; pt += blockDim.x) sA[padded(P, (int)pt)] = vjp_field_grad(P, S, c, pt);
   __syncthreads();
   double2* f = fft_planes_t<true, true>(sA, sB, P, tab);
   const double2* wO = wF + (size_t)(c < 3 ? 3 : 0) * pl;   // w_B for E, w_E for B
