@@ -231,6 +231,43 @@ def plan_for_params(params, mask_mode=None, device=None, tuned=False, tune_for="
     return autotune(pb, device, target=tune_for, sample=sample) if tuned else get_plan(pb, device)
 
 
+class RHSFunction(torch.autograd.Function):
+    """dy/dt = f(y) as a torch autograd node, for ``RHSFunction.apply(y, plan)``.
+
+    f is holomorphic in y (spectrax/_model.py uses no conjugation), so with
+    torch's convention for complex gradients the reverse mode is
+    grad_y = J^H g = conj(J^T conj(g)) (``spx_vjp`` computes the plain
+    transpose J^T) and the forward mode is J v (``spx_jvp``).  The backward is
+    not itself differentiable."""
+
+    @staticmethod
+    def forward(ctx, y, plan):
+        ctx.plan = plan
+        ctx.save_for_backward(y)
+        ctx.save_for_forward(y)
+        return plan.rhs(y.detach().contiguous())
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, g):
+        (y,) = ctx.saved_tensors
+        out = torch.empty_like(y)
+        ctx.plan.vjp_into(y.contiguous(), torch.conj_physical(g).contiguous(), out)
+        return torch.conj_physical(out), None
+
+    @staticmethod
+    def jvp(ctx, y_t, plan_t):
+        (y,) = ctx.saved_tensors
+        out = torch.empty_like(y)
+        return ctx.plan.jvp_into(y.contiguous(), y_t.contiguous(), out)
+
+
+def _apply_rhs(plan, y):
+    if y.requires_grad and torch.is_grad_enabled():
+        return RHSFunction.apply(y, plan)
+    return plan.rhs(y)
+
+
 def _as_cuda_state(y, dev):
     if isinstance(y, torch.Tensor):
         return (y if y.is_cuda else y.to(dev)).to(torch.complex128).contiguous(), "torch_cpu" if not y.is_cuda else "torch"
@@ -239,12 +276,14 @@ def _as_cuda_state(y, dev):
 
 
 def ode_system(Nx, Ny, Nz, Nn, Nm, Np, Ns, t, Ck_Fk, args, mask_mode=None):
-    """Drop-in for spectrax/_simulation.py:55-111 (same signature and layout)."""
+    """Drop-in for spectrax/_simulation.py:55-111 (same signature and layout).
+    A torch state that requires grad goes through ``RHSFunction`` (reverse and
+    forward mode on the GPU)."""
     del t
     pb = problem_from_args(Nx, Ny, Nz, Nn, Nm, Np, Ns, args, mask_mode or get_mask_mode())
     plan = get_plan(pb)
     y, kind = _as_cuda_state(Ck_Fk, plan.device)
-    dy = plan.rhs(y)
+    dy = _apply_rhs(plan, y)
     if kind == "numpy":
         return dy.cpu().numpy()
     if kind == "torch_cpu":
@@ -257,7 +296,7 @@ def rhs(t, y, params, mask_mode=None):
     del t
     plan = plan_for_params(params, mask_mode)
     yy, kind = _as_cuda_state(y, plan.device)
-    dy = plan.rhs(yy)
+    dy = _apply_rhs(plan, yy)
     if kind == "numpy":
         return dy.cpu().numpy()
     if kind == "torch_cpu":
