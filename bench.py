@@ -465,6 +465,8 @@ def run_ours(args):
     from spectrax_gb300.vector_field import plan_for_params
 
     p, y0 = two_stream_params(seed=rank)
+    from spectrax_gb300.vector_field import set_product_grid
+    set_product_grid(args.product_grid)
     if args.tile > 0:
         # a fixed plan (e.g. the autotuner's earlier choice, for profiling runs)
         from spectrax_gb300.vector_field import get_plan, problem_from_params
@@ -530,7 +532,7 @@ def run_ours(args):
     launch_ms = ms_per_step / 13.0
     # algorithmic bytes of an average stage launch (the save launch is empty between saves)
     bytes_launch = perf.dopri8_vectors_per_step() * n * 16 / 13.0
-    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile))
+    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile), plan.product_grid)
     # FP64 work of a step: 13 RHS + the Runge-Kutta combinations (4 flops per complex FMA)
     flops_step = 13.0 * ops.flops + 4.0 * perf.dopri8_combination_fmas_per_entry() * n
     achieved_gbs = bytes_launch / (launch_ms * 1e-3) / 1e9
@@ -542,7 +544,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "step": "one Dopri8 step attempt (13 fused RHS stages with the controller in the last, save)",
                    "state_len": n, "l2": "flushed (256 MB write) before every timed step",
-                   "tile": plan.tile, "threads": plan.threads,
+                   "tile": plan.tile, "threads": plan.threads, "product_grid": plan.product_grid,
                    "parallelism": "replicas" if world > 1 else "single"},
         "accepted_steps_per_s": acc_all / (t_ms * 1e-3),
         "e2e": {"value": e2e_evals_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 16,
@@ -554,10 +556,10 @@ def run_ours(args):
                      "kernel": "k_d8_stage_1v (duration = step time / 13)"},
         "fp64": {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
                  "frac": achieved_tf / fp64_peak, "peak_source": "live FMA probe (spx_probe_fp64)",
-                 "note": "FP64 work of the complex-transform formulation of the step (pruned transforms, "
-                         "products, streaming, stage combinations) per unit time; the packed real transforms "
-                         "used for this exactly Hermitian state execute fewer instructions (ncu: 6.7 M FP64 "
-                         "instructions per stage launch). FP64 issue is the binding ceiling of this path on GB300"},
+                 "note": "FP64 work of the complex-transform formulation of the step (pruned transforms on "
+                         "the plan's product grid, products, streaming, stage combinations) per unit time; the "
+                         "packed real transforms used for this exactly Hermitian state execute fewer instructions. "
+                         "FP64 issue is the binding ceiling of this path on GB300"},
         "clocks": clk.summary(),
     }
     if world == 1:
@@ -585,6 +587,8 @@ def main():
     ap.add_argument("--scan-t1", type=float, default=4.0, help="horizon of the batched scan extra")
     ap.add_argument("--tile", type=int, default=0, help="Hermite planes per CTA (0: autotune)")
     ap.add_argument("--threads", type=int, default=256, help="CTA width when --tile is given")
+    ap.add_argument("--product-grid", default="auto", choices=["auto", "nx", "fp64"],
+                    help="grid of the stepper's nonlinear products (spx_set_product_grid)")
     ap.add_argument("--only-extra", default="", choices=["", "landau", "two_stream_run", "orszag_tang"],
                     help="run just this extra workload and print its JSON (for profiling)")
     args = ap.parse_args()

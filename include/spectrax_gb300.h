@@ -84,6 +84,22 @@ int spx_plan_destroy(spx_plan* plan);
 /* Launch shape chosen for a plan (any pointer may be NULL); path 0 = fused 1D1V, 1 = general. */
 int spx_plan_info(const spx_plan* plan, int32_t* tile, int32_t* ntiles, int32_t* threads, int32_t* path);
 
+/*
+ * Grid of the nonlinear products in the 1D1V Dopri8 stage kernels (the device
+ * stepper and the adjoint's recomputation; the batch keeps Nx points).  The masked factors hold
+ * |k| <= K, so the kept modes of their product are exact on any grid of
+ * M >= 3K + 1 points (adding back the one term the reference's Nx-point grid
+ * folds onto |k| = K when Nx = 3K).  For plans created afterwards: mode 0
+ * (default) uses such a grid where its transforms are modeled >= 2x cheaper
+ * than Nx-point ones (prime Nx: 97 -> 104, 127 -> 128, 251 -> 256); mode 1 always Nx
+ * points; mode 2 the cheapest grid of <= 0.8x the modeled FP64 work without an
+ * extra Stockham stage (129 -> 136, 65 -> 64; measured slower than Nx on the
+ * two-stream stage kernel).  Results agree to rounding.  spx_plan_product_grid
+ * returns the grid length M of a plan.
+ */
+int spx_set_product_grid(int32_t mode);
+int spx_plan_product_grid(const spx_plan* plan);
+
 /* Number of complex128 entries of the flat state (N_C + N_F). */
 int64_t spx_state_len(const spx_problem* pb);
 
@@ -254,8 +270,8 @@ typedef struct spx_dopri8_opts {
                            The symmetry is then kept exactly by every stage.  0: never. */
   int32_t persistent; /* 1: on the fused 1D1V path, run all attempts of a replay in one
                            cooperative launch whose CTAs chain stages through completion
-                           counters (used when every CTA fits on the GPU at once);
-                           0: one launch per stage. */
+                           counters (used when every CTA fits on the GPU at once and the
+                           plan's product grid is Nx points); 0: one launch per stage. */
 } spx_dopri8_opts;
 
 typedef struct spx_dopri8 spx_dopri8;   /* opaque: stage buffers + CUDA graph */

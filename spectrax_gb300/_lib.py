@@ -101,6 +101,8 @@ _PROTOS = {
                                 C.POINTER(C.c_int32)]),
     "spx_state_len": (C.c_int64, [C.POINTER(spx_problem)]),
     "spx_rhs_workspace_bytes": (C.c_size_t, [_VP]),
+    "spx_set_product_grid": (C.c_int, [C.c_int32]),
+    "spx_plan_product_grid": (C.c_int, [_VP]),
     "spx_rhs": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_jvp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_linearize_bytes": (C.c_size_t, [_VP]),

@@ -52,6 +52,15 @@ __host__ __device__ __forceinline__ int lines_1v(int T, int Ns) {
   return (4 * (T + 1) > 2 * Ns + 6) ? 4 * (T + 1) : 2 * Ns + 6;
 }
 
+// Shared memory (double2 entries, after the table) of the staged 1D1V stage
+// kernel for tiles of T planes, Nx = N and product grid M: transform lines sA,
+// sB ((T+1)*M each), staged planes U ((T+2)*N), field lines F3 (3*N); the field
+// CTA reuses the area for its (2*Ns+12)*N gather and output lines.
+__host__ __device__ __forceinline__ int stage_area_1v(int T, int Ns, int N, int M) {
+  const int a = 2 * (T + 1) * M + (T + 2) * N + 3 * N, b = (2 * Ns + 12) * N;
+  return a > b ? a : b;
+}
+
 // Everything a kernel needs about one problem; lives in device memory next to
 // the double2 table it indexes.
 struct DevPlan {
@@ -73,6 +82,16 @@ struct DevPlan {
   double ua[SPX_MAX_SPECIES];   // u_x / alpha_x per species
   double iO0;                   // 1 / Omega_c of species 0
   const void* gen;              // general path: per-plane constants (GenPlane[Ns * nh]), device memory
+  // Fused 1D1V stepper: the grid of the real-space products G * C_{n-1}.  Both
+  // factors are masked to |k| <= K (K = ax[1].cut), so on any grid of M >= 3K+1
+  // points the kept output modes come out without wrap-around.  axm is such a
+  // grid when one is cheaper to transform than Nx (a copy of ax[1] otherwise);
+  // rnm = Nx / M rescales the 1/Nx of coef_1v; alias = 1 when M != Nx and
+  // Nx == 3K: the reference's Nx-point products then fold the k = +-2K term
+  // C_{+-K} G_{+-K} onto -+K, which the stepper adds back.
+  AxisPlan axm;
+  double rnm;
+  int alias;
 };
 
 // Coefficients of Hermite plane n of species s on the fused 1D1V path:

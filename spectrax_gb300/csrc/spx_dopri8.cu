@@ -278,7 +278,9 @@ __device__ void fill_terms(EpiTerms& T, int stage, double h) {
 // One stage of the fused 1D1V path (staged_stage_1v): stage inputs and
 // epilogue operands arrive by bulk copies; the last stage (LAST) forms y_new
 // and the error and runs the controller in its last CTA.
-template <bool LAST>
+// MG: the plan's products run on its own product grid (axm.n != Nx); one
+// kernel per case so the Nx-grid kernel keeps its smaller register allocation
+template <bool LAST, bool MG>
 __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage) {
   __shared__ DevPlan P;
   __shared__ D8Dev s;
@@ -339,7 +341,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_stage_1v(D8Args a, int stage
   io.adaptive = s.adaptive;
   io.timeout_status = &a.st->status;
   io.persistent = false;
-  staged_stage_1v<LAST>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
+  staged_stage_1v<LAST, 2, MG ? 1 : 0>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
 }
 
 // ------------------------------------------------------------------ persistent 1D1V solver
@@ -482,8 +484,8 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_persist(D8Args a, int natt) 
         io.persistent = true;
         const bool ok_stage =
             (stage < rk::S - 1)
-                ? staged_stage_1v<false>(P, stab, io, terms, bars, [](auto&) {})
-                : staged_stage_1v<true>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
+                ? staged_stage_1v<false, 2, 0>(P, stab, io, terms, bars, [](auto&) {})
+                : staged_stage_1v<true, 2, 0>(P, stab, io, terms, bars, [&](auto& el) { last_stage_tail(a, at, el, red); });
         if (!ok_stage) return;   // status already says WAIT_TIMEOUT; the CTAs waiting on this one time out too
       }
       // this stage's writes (generic proxy) are read by later bulk copies (async proxy)
@@ -750,10 +752,14 @@ static int d8_attrs() {
   if (done) return SPX_OK;
   const int optin = smem_optin();
   cudaFuncAttributes fa;
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<false>));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>));
-  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<false, false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true, false>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<false, true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_stage_1v<true, true>));
+  SPX_CUDA(cudaFuncSetAttribute(k_d8_stage_1v<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_persist));
   SPX_CUDA(cudaFuncSetAttribute(k_d8_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_d8_real));
@@ -786,10 +792,10 @@ static void enqueue_attempt(spx_dopri8* s, cudaStream_t st) {
   const DevPlan& P = s->plan->host;
   for (int stage = 0; stage < rk::S; ++stage) {
     if (P.path == 0) {
-      if (stage < rk::S - 1)
-        launch_pdl(k_d8_stage_1v<false>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
-      else
-        launch_pdl(k_d8_stage_1v<true>, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
+      const bool mg = P.axm.n != P.ax[1].n;
+      auto k = stage < rk::S - 1 ? (mg ? k_d8_stage_1v<false, true> : k_d8_stage_1v<false, false>)
+                                 : (mg ? k_d8_stage_1v<true, true> : k_d8_stage_1v<true, false>);
+      launch_pdl(k, s->grid_stage, s->plan->threads, s->smem_stage, st, s->args, stage);
     } else {
       launch_pdl(k_d8_real, s->grid_real, GEN_THREADS, s->plan->smem_gen, st, s->args, stage);
       if (stage < rk::S - 1)
@@ -845,12 +851,13 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
     // stage kernel shared memory: table + line buffers + coefficients + staged
     // epilogue operands (as many as keep two CTAs per SM resident, at least y)
     cudaFuncAttributes fa;
-    cudaError_t ea = cudaFuncGetAttributes(&fa, k_d8_stage_1v<true>);
+    cudaError_t ea = cudaFuncGetAttributes(&fa, k_d8_stage_1v<true, false>);
     if (ea != cudaSuccess) { delete s; return cuda_fail(ea, "cudaFuncGetAttributes"); }
     s->smem_stage = stage_smem_1v(plan, fa.sharedSizeBytes, &npf);
     if (npf < 1) { delete s; set_error("Nx / tile too large for the Dopri8 stage kernel"); return SPX_E_UNSUPPORTED; }
-    if (o->persistent) {
-      // the persistent kernel needs every CTA resident at once (a cooperative launch)
+    if (o->persistent && P.axm.n == P.ax[1].n) {
+      // the persistent kernel needs every CTA resident at once (a cooperative launch);
+      // it is compiled for the Nx-point product grid only (its register budget)
       int coop = 0, per_sm = 0;
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, plan->device);
       cudaFuncAttributes fp;

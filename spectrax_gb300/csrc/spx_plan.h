@@ -28,7 +28,9 @@ namespace spx {
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 // Fill `pl` (everything but the device pointers) from a problem; returns SPX_OK or an error code.
-int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile = 0);
+// mgrid (fused 1D1V path): 0 = products on the Nx-point grid, 1 = the stepper's
+// product grid may be any cheaper length, 2 = only one no longer than Nx.
+int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile = 0, int mgrid = 1);
 // Launch helpers used by several entry points.
 int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, cudaStream_t st);
 // Opt-in shared memory per block of the current device (0 on failure).

@@ -49,19 +49,22 @@ static std::vector<int> factorize(int n) {
   return r;
 }
 
-static int build_axis(int n, int cut, double L, std::vector<double2>& tab, AxisPlan& ap) {
+// rads: the Stockham radices in stage order (default: factorize(n)); ktable:
+// append the axis' k table (not needed by a transform-only axis).
+static int build_axis(int n, int cut, double L, std::vector<double2>& tab, AxisPlan& ap,
+                      const std::vector<int>* rads = nullptr, bool ktable = true) {
   std::memset(&ap, 0, sizeof(ap));
   ap.n = n;
   ap.cut = cut;
   const int fl = -((n + 1) / 2);     // floor(-n/2)
   ap.koff = fl + 1;
   ap.kofs = (int)tab.size();
-  for (int c = 0; c < n; ++c) {
+  for (int c = 0; ktable && c < n; ++c) {
     const double k = (double)(2 * (c + ap.koff)) * M_PI;
     tab.push_back(make_double2(k / L, k));
   }
   if (n == 1) { ap.nst = 0; return SPX_OK; }
-  std::vector<int> rad = factorize(n);
+  std::vector<int> rad = rads ? *rads : factorize(n);
   if ((int)rad.size() > MAXST) { set_error("FFT length has too many factors"); return SPX_E_UNSUPPORTED; }
   ap.nst = (int)rad.size();
   std::map<int, int> cs_of;
@@ -98,7 +101,93 @@ static int build_axis(int n, int cut, double L, std::vector<double2>& tab, AxisP
   return SPX_OK;
 }
 
-int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
+// FP64 instructions of one masked inverse (input-pruned) plus one forward
+// (output-pruned) transform of a line of length n with radices `rads`: the
+// count the Stockham stages of spx_core.cuh issue (twiddles, register
+// butterflies for 2/3/4/8, the two-phase symmetric DFT for other odd radices,
+// pruned at the stage next to the masked side).
+static double line_pair_cost(int n, const std::vector<int>& rads, int cut) {
+  double total = 0.0;
+  for (int dif = 0; dif < 2; ++dif) {
+    int Ns = 1;
+    for (size_t si = 0; si < rads.size(); ++si) {
+      const int R = rads[si], M = n / R;
+      const double tw_tasks = Ns > 1 ? (double)(M - M / Ns) : 0.0;
+      if (R == 2 || R == 3 || R == 4 || R == 8) {
+        total += tw_tasks * 4.0 * (R - 1);
+        total += (double)M * (R == 2 ? 4 : R == 3 ? 12 : R == 4 ? 16 : 56);
+      } else {
+        const int h = (R - 1) / 2;
+        total += tw_tasks * h * 8.0;
+        double pairs = 0.0, outs = 0.0;
+        for (int j = 0; j < M; ++j) {
+          const int q = si == 0 ? std::min(h, (cut + j) / M) : h;
+          if (!dif) { pairs += q; outs += (4.0 * q + 4.0) * (h + 1); }
+          else { pairs += h; outs += (4.0 * h + 4.0) * (q + 1); }
+        }
+        total += 4.0 * pairs + outs;
+      }
+      Ns *= R;
+    }
+  }
+  return total;
+}
+
+// Radix orders tried for a product-grid length m: the default factorisation,
+// and with two factors 3 merged into one odd radix 9 placed first (fewer
+// stages; the first stage is the one the mask prunes).
+static std::vector<std::vector<int>> radix_orders(int m) {
+  std::vector<std::vector<int>> out{factorize(m)};
+  std::vector<int> f = factorize(m);
+  int threes = (int)std::count(f.begin(), f.end(), 3);
+  if (threes >= 2) {
+    std::vector<int> g{9};
+    int skip = 2;
+    for (int r : f) {
+      if (r == 3 && skip > 0) { --skip; continue; }
+      g.push_back(r);
+    }
+    out.push_back(g);
+  }
+  if (m == 16) out.push_back({4, 4});
+  return out;
+}
+
+// 0: a product grid only where it is modeled >= 2x cheaper; 1: always Nx;
+// 2: the cheapest modeled grid at <= 0.8x without an extra stage
+static int g_product_grid = 0;
+
+// Product grid of the fused 1D1V stepper for an axis of n points and mask cut
+// K: the cheapest length m >= 3K+1 (m <= n when max_n) with radices 2, 4, 8 or
+// odd up to 31, by line_pair_cost.  Mode 0 keeps it only at <= 0.5 of the
+// n-point cost (prime n and the like): measured on the two-stream stage kernel
+// (Nx = 129), grids of 0.67x the FP64 work (144 = 9*8*2, 136 = 17*8) ran
+// 1.5-4 % slower than the 43*3 transform, each point and Stockham pass costing
+// shared-memory traffic and barriers the count does not see.  Mode 2 keeps it
+// at <= 0.8 with no more stages than n.  Returns m == n (and rads empty) otherwise.
+static int choose_product_grid(int n, int cut, bool max_n, std::vector<int>& rads) {
+  rads.clear();
+  if (g_product_grid == 1 || cut < 1 || n < 8) return n;
+  const std::vector<int> fn = factorize(n);
+  const double base = line_pair_cost(n, fn, cut);
+  double best = (g_product_grid == 2 ? 0.8 : 0.5) * base;
+  int bm = n;
+  for (int m = 3 * cut + 1; m <= 2 * n; ++m) {
+    if (m == n || (max_n && m > n)) continue;
+    const std::vector<int> f = factorize(m);
+    bool small = (int)f.size() <= MAXST;
+    for (int r : f) small = small && (r <= 8 || ((r & 1) && r <= 31));
+    if (!small) continue;
+    for (const auto& o : radix_orders(m)) {
+      const double c = line_pair_cost(m, o, cut);
+      if ((int)o.size() > (int)fn.size() && c > 0.5 * base) continue;
+      if (c < best) { best = c; bm = m; rads = o; }
+    }
+  }
+  return bm;
+}
+
+int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile, int mgrid) {
   if (!pb) { set_error("null problem"); return SPX_E_ARG; }
   const spx_problem& p = *pb;
   if (p.Nx < 1 || p.Ny < 1 || p.Nz < 1 || p.Nn < 1 || p.Nm < 1 || p.Np < 1 || p.Ns < 1) {
@@ -151,6 +240,29 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile) {
     T = (p.Nn + ntiles - 1) / ntiles;   // even out the tiles
     P.tile = T;
     P.ntiles = ntiles;
+    // product grid of the stepper (axm); its twiddles extend the table
+    P.axm = P.ax[1];
+    P.rnm = 1.0;
+    P.alias = 0;
+    std::vector<int> mr;
+    const int M = mgrid ? choose_product_grid(N, p.cut_x, mgrid == 2, mr) : N;
+    if (M != N) {
+      std::vector<double2> tab2 = pl->tab;
+      AxisPlan am;
+      if ((rc = build_axis(M, p.cut_x, p.Lx, tab2, am, &mr, false)) != SPX_OK) return rc;
+      const size_t tab2_bytes = (tab2.size() * sizeof(double2) + 255) / 256 * 256;
+      // the staged stage kernel must still fit with one staged epilogue operand
+      const size_t stage = tab2_bytes + (size_t)stage_area_1v(T, p.Ns, N, M) * sizeof(double2) +
+                           64 * sizeof(double) + (size_t)T * N * sizeof(double2);
+      if (stage <= smem_max) {
+        pl->tab.swap(tab2);
+        P.tab_len = (int)pl->tab.size();
+        pl->smem_tab = tab2_bytes;
+        P.axm = am;
+        P.rnm = (double)N / (double)M;
+        P.alias = (3 * p.cut_x == N) ? 1 : 0;
+      }
+    }
     pl->smem_1v = pl->smem_tab + (size_t)lines_1v(T, p.Ns) * N * sizeof(double2) + 16 * 4 * sizeof(double);
     // the VJP keeps one partial field line per (species, tile); the fused
     // VJP + parameter kernel adds per-CTA parameter partials and one partial
@@ -596,6 +708,14 @@ int spx_plan_destroy(spx_plan* pl) {
   delete pl;
   return SPX_OK;
 }
+
+int spx_set_product_grid(int32_t mode) {
+  if (mode < 0 || mode > 2) { set_error("spx_set_product_grid: mode must be 0 (auto), 1 (Nx) or 2 (least FP64)"); return SPX_E_ARG; }
+  g_product_grid = mode;
+  return SPX_OK;
+}
+
+int spx_plan_product_grid(const spx_plan* pl) { return pl ? pl->host.axm.n : 0; }
 
 size_t spx_rhs_workspace_bytes(const spx_plan* pl) { return pl ? pl->ws_bytes : 0; }
 

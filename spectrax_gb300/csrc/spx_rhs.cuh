@@ -150,11 +150,15 @@ __device__ __forceinline__ void rhs1v_tile(const DevPlan& P, const double2* __re
 // trajectory.
 // sA / sB: (nt+1)*N double2 each; scoef: 4*nt doubles.
 // ------------------------------------------------------------------------
-template <bool HERM, class Epi>
+template <bool HERM, bool MG, class Epi>
 __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, int s, int n0, int nt,
                              const double2* U, const double2* F3, double2* sA, double2* sB,
                              double* scoef, Epi& epi) {
   const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  // MG: products on the grid axm of Lm points (mode k at position k mod Lm);
+  // otherwise on the Nx-point grid (positions std_index(c, N)), compiled apart
+  const AxisPlan& am = MG ? P.axm : P.ax[1];
+  const int Lm = MG ? am.n : N, half = N / 2;
   const size_t sbase = (size_t)s * Nn * N;
   const double a0 = P.pb.alpha_s[3 * s];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
@@ -163,7 +167,8 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
     double* c = scoef + 4 * threadIdx.x;
     const double* t = P.coef + ((size_t)s * Nn + n) * COEF_1V;
     // HERM: the 1/2 of the packed-spectrum split is folded into the coefficient (exact)
-    c[0] = t[0]; c[1] = t[1]; c[2] = HERM ? 0.5 * t[2] : t[2]; c[3] = t[3];
+    // rnm = N / Lm turns the 1/N of the table into the product grid's 1/Lm
+    c[0] = t[0]; c[1] = t[1]; c[2] = (HERM ? 0.5 * t[2] : t[2]) * (MG ? P.rnm : 1.0); c[3] = t[3];
   }
   // G = E_x + u_y B_z - u_z B_y at centred index c (masked)
   auto G = [&](int c) {
@@ -175,55 +180,58 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
   double2* f;                           // forward transforms of the products
   if (!HERM) {
     // FFT lines: 0 = G, l + 1 = C_{n0+l-1} = U line l (masked, transform order)
-    for (int i = threadIdx.x; i < (nt + 1) * N; i += blockDim.x) {
-      const int l = i / N, c = i - l * N;
+    for (int i = threadIdx.x; i < (nt + 1) * Lm; i += blockDim.x) {
+      const int l = i / Lm, x = i - l * Lm;
+      const int k = x < (Lm + 1) / 2 ? x : x - Lm;
       double2 v = zero;
-      if (kept(c, N, cut)) v = (l == 0) ? G(c) : U[(l - 1) * N + c];
-      sA[l * N + std_index(c, N)] = v;
+      if (k >= -cut && k <= cut) v = (l == 0) ? G(k + half) : U[(l - 1) * N + k + half];
+      sA[i] = v;
     }
     __syncthreads();
-    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
+    double2* r = fft_axis_t<true, false>(sA, sB, am, tab, Lines{nt + 1, 1, 1, Lm, 0}, cut);
     double2* o = (r == sA) ? sB : sA;
-    for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-      const int x = i % N;
-      r[N + i] = cmul(r[x], r[N + i]);
+    for (int i = threadIdx.x; i < nt * Lm; i += blockDim.x) {
+      const int x = i % Lm;
+      r[Lm + i] = cmul(r[x], r[Lm + i]);
     }
     __syncthreads();
-    f = fft_axis_t<false, true>(r + N, o + N, P.ax[1], tab, Lines{nt, 1, 1, N, 0}, cut);
+    f = fft_axis_t<false, true>(r + Lm, o + Lm, am, tab, Lines{nt, 1, 1, Lm, 0}, cut);
   } else {
     const int nreal = nt + 1;             // real lines: 0 = G, q + 1 = C_{n0+q-1} = U line q
     const int nin = (nreal + 1) / 2;      // packed inverse transforms
     const int nout = (nt + 1) / 2;        // packed forward transforms
-    for (int i = threadIdx.x; i < nin * N; i += blockDim.x) {
-      const int j = i / N, c = i - j * N;
+    for (int i = threadIdx.x; i < nin * Lm; i += blockDim.x) {
+      const int j = i / Lm, x = i - j * Lm;
+      const int k = x < (Lm + 1) / 2 ? x : x - Lm;
       double2 z = zero;
-      if (kept(c, N, cut)) {
+      if (k >= -cut && k <= cut) {
+        const int c = k + half;
         const int la = 2 * j, lb = 2 * j + 1;
         const double2 xa = la == 0 ? G(c) : U[(la - 1) * N + c];
         const double2 xb = lb < nreal ? U[(lb - 1) * N + c] : zero;
         z = make_double2(xa.x - xb.y, xa.y + xb.x);
       }
-      sA[j * N + std_index(c, N)] = z;
+      sA[i] = z;
     }
     __syncthreads();
-    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nin, 1, 1, N, 0}, cut);
+    double2* r = fft_axis_t<true, false>(sA, sB, am, tab, Lines{nin, 1, 1, Lm, 0}, cut);
     double2* o = (r == sA) ? sB : sA;
     // real-space products p_q = G * C_{n0+q-1}, packed in pairs into o
-    for (int i = threadIdx.x; i < nout * N; i += blockDim.x) {
-      const int j = i / N, x = i - j * N;
+    for (int i = threadIdx.x; i < nout * Lm; i += blockDim.x) {
+      const int j = i / Lm, x = i - j * Lm;
       const double g = r[x].x;
       const int qa = 2 * j, qb = 2 * j + 1;      // real lines qa + 1, qb + 1
-      const double2 za = r[((qa + 1) >> 1) * N + x];
+      const double2 za = r[((qa + 1) >> 1) * Lm + x];
       const double ca = ((qa + 1) & 1) ? za.y : za.x;
       double cb = 0.0;
       if (qb < nt) {
-        const double2 zb = r[((qb + 1) >> 1) * N + x];
+        const double2 zb = r[((qb + 1) >> 1) * Lm + x];
         cb = ((qb + 1) & 1) ? zb.y : zb.x;
       }
-      o[j * N + x] = make_double2(g * ca, g * cb);
+      o[j * Lm + x] = make_double2(g * ca, g * cb);
     }
     __syncthreads();
-    f = fft_axis_t<false, true>(o, r, P.ax[1], tab, Lines{nout, 1, 1, N, 0}, cut);
+    f = fft_axis_t<false, true>(o, r, am, tab, Lines{nout, 1, 1, Lm, 0}, cut);
   }
   // the epilogue's own staged operands (called by every thread; false: give up)
   if (!epi.prepare()) return;
@@ -248,13 +256,21 @@ __device__ void rhs1v_tile_u(const DevPlan& P, const double2* __restrict__ tab, 
     double im = fma(-w, t.x, -d * C0.y);
     if (n >= 1 && kept(c, N, cut)) {
       double2 nl2;
+      const int kk = c - half;
+      const int px = kk < 0 ? kk + Lm : kk;       // grid position of mode kk
       if (!HERM) {
-        nl2 = f[l * N + std_index(c, N)];
+        nl2 = f[l * Lm + px];
       } else {
-        const double2* fl = f + (l >> 1) * N;
-        const double2 W = fl[std_index(c, N)], Wm = fl[std_index(N - 1 - c, N)];
+        const double2* fl = f + (l >> 1) * Lm;
+        const double2 W = fl[px], Wm = fl[kk > 0 ? Lm - kk : -kk];
         if ((l & 1) == 0) nl2 = make_double2(W.x + Wm.x, W.y - Wm.y);
         else nl2 = make_double2(W.y + Wm.y, Wm.x - W.x);
+      }
+      if (MG && P.alias && (kk == cut || kk == -cut)) {
+        // the Nx-point products fold k1 = k2 = -kk (sum -2kk = kk -+ Nx) onto kk:
+        // add G_{-kk} C_{-kk}, in the units of the transform output (x Lm, x 2 packed)
+        const int cc = half - kk;
+        nl2 = cfma(cscale(HERM ? 2.0 * Lm : (double)Lm, G(cc)), U[l * N + cc], nl2);
       }
       re = fma(cf[2], nl2.x, re);
       im = fma(cf[2], nl2.y, im);

@@ -10,6 +10,7 @@
 // scaled error on the last stage).  The field CTA gathers its few lines with
 // plain loads.  Every wait is bounded; a wait that gives up sets *timeout_status.
 #pragma once
+#include <type_traits>
 #include <algorithm>
 
 #include "spx_plan.h"
@@ -173,14 +174,10 @@ struct EpiFinal {
 };
 
 // Shared-memory layout of the fused 1D1V stage kernel after the table (double2
-// units, all 16-byte aligned):
-//   sA, sB : (T+1)*N each   U : (T+2)*N   F3 : 3*N   (the field CTA reuses
-//   sA.. as its (2*Ns+12)*N gather + output area)   scoef : 64 doubles
-//   pf     : npf * T * N   (y and K_j of the CTA's own planes)
-__host__ __device__ __forceinline__ int stage_lines_1v(int T, int Ns) {
-  const int a = 2 * (T + 1) + (T + 2) + 3, b = 2 * Ns + 12;
-  return a > b ? a : b;
-}
+// units, all 16-byte aligned): stage_area_1v(T, Ns, N, M) entries, i.e.
+//   sA, sB : (T+1)*M each (M = the product grid axm.n)   U : (T+2)*N   F3 : 3*N
+//   (the field CTA reuses the area as its (2*Ns+12)*N gather + output lines),
+// then scoef : 64 doubles, then pf : npf * T * N (y and K_j of the CTA's own planes).
 
 // Dynamic shared memory of a staged stage kernel for `plan` and the number of
 // epilogue operands (y first, then K_j) staged: as many as keep two CTAs per SM
@@ -188,7 +185,8 @@ __host__ __device__ __forceinline__ int stage_lines_1v(int T, int Ns) {
 inline size_t stage_smem_1v(const spx_plan* plan, size_t static_smem, int* npf_out) {
   const DevPlan& P = plan->host;
   const int T = P.tile, N = P.ax[1].n;
-  const size_t base = plan->smem_tab + (size_t)stage_lines_1v(T, P.pb.Ns) * N * sizeof(double2) + 64 * sizeof(double);
+  const size_t base = plan->smem_tab + (size_t)stage_area_1v(T, P.pb.Ns, N, P.axm.n) * sizeof(double2) +
+                      64 * sizeof(double);
   const size_t per = (size_t)T * N * sizeof(double2);
   const size_t two_per_sm = 228 * 1024 / 2 - 1024 - static_smem;
   const size_t optin = (size_t)smem_optin() - static_smem;
@@ -226,8 +224,10 @@ struct SrcL2 {
 // caller's shared scratch.  LAST: `tail(el)` is called by every thread of every
 // CTA with the stage's EpiFinal (or an empty accumulator) for the error reduction.
 // HM: 0 general transforms only, 1 packed transforms only, 2 chosen by io.herm
-// at run time (both variants compiled into the caller).
-template <bool LAST, int HM = 2, class Tail>
+// at run time (both variants compiled into the caller).  MGS: 0 products on the
+// Nx-point grid only, 1 on the plan's product grid only, 2 chosen at run time
+// (a kernel holding both variants takes the larger register allocation).
+template <bool LAST, int HM = 2, int MGS = 2, class Tail>
 __device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ stab, const StageIO& io,
                                 const EpiTerms& terms, uint64_t* bars, Tail&& tail) {
   const long long len = io.len;
@@ -235,7 +235,8 @@ __device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
   const int N = P.ax[1].n, T = P.tile, Nn = P.pb.Nn;
   const int b = blockIdx.x;
   double2* sA = const_cast<double2*>(stab) + (P.tab_len + 15) / 16 * 16;
-  double* scoef = reinterpret_cast<double*>(sA + (size_t)stage_lines_1v(T, P.pb.Ns) * N);
+  const int Lm = P.axm.n;
+  double* scoef = reinterpret_cast<double*>(sA + (size_t)stage_area_1v(T, P.pb.Ns, N, Lm));
   double2* pf = reinterpret_cast<double2*>(scoef + 64);
   if (b == nblk) {
     // field CTA: plain gather (one CTA, small) and global epilogue operands
@@ -261,8 +262,8 @@ __device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
     }
     return true;
   }
-  double2* sB = sA + (size_t)(T + 1) * N;
-  double2* U = sB + (size_t)(T + 1) * N;
+  double2* sB = sA + (size_t)(T + 1) * Lm;
+  double2* U = sB + (size_t)(T + 1) * Lm;
   double2* F3 = U + (size_t)(T + 2) * N;
   const size_t sbase = (size_t)sp * Nn * N;
   const int own = nt * N;
@@ -305,15 +306,26 @@ __device__ bool staged_stage_1v(const DevPlan& P, const double2* __restrict__ st
     }
     return false;
   }
+  // the product-grid variant only where the plan has one (a uniform branch)
+  const bool mg = Lm != N;
+  auto tile_g = [&](auto mgc, auto& epi) {
+    constexpr bool G = decltype(mgc)::value;
+    if (HM == 1 || (HM == 2 && io.herm)) rhs1v_tile_u<HM != 0, G>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
+    else rhs1v_tile_u<false, G>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
+  };
+  auto tile = [&](auto& epi) {
+    if constexpr (MGS == 0) tile_g(std::false_type{}, epi);
+    else if constexpr (MGS == 1) tile_g(std::true_type{}, epi);
+    else if (mg) tile_g(std::true_type{}, epi);
+    else tile_g(std::false_type{}, epi);
+  };
   if constexpr (!LAST) {
     EpiNext epi{io.Ki, io.out, io.Y, io.K, len, &terms, pf, own, npf, &bars[1]};
-    if (HM == 1 || (HM == 2 && io.herm)) rhs1v_tile_u<HM != 0>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
-    else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, epi);
+    tile(epi);
   } else {
     EpiFinal el{io.Ki, io.out, io.Y, io.K, len, &terms, pf, own, npf, &bars[1],
                 io.rtol, io.atol, io.adaptive, 0.0, 0, make_double2(0.0, 0.0), 0.0};
-    if (HM == 1 || (HM == 2 && io.herm)) rhs1v_tile_u<HM != 0>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
-    else rhs1v_tile_u<false>(P, stab, sp, n0, nt, U, F3, sA, sB, scoef, el);
+    tile(el);
     tail(el);
   }
   // a failed prepare() returns from the tile early: record it once

@@ -57,7 +57,25 @@ class Ops:
         self.flops += mult * (2 * fma + addmul)
 
 
-def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit") -> Ops:
+def radix_orders(m: int):
+    """Radix orders the plan builder tries for a product-grid length m (csrc/spx_rhs.cu):
+    the default factorisation, two 3s merged into a leading 9, and 4 x 4 for 16."""
+    f = factorize(m)
+    out = [f]
+    if f.count(3) >= 2:
+        g, skip = [9], 2
+        for r in f:
+            if r == 3 and skip > 0:
+                skip -= 1
+                continue
+            g.append(r)
+        out.append(g)
+    if m == 16:
+        out.append([4, 4])
+    return out
+
+
+def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit", radices=None) -> Ops:
     """FP64 work of one length-n line through the Stockham engine.
 
     cut (the 2/3-mask cutoff) prunes the first decimation-in-time stage (masked
@@ -67,7 +85,7 @@ def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit") -> Ops:
     if n == 1:
         return o
     Ns = 1
-    for si, R in enumerate(factorize(n)):
+    for si, R in enumerate(radices or factorize(n)):
         M = n // R
         tw_tasks = (M - M // Ns) if Ns > 1 else 0
         if R % 2 == 0 or R == 3:
@@ -91,20 +109,28 @@ def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit") -> Ops:
     return o
 
 
-def rhs_ops(shape, tile=None, ntiles=None) -> Ops:
-    """FP64 work of one right-hand-side evaluation (fused 1D1V or general path)."""
+def rhs_ops(shape, tile=None, ntiles=None, product_grid=None) -> Ops:
+    """FP64 work of one right-hand-side evaluation (fused 1D1V or general path).
+    product_grid: length of the 1D1V products' grid (the plan's; default Nx),
+    transformed with the cheapest radix order the plan builder tries."""
     Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
     o = Ops()
     plane = Nx * Ny * Nz
     if Ny == 1 and Nz == 1 and Nm == 1 and Np == 1:
         cut = Nx // 3
-        fi, ff = fft_line_ops(Nx, cut, "dit"), fft_line_ops(Nx, cut, "dif")
+        M = product_grid or Nx
+        if M == Nx:
+            rad = factorize(Nx)
+        else:
+            rad = min(radix_orders(M), key=lambda r: fft_line_ops(M, cut, "dit", r).instr +
+                      fft_line_ops(M, cut, "dif", r).instr)
+        fi, ff = fft_line_ops(M, cut, "dit", rad), fft_line_ops(M, cut, "dif", rad)
         ntiles = ntiles or 1
         lines_inv = Ns * (Nn + ntiles)          # C_{n-1} per plane + one G per tile
         lines_fwd = Ns * Nn
         o.instr += fi.instr * lines_inv + ff.instr * lines_fwd
         o.flops += fi.flops * lines_inv + ff.flops * lines_fwd
-        o.add(fma=2, addmul=2, mult=Ns * Nn * Nx)            # G * C
+        o.add(fma=2, addmul=2, mult=Ns * Nn * M)             # G * C
         o.add(fma=6, addmul=4, mult=Ns * Nn * Nx)            # streaming, damping, NL add
         o.add(fma=4, addmul=2, mult=Ns * Nx)                 # G combination
         o.add(fma=8 * Ns + 6, addmul=24, mult=Nx)            # Maxwell + current

@@ -44,6 +44,7 @@ class Plan:
         t, nt, th, path = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         _lib.check(L.spx_plan_info(h, C.byref(t), C.byref(nt), C.byref(th), C.byref(path)), "spx_plan_info")
         self.tile, self.ntiles, self.threads, self.path = t.value, nt.value, th.value, path.value
+        self.product_grid = int(L.spx_plan_product_grid(h))
 
     @property
     def shape(self):
@@ -150,9 +151,31 @@ class Plan:
             self.handle = None
 
 
+_product_grid = "auto"
+
+
+_GRID_MODES = {"auto": 0, "nx": 1, "fp64": 2}
+
+
+def set_product_grid(mode: str) -> None:
+    """Grid of the nonlinear products in the 1D1V stepper kernels for plans made
+    from now on (spx_set_product_grid): "auto" (a grid of M >= 3K + 1 points
+    where its transforms are modeled >= 2x cheaper, e.g. prime Nx), "nx" (always
+    Nx points) or "fp64" (the least modeled FP64 work).  Results agree to rounding."""
+    global _product_grid
+    if mode not in _GRID_MODES:
+        raise ValueError("mode must be one of " + ", ".join(_GRID_MODES))
+    _lib.check(_lib.lib().spx_set_product_grid(_GRID_MODES[mode]), "spx_set_product_grid")
+    _product_grid = mode
+
+
+def get_product_grid() -> str:
+    return _product_grid
+
+
 def get_plan(problem: _lib.spx_problem, device=None, tile=0, threads=0) -> Plan:
     dev = torch.cuda.current_device() if device is None else device
-    key = (bytes(problem), dev, int(tile), int(threads))
+    key = (bytes(problem), dev, int(tile), int(threads), _product_grid)
     with _cache_lock:
         pl = _plan_cache.get(key)
         if pl is None:
@@ -176,7 +199,7 @@ def autotune(problem: _lib.spx_problem, device=None, reps=20, verbose=False, tar
     if target not in ("rhs", "dopri8"):
         raise ValueError("target must be 'rhs' or 'dopri8'")
     dev = torch.cuda.current_device() if device is None else device
-    key = (bytes(problem), dev, target, sample is not None)
+    key = (bytes(problem), dev, target, sample is not None, _product_grid)
     if key in _tuned:
         return _tuned[key]
     base = get_plan(problem, dev)
