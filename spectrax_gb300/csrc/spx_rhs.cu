@@ -295,9 +295,9 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile, int 
     std::memcpy(pl->gen.data() + (size_t)nplanes * sizeof(GenPlane), tr.data(),
                 (size_t)nplanes * sizeof(GenPlaneT));
     // real-space planes of y (RHS), of y and v (JVP); of y, the forward
-    // transforms of w and 6 Ns per-species field sums (VJP)
+    // transforms of w and 6 Ns partial field sums per chunk of planes (VJP)
     const size_t nreal = (size_t)p.Ns * P.nh + 3 * (size_t)p.Ns + 3;
-    const size_t nws = std::max(2 * nreal, nreal + (size_t)nplanes + 6 * (size_t)p.Ns);
+    const size_t nws = std::max(2 * nreal, nreal + (size_t)nplanes + 6 * (size_t)p.Ns * vjp_nchunk(P.nh));
     pl->ws_bytes = nws * P.plane * sizeof(double2);
   }
   if (pl->smem_1v > smem_max) { set_error("Nx too large for the fused path"); return SPX_E_UNSUPPORTED; }
@@ -530,8 +530,9 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_real(const DevPlan* __re
   else general_w_real(P, stab, w, b - nreal, ws + (size_t)b * P.plane, sA, sB);
 }
 
-// Pass 2: the per-species field sums, one thread per (point, species,
-// component): blockIdx.y = s * 6 + j, written to plane blockIdx.y of S.
+// Pass 2: the partial field sums, one thread per (point, species, component,
+// chunk of VJP_HCHUNK planes): blockIdx.y = s * 6 + j, blockIdx.z = chunk,
+// written to plane blockIdx.z * 6 Ns + blockIdx.y of S.
 __global__ void __launch_bounds__(NTHREADS) k_vjp_fsum(const DevPlan* __restrict__ gP,
                                                       const double2* __restrict__ ws,
                                                       double2* __restrict__ S) {
@@ -541,10 +542,11 @@ __global__ void __launch_bounds__(NTHREADS) k_vjp_fsum(const DevPlan* __restrict
   const int nreal = P.pb.Ns * P.nh + 3 * P.pb.Ns + 3;
   const double2* W = ws + (size_t)nreal * P.plane;
   const int s = blockIdx.y / 6, j = blockIdx.y % 6;
-  double2* out = S + (size_t)blockIdx.y * P.plane;
+  const int h0 = blockIdx.z * VJP_HCHUNK, h1 = min(P.nh, h0 + VJP_HCHUNK);
+  double2* out = S + ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * P.plane;
   for (size_t pt = blockIdx.x * (size_t)blockDim.x + threadIdx.x; pt < (size_t)P.plane;
        pt += (size_t)gridDim.x * blockDim.x)
-    out[pt] = vjp_field_sum(P, ws, W, pt, s, j);
+    out[pt] = vjp_field_sum(P, ws, W, pt, s, j, h0, h1);
 }
 
 // Pass 3: blocks [0, nplanes) the Hermite planes of g, then six field blocks.
@@ -835,7 +837,7 @@ int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws
   const DevPlan& P = pl->host;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (P.path != 0) {
-    // workspace: y's real planes (nreal), W (nplanes), 6 Ns per-species field sums
+    // workspace: y's real planes (nreal), W (nplanes), 6 Ns partial field sums per chunk
     const int nplanes = P.pb.Ns * P.nh;
     const int nreal = nplanes + 3 * P.pb.Ns + 3;
     const double2* yy = static_cast<const double2*>(y);
@@ -844,7 +846,7 @@ int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws
     double2* S = W + (size_t)(nreal + nplanes) * P.plane;
     k_vjp_real<<<nreal + nplanes, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, yy, ww, W);
     const int fx = (int)std::min<long long>((P.plane + NTHREADS - 1) / NTHREADS, 65535LL);
-    k_vjp_fsum<<<dim3(fx, 6 * P.pb.Ns), NTHREADS, 0, st>>>(pl->d_plan, W, S);
+    k_vjp_fsum<<<dim3(fx, 6 * P.pb.Ns, vjp_nchunk(P.nh)), NTHREADS, 0, st>>>(pl->d_plan, W, S);
     k_vjp_gen<<<nplanes + 6, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, ww, W, S,
                                                               static_cast<double2*>(g));
     SPX_CUDA(cudaGetLastError());

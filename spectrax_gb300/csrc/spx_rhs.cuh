@@ -799,13 +799,18 @@ __device__ inline void general_w_real(const DevPlan& P, const double2* __restric
 
 // Field part of the transpose, per species s and bracket component j at
 // real-space point pt: R_{s,j} = sum_{r in s} W_r S_{r,j} (j = 0..2: the G_s
-// terms; j = 3..5: the species' share of the B terms), summed in plane order.
+// terms; j = 3..5: the species' share of the B terms), here the partial sum
+// over the species' planes h in [h0, h1), in plane order.
+constexpr int VJP_HCHUNK = 64;   // Hermite planes per partial field sum
+__host__ __device__ __forceinline__ int vjp_nchunk(int nh) { return (nh + VJP_HCHUNK - 1) / VJP_HCHUNK; }
+
 __device__ inline double2 vjp_field_sum(const DevPlan& P, const double2* __restrict__ Cr,
-                                        const double2* __restrict__ W, size_t pt, int s, int j) {
+                                        const double2* __restrict__ W, size_t pt, int s, int j,
+                                        int h0, int h1) {
   const size_t pl = (size_t)P.plane;
   const GenPlane* gp = static_cast<const GenPlane*>(P.gen);
   double2 R = make_double2(0.0, 0.0);
-  for (int h = 0; h < P.nh; ++h) {
+  for (int h = h0; h < h1; ++h) {
     const int r = s * P.nh + h;
     const NlCoef& cf = gp[r].cf;
     double2 t;
@@ -823,25 +828,27 @@ __device__ inline double2 vjp_field_sum(const DevPlan& P, const double2* __restr
 }
 
 // Real-space gradient of field component c (0..5 = Ex..Bz) at pt from the
-// per-species sums S (plane s*6 + j): g_E = sum_s R_{s,0..2}, g_B = sum_s
-// (R_{s,3..5} + the chain through G_s = E + u_s x B).
+// partial sums S (plane (chunk * Ns + s) * 6 + j), chunks added in order:
+// g_E = sum_s R_{s,0..2}, g_B = sum_s (R_{s,3..5} + the chain through
+// G_s = E + u_s x B).
 __device__ __forceinline__ double2 vjp_field_grad(const DevPlan& P, const double2* __restrict__ S, int c,
                                                   size_t pt) {
   const size_t pl = (size_t)P.plane;
+  const int Ns = P.pb.Ns, nch = vjp_nchunk(P.nh);
+  auto R = [&](int s, int j) {
+    double2 v = make_double2(0.0, 0.0);
+    for (int k = 0; k < nch; ++k) v = cadd(v, S[((size_t)(k * Ns + s) * 6 + j) * pl + pt]);
+    return v;
+  };
   double2 g = make_double2(0.0, 0.0);
-  for (int s = 0; s < P.pb.Ns; ++s) {
-    const double2* Ss = S + (size_t)s * 6 * pl + pt;
-    if (c < 3) {
-      g = cadd(g, Ss[(size_t)c * pl]);
-      continue;
-    }
+  for (int s = 0; s < Ns; ++s) {
+    g = cadd(g, R(s, c));
+    if (c < 3) continue;
     const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
-    const double2 R0 = Ss[0], R1 = Ss[pl], R2 = Ss[2 * pl];
-    g = cadd(g, Ss[(size_t)c * pl]);
     // G_x = E_x + u_y B_z - u_z B_y, G_y = E_y + u_z B_x - u_x B_z, G_z = E_z + u_x B_y - u_y B_x
-    if (c == 3) { g = crfma(u2, R1, g); g = crfma(-u1, R2, g); }
-    else if (c == 4) { g = crfma(-u2, R0, g); g = crfma(u0, R2, g); }
-    else { g = crfma(u1, R0, g); g = crfma(-u0, R1, g); }
+    if (c == 3) { g = crfma(u2, R(s, 1), g); g = crfma(-u1, R(s, 2), g); }
+    else if (c == 4) { g = crfma(-u2, R(s, 0), g); g = crfma(u0, R(s, 2), g); }
+    else { g = crfma(u1, R(s, 0), g); g = crfma(-u0, R(s, 1), g); }
   }
   return g;
 }

@@ -146,7 +146,8 @@ def test_vjp_general_layout_is_transpose(shape):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", [(16, 16, 1, 3, 3, 3, 2), (8, 8, 8, 2, 2, 2, 1), (33, 32, 1, 4, 4, 1, 2)],
+@pytest.mark.parametrize("shape", [(16, 16, 1, 3, 3, 3, 2), (8, 8, 8, 2, 2, 2, 1), (33, 32, 1, 4, 4, 1, 2),
+                                   (16, 16, 1, 5, 5, 5, 2)],   # 125 planes per species: two partial field sums
                          ids=lambda s: "x".join(map(str, s)))
 def test_vjp_general_layout_adjoint_identity(shape):
     # <w, J v> = <J^T w, v> with J v from the oracle (exact central difference),
