@@ -225,6 +225,9 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile, int 
   P.iO0 = 1.0 / p.Omega_cs[0];
   pl->coef.clear();
   pl->gen.clear();
+  P.axm = P.ax[1];      // products on the Nx-point grid unless the 1D1V branch picks another
+  P.rnm = 1.0;
+  P.alias = 0;
   if (onev) {
     P.path = 0;
     pl->coef.resize((size_t)p.Ns * p.Nn * COEF_1V);
@@ -241,9 +244,6 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile, int 
     P.tile = T;
     P.ntiles = ntiles;
     // product grid of the stepper (axm); its twiddles extend the table
-    P.axm = P.ax[1];
-    P.rnm = 1.0;
-    P.alias = 0;
     std::vector<int> mr;
     const int M = mgrid ? choose_product_grid(N, p.cut_x, mgrid == 2, mr) : N;
     if (M != N) {
