@@ -81,7 +81,11 @@ int spx_plan_create(const spx_problem* pb, spx_plan** out);
  * 0 = 256).  Used by the autotuner. */
 int spx_plan_create_ex(const spx_problem* pb, int32_t tile, int32_t threads, spx_plan** out);
 int spx_plan_destroy(spx_plan* plan);
-/* Launch shape chosen for a plan (any pointer may be NULL); path 0 = fused 1D1V, 1 = general. */
+/* Launch shape chosen for a plan (any pointer may be NULL); path 0 = fused 1D1V,
+ * 1 = general, 2 = general with planes larger than one CTA's shared memory
+ * (about 6.9k points): spx_rhs then transforms one axis at a time over batches
+ * of lines through global memory, and spx_jvp, spx_jvp_lin, spx_linearize,
+ * spx_vjp and spx_dopri8_create return SPX_E_UNSUPPORTED. */
 int spx_plan_info(const spx_plan* plan, int32_t* tile, int32_t* ntiles, int32_t* threads, int32_t* path);
 
 /*

@@ -834,6 +834,11 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   }
   for (int i = 1; i < o->nsave; ++i)
     if (!(o->save_ts[i] >= o->save_ts[i - 1])) { set_error("save times must be non-decreasing"); return SPX_E_ARG; }
+  if (plan->big) {
+    set_error("spx_dopri8_create: a Fourier plane of this size does not fit in shared memory "
+              "(drive spx_rhs from the host instead)");
+    return SPX_E_UNSUPPORTED;
+  }
   int rc;
   if ((rc = upload_consts()) != SPX_OK) return rc;
   if ((rc = d8_attrs()) != SPX_OK) return rc;

@@ -22,6 +22,11 @@ struct spx_plan {
   size_t ws_bytes = 0;          // scratch of spx_rhs
   int threads = 256;            // CTA width of the right-hand-side kernels (<= 256)
   bool herm_ok = false;         // fused 1D1V path, odd Nx, antisymmetric k table: packed transforms valid
+  // general layout whose plane does not fit in one CTA's shared memory: spx_rhs
+  // runs the multi-pass kernels (line batches of big_nl lines, smem_big bytes)
+  bool big = false;
+  int big_nl = 0;
+  size_t smem_big = 0;
 };
 
 namespace spx {

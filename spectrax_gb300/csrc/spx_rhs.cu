@@ -277,9 +277,18 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile, int 
     if (p.Ny > 1 && (P.prow & 1) == 0) P.prow += 1;
     P.pplane = p.Ny * P.prow;
     pl->smem_gen = pl->smem_tab + 2 * (size_t)P.pplane * sizeof(double2);
-    if (pl->smem_gen > smem_max) {
-      set_error("a Fourier plane of this size does not fit in shared memory");
-      return SPX_E_UNSUPPORTED;
+    pl->big = pl->smem_gen > smem_max;
+    if (pl->big) {
+      // the plane does not fit: spx_rhs transforms one axis at a time over
+      // batches of lines staged through shared memory (k_big_lines)
+      const int nmax = std::max(p.Nx, std::max(p.Ny, p.Nz));
+      const size_t per_line = 2 * (size_t)nmax * sizeof(double2);
+      if (pl->smem_tab + per_line > smem_max) {
+        set_error("an FFT line of this length does not fit in shared memory");
+        return SPX_E_UNSUPPORTED;
+      }
+      pl->big_nl = (int)std::min<size_t>(32, (smem_max - pl->smem_tab) / per_line);
+      pl->smem_big = pl->smem_tab + (size_t)pl->big_nl * per_line;
     }
     const int nplanes = p.Ns * P.nh;
     // forward table (GenPlane per plane), then the transposed bracket (GenPlaneT per plane)
@@ -575,6 +584,141 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_vjp_gen(const DevPlan* __res
   general_nl_plane_t<3>(P, stab, w, W, GB, nullptr, nullptr, b, sA, sB, epi);
 }
 
+// ------------------------------------------------------------------------
+// Multi-pass general path (planes larger than one CTA's shared memory).  The
+// plane transforms run one axis at a time over batches of lines staged through
+// shared memory; between passes the planes sit in global memory in natural
+// order (standard, unshifted index along every axis).  Workspace planes:
+// [0, nplanes) real-space Hermite planes, [nplanes, nreal) field combinations,
+// [nreal, nreal + nplanes) bracket products, transformed in place.
+// ------------------------------------------------------------------------
+
+// Masked entries of y (Hermite planes, then the field combinations) scattered
+// to standard order.
+__global__ void __launch_bounds__(NTHREADS) k_big_scatter(const DevPlan* __restrict__ gP,
+                                                         const double2* __restrict__ y,
+                                                         double2* __restrict__ ws) {
+  __shared__ DevPlan P;
+  if (threadIdx.x == 0) P = *gP;
+  __syncthreads();
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const int nplanes = P.pb.Ns * P.nh;
+  const size_t pl = (size_t)P.plane;
+  const size_t total = (size_t)(nplanes + 3 * P.pb.Ns + 3) * pl;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int id = (int)(i / pl);
+    const size_t pt = i - (size_t)id * pl;
+    const int cz = (int)(pt % Nz), cx = (int)((pt / Nz) % Nx), cy = (int)(pt / ((size_t)Nz * Nx));
+    double2 v = make_double2(0.0, 0.0);
+    if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut))
+      v = id < nplanes ? y[i] : field_combo_point(P, y + P.nc, id - nplanes, pt);
+    ws[(size_t)id * pl + ((size_t)std_index(cy, Ny) * Nx + std_index(cx, Nx)) * Nz + std_index(cz, Nz)] = v;
+  }
+}
+
+// One pass of the plane transforms along `axis` (0 y, 1 x, 2 z) for planes
+// blockIdx.y of buf: CTA blockIdx.x stages lines [l0, l0 + nl) in shared
+// memory (rows of the axis length), transforms them with the axis plan's
+// pruning (DIF = false: inputs masked along the axis; true: only the kept
+// outputs are needed) and writes them back.  Loads and stores walk along
+// whichever of element and line index is contiguous in memory.
+template <bool INV, bool DIF>
+__global__ void __launch_bounds__(NTHREADS) k_big_lines(const DevPlan* __restrict__ gP,
+                                                       const double2* __restrict__ gtab,
+                                                       double2* __restrict__ buf, int axis, int nl) {
+  __shared__ DevPlan P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* stab = reinterpret_cast<double2*>(smem_raw);
+  load_plan(P, stab, gP, gtab);
+  const AxisPlan& ap = P.ax[axis];
+  const int n = ap.n;
+  const int Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const size_t pl = (size_t)P.plane;
+  const int nlines = (int)(pl / n);
+  const int l0 = blockIdx.x * nl;
+  if (l0 >= nlines) return;
+  const int nt = min(nl, nlines - l0);
+  double2* sA = stab + (P.tab_len + 15) / 16 * 16;
+  double2* sB = sA + (size_t)nl * n;
+  double2* g = buf + (size_t)blockIdx.y * pl;
+  // element e of line l: base(l) + e * stride
+  const size_t stride = axis == 2 ? 1 : (axis == 1 ? (size_t)Nz : (size_t)Nx * Nz);
+  auto base = [&](int l) -> size_t {
+    if (axis == 2) return (size_t)l * Nz;                              // l = y*Nx + x
+    if (axis == 1) return (size_t)(l / Nz) * Nx * Nz + (size_t)(l % Nz);  // l = y*Nz + z
+    return (size_t)l;                                                  // l = x*Nz + z
+  };
+  const bool efast = stride == 1;
+  const int tot = nt * n;
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int j = efast ? i / n : i % nt, e = efast ? i % n : i / nt;
+    sA[j * n + e] = g[base(l0 + j) + (size_t)e * stride];
+  }
+  __syncthreads();
+  const double2* r = fft_axis_t<INV, DIF>(sA, sB, ap, stab, Lines{nt, 1, 1, n, 0}, ap.cut);
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int j = efast ? i / n : i % nt, e = efast ? i % n : i / nt;
+    g[base(l0 + j) + (size_t)e * stride] = r[j * n + e];
+  }
+}
+
+// Real-space bracket of every Hermite plane into the product planes.
+__global__ void __launch_bounds__(NTHREADS) k_big_bracket(const DevPlan* __restrict__ gP,
+                                                         double2* __restrict__ ws) {
+  __shared__ DevPlan P;
+  if (threadIdx.x == 0) P = *gP;
+  __syncthreads();
+  const int Ns = P.pb.Ns, nplanes = Ns * P.nh, nreal = nplanes + 3 * Ns + 3;
+  const size_t pl = (size_t)P.plane;
+  const double2* GB = ws + (size_t)nplanes * pl;
+  double2* prod = ws + (size_t)nreal * pl;
+  const GenPlane* gp = static_cast<const GenPlane*>(P.gen);
+  const size_t total = (size_t)nplanes * pl;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / pl);
+    const size_t x = i - (size_t)r * pl;
+    const NlCoef& cf = gp[r].cf;
+    const bool anyx = cf.ix[0] >= 0 || cf.ix[1] >= 0 || cf.ix[2] >= 0;
+    const bool anyy = cf.iy[0] >= 0 || cf.iy[1] >= 0 || cf.iy[2] >= 0;
+    const bool anyz = cf.iz[0] >= 0 || cf.iz[1] >= 0 || cf.iz[2] >= 0;
+    prod[i] = bracket_point(cf, ws, field_planes(GB, r / P.nh, Ns, pl), pl, x, anyx, anyy, anyz,
+                            make_double2(0.0, 0.0));
+  }
+}
+
+// Output Hermite planes: linear terms plus the transformed bracket.
+__global__ void __launch_bounds__(NTHREADS) k_big_epi(const DevPlan* __restrict__ gP,
+                                                     const double2* __restrict__ gtab,
+                                                     const double2* __restrict__ y,
+                                                     const double2* __restrict__ ws,
+                                                     double2* __restrict__ dy) {
+  __shared__ DevPlan P;
+  if (threadIdx.x == 0) P = *gP;
+  __syncthreads();
+  const int nplanes = P.pb.Ns * P.nh, nreal = nplanes + 3 * P.pb.Ns + 3;
+  const size_t pl = (size_t)P.plane;
+  const double2* F = ws + (size_t)nreal * pl;
+  const size_t total = (size_t)nplanes * pl;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int id = (int)(i / pl);
+    dy[i] = big_epi_point(P, gtab, y, F, id, i - (size_t)id * pl);
+  }
+}
+
+// Current and Maxwell's equations, a range of points per CTA.
+__global__ void __launch_bounds__(NTHREADS) k_big_maxwell(const DevPlan* __restrict__ gP,
+                                                         const double2* __restrict__ gtab,
+                                                         const double2* __restrict__ y,
+                                                         double2* __restrict__ dy) {
+  __shared__ DevPlan P;
+  if (threadIdx.x == 0) P = *gP;
+  __syncthreads();
+  EpiStore epi{dy};
+  const int chunk = (P.plane + gridDim.x - 1) / gridDim.x;
+  const int p0 = blockIdx.x * chunk, p1 = min(P.plane, p0 + chunk);
+  if (p0 < p1) maxwell_range(P, gtab, y, p0, p1, epi);
+}
+
 static bool g_attr_done = false;
 
 // Allow each kernel the opt-in shared memory minus its static part.
@@ -610,6 +754,8 @@ static int set_attrs() {
   if ((rc = allow_smem(k_jvp_nl_lin, optin)) != SPX_OK) return rc;
   if ((rc = allow_smem(k_vjp_real, optin)) != SPX_OK) return rc;
   if ((rc = allow_smem(k_vjp_gen, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_big_lines<true, false>, optin)) != SPX_OK) return rc;
+  if ((rc = allow_smem(k_big_lines<false, true>, optin)) != SPX_OK) return rc;
   g_attr_done = true;
   return SPX_OK;
 }
@@ -619,6 +765,29 @@ int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, c
   if (P.path == 0) {
     const int grid = P.pb.Ns * P.ntiles + 1;
     k_rhs1v<<<grid, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab, y, dy);
+  } else if (pl->big) {
+    const int nplanes = P.pb.Ns * P.nh, nreal = nplanes + 3 * P.pb.Ns + 3;
+    const size_t pln = (size_t)P.plane;
+    const int grid = 152 * 8;
+    k_big_scatter<<<grid, NTHREADS, 0, st>>>(pl->d_plan, y, ws);
+    for (int axis = 2; axis >= 0; --axis) {     // z, x, y
+      const int n = P.ax[axis].n;
+      if (n == 1) continue;
+      const int nb = (int)((pln / n + pl->big_nl - 1) / pl->big_nl);
+      k_big_lines<true, false><<<dim3(nb, nreal), NTHREADS, pl->smem_big, st>>>(pl->d_plan, pl->d_tab, ws, axis,
+                                                                                pl->big_nl);
+    }
+    k_big_bracket<<<grid, NTHREADS, 0, st>>>(pl->d_plan, ws);
+    for (int axis = 2; axis >= 0; --axis) {
+      const int n = P.ax[axis].n;
+      if (n == 1) continue;
+      const int nb = (int)((pln / n + pl->big_nl - 1) / pl->big_nl);
+      k_big_lines<false, true><<<dim3(nb, nplanes), NTHREADS, pl->smem_big, st>>>(
+          pl->d_plan, pl->d_tab, ws + (size_t)nreal * pln, axis, pl->big_nl);
+    }
+    k_big_epi<<<grid, NTHREADS, 0, st>>>(pl->d_plan, pl->d_tab, y, ws, dy);
+    k_big_maxwell<<<(int)std::min<size_t>(152, (pln + NTHREADS - 1) / NTHREADS), NTHREADS, 0, st>>>(
+        pl->d_plan, pl->d_tab, y, dy);
   } else {
     const int nplanes = P.pb.Ns * P.nh;
     k_gen_real<<<nplanes + 3 * P.pb.Ns + 3, GEN_THREADS, pl->smem_gen, st>>>(pl->d_plan, pl->d_tab, y, ws);
@@ -626,6 +795,15 @@ int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, c
   }
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
+}
+
+// Entry points that keep whole planes in shared memory refuse plans whose
+// planes do not fit (those run spx_rhs through the multi-pass kernels only).
+static int refuse_big(const spx_plan* pl, const char* who) {
+  if (!pl || !pl->big) return SPX_OK;
+  set_error(std::string(who) + ": a Fourier plane of this size does not fit in shared memory "
+                               "(such plans support spx_rhs only)");
+  return SPX_E_UNSUPPORTED;
 }
 
 }  // namespace spx
@@ -726,7 +904,7 @@ int spx_plan_info(const spx_plan* pl, int32_t* tile, int32_t* ntiles, int32_t* t
   if (tile) *tile = pl->host.tile;
   if (ntiles) *ntiles = pl->host.ntiles;
   if (threads) *threads = pl->threads;
-  if (path) *path = pl->host.path;
+  if (path) *path = pl->big ? 2 : pl->host.path;
   return SPX_OK;
 }
 
@@ -758,6 +936,7 @@ static int check_vec_args(const spx_plan* pl, const void* a, const void* b, cons
 int spx_jvp(const spx_plan* pl, const void* y, const void* v, void* Jv, void* ws, size_t ws_bytes,
             void* stream) {
   int rc = check_vec_args(pl, y, v, Jv, ws, ws_bytes, "spx_jvp");
+  if (rc == SPX_OK) rc = refuse_big(pl, "spx_jvp");
   if (rc != SPX_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const DevPlan& P = pl->host;
@@ -792,6 +971,7 @@ int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes
   if (!pl || !y || !lin) { set_error("spx_linearize: null argument"); return SPX_E_ARG; }
   if (((uintptr_t)y | (uintptr_t)lin) & 15) { set_error("spx_linearize: pointers must be 16-byte aligned"); return SPX_E_ARG; }
   if (lin_bytes < spx_linearize_bytes(pl)) { set_error("spx_linearize: lin too small"); return SPX_E_WORKSPACE; }
+  if (int rb = refuse_big(pl, "spx_linearize")) return rb;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const DevPlan& P = pl->host;
   if (P.path == 0) {
@@ -810,6 +990,7 @@ int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes
 int spx_jvp_lin(const spx_plan* pl, const void* lin, const void* v, void* Jv, void* ws, size_t ws_bytes,
                 void* stream) {
   int rc = check_vec_args(pl, lin, v, Jv, ws, ws_bytes, "spx_jvp_lin");
+  if (rc == SPX_OK) rc = refuse_big(pl, "spx_jvp_lin");
   if (rc != SPX_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const DevPlan& P = pl->host;
@@ -833,6 +1014,7 @@ int spx_jvp_lin(const spx_plan* pl, const void* lin, const void* v, void* Jv, vo
 int spx_vjp(const spx_plan* pl, const void* y, const void* wv, void* g, void* ws, size_t ws_bytes,
             void* stream) {
   int rc = check_vec_args(pl, y, wv, g, ws, ws_bytes, "spx_vjp");
+  if (rc == SPX_OK) rc = refuse_big(pl, "spx_vjp");
   if (rc != SPX_OK) return rc;
   const DevPlan& P = pl->host;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

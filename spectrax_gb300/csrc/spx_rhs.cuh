@@ -749,6 +749,65 @@ __device__ __forceinline__ void general_nl_plane(const DevPlan& P, const double2
   general_nl_plane_t<0>(P, tab, y, Creal, GB, nullptr, nullptr, id, sA, sB, epi);
 }
 
+// Multi-pass general path (planes larger than one CTA's shared memory): the
+// value of output entry pt (centred order) of Hermite plane `id` as in the
+// epilogue of general_nl_plane_t (MODE 0), with the forward-transformed bracket
+// read from plane `id` of F (global, natural order, standard index per axis).
+__device__ inline double2 big_epi_point(const DevPlan& P, const double2* __restrict__ tab,
+                                        const double2* __restrict__ y, const double2* __restrict__ F,
+                                        int id, size_t pt) {
+  const spx_problem& pb = P.pb;
+  const int Ny = P.ax[0].n, Nx = P.ax[1].n, Nz = P.ax[2].n;
+  const size_t pl = (size_t)P.plane;
+  const int Nn = pb.Nn, Nm = pb.Nm, Np = pb.Np;
+  const int s = id / P.nh, h = id % P.nh;
+  const int n = h % Nn, m = (h / Nn) % Nm, p = h / (Nn * Nm);
+  const double* L = (static_cast<const GenPlane*>(P.gen) + id)->lin;
+  const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
+  const double2* Cp = y + (size_t)id * pl;
+  const size_t sn_ = pl, sm_ = (size_t)Nn * pl, sp_ = (size_t)Nn * Nm * pl;
+  const int cz = (int)(pt % Nz), cx = (int)((pt / Nz) % Nx), cy = (int)(pt / ((size_t)Nz * Nx));
+  const double2 C0 = Cp[pt];
+  double re = 0.0, im = 0.0, k2 = 0.0;
+  if (Nx > 1) {
+    const double2 kt = ktab(P, tab, 1, cx);
+    double2 t = cscale(L[8], C0);
+    if (n + 1 < Nn) t = crfma(L[2], Cp[pt + sn_], t);
+    if (n >= 1) t = crfma(L[3], Cp[pt - sn_], t);
+    const double w = kt.x * a0;
+    re = fma(w, t.y, re); im = fma(-w, t.x, im);
+    k2 = fma(kt.y, kt.y, k2);
+  }
+  if (Ny > 1) {
+    const double2 kt = ktab(P, tab, 0, cy);
+    double2 t = cscale(L[9], C0);
+    if (m + 1 < Nm) t = crfma(L[4], Cp[pt + sm_], t);
+    if (m >= 1) t = crfma(L[5], Cp[pt - sm_], t);
+    const double w = kt.x * a1;
+    re = fma(w, t.y, re); im = fma(-w, t.x, im);
+    k2 = fma(kt.y, kt.y, k2);
+  }
+  if (Nz > 1) {
+    const double2 kt = ktab(P, tab, 2, cz);
+    double2 t = cscale(L[10], C0);
+    if (p + 1 < Np) t = crfma(L[6], Cp[pt + sp_], t);
+    if (p >= 1) t = crfma(L[7], Cp[pt - sp_], t);
+    const double w = kt.x * a2;
+    re = fma(w, t.y, re); im = fma(-w, t.x, im);
+    k2 = fma(kt.y, kt.y, k2);
+  }
+  const double d = fma(pb.D, k2, L[1]);
+  re = fma(-d, C0.x, re);
+  im = fma(-d, C0.y, im);
+  if (kept(cy, Ny, P.ax[0].cut) && kept(cx, Nx, P.ax[1].cut) && kept(cz, Nz, P.ax[2].cut)) {
+    const size_t sidx = ((size_t)std_index(cy, Ny) * Nx + std_index(cx, Nx)) * Nz + std_index(cz, Nz);
+    const double2 v = F[(size_t)id * pl + sidx];
+    re = fma(L[0], v.x, re);
+    im = fma(L[0], v.y, im);
+  }
+  return make_double2(re, im);
+}
+
 // The six bracket sums of plane `id` for the real-space planes R of a state y
 // (the part of N(F_v, C_y) that does not depend on v): S_0..2 = g_x C_{n-1},
 // g_y C_{m-1}, g_z C_{p-1}; S_3..5 = the B_x, B_y, B_z neighbour combinations;

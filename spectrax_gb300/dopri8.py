@@ -254,6 +254,19 @@ def simulation(input_parameters=None, Nx=33, Ny=1, Nz=1, Nn=20, Nm=1, Np=1, Ns=2
     if isinstance(solver, ImplicitMidpoint):
         from .midpoint import midpoint_solve
         ys, en, info = midpoint_solve(p, time, solver, mask_mode=mask_mode)
+    elif plan_for_params(p, mask_mode).path == 2:
+        # planes too large for the device stepper's shared memory: the same
+        # tableau, controller and save rule driven from the host around spx_rhs
+        plan = plan_for_params(p, mask_mode)
+        from .midpoint import energies
+        tol = float(p.get("ode_tolerance", 1e-12))
+        _, saved, info = host_dopri8_solve(plan, initial_state(p), float(time[-1]), dt, ts=time,
+                                           adaptive=adaptive_time_step, rtol=tol, atol=tol, max_steps=max_steps)
+        if info["status_name"] != "DONE":
+            raise RuntimeError(f"Dopri8 solve ended with status {info['status_name']}")
+        masses = species_masses(p)
+        en = np.array([[e, k] + list(ks) for e, k, ks in (energies(plan, y, masses) for y in saved)])
+        ys = saved.cpu().numpy()
     else:
         s, status = solve(p, ts=time, adaptive=adaptive_time_step, dt=dt, max_steps=max_steps,
                           mask_mode=mask_mode)

@@ -125,15 +125,19 @@ def test_rhs_rejects_bad_inputs():
 
 
 @pytest.mark.gpu
-def test_oversized_planes_are_refused_not_launched():
+def test_oversized_planes_take_the_multipass_path():
     # a general-path plane whose two shared-memory buffers exceed a CTA's
-    # shared memory is refused at plan creation (SPX_E_UNSUPPORTED), before
-    # any launch
+    # shared memory gets plan path 2 (spx_rhs through the multi-pass kernels);
+    # the entry points that hold whole planes refuse it before any launch
+    import torch
     import spectrax_gb300 as sg
     from spectrax_gb300 import SpectraxError, vector_field
     pb = sg.make_problem(64, 64, 8, 2, 2, 1, 1, [-1], 1, 0, [1], [1, 1, 1], [0, 0, 0], 1, 1, 1)
+    plan = vector_field.get_plan(pb)
+    assert plan.path == 2
+    z = torch.zeros(plan.state_len, dtype=torch.complex128, device="cuda")
     with pytest.raises(SpectraxError):
-        vector_field.get_plan(pb)
+        plan.jvp_into(z, z.clone(), torch.empty_like(z))
 
 
 @pytest.mark.gpu
