@@ -1,4 +1,10 @@
-// spx_rhs.cu — plan construction, right-hand-side kernels and their C ABI.
+// spx_rhs.cu — plan construction, right-hand-side kernels and their C ABI:
+//  * plans: FFT tables, the 1D1V coefficient table and product grid, the
+//    general layout's per-plane tables (GenPlane, GenPlaneT);
+//  * spx_rhs / spx_jvp / spx_linearize / spx_jvp_lin on the fused 1D1V path
+//    (one launch) and the general path (plane transforms in shared memory, or
+//    the multi-pass kernels k_big_* for planes larger than a CTA's shared memory);
+//  * spx_vjp: the transposes of both paths (k_vjp1v*, k_vjp_real/_fsum/_gen).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
