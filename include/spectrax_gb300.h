@@ -103,6 +103,9 @@ int spx_plan_info(const spx_plan* plan, int32_t* tile, int32_t* ntiles, int32_t*
  */
 int spx_set_product_grid(int32_t mode);
 int spx_plan_product_grid(const spx_plan* plan);
+/* The product grid a 1D1V plan with Nx = nx and mask cut `cut` gets under
+ * `mode` (host only; no device, no plan). */
+int spx_product_grid_for(int32_t nx, int32_t cut, int32_t mode);
 
 /* Number of complex128 entries of the flat state (N_C + N_F). */
 int64_t spx_state_len(const spx_problem* pb);

@@ -103,6 +103,7 @@ _PROTOS = {
     "spx_rhs_workspace_bytes": (C.c_size_t, [_VP]),
     "spx_set_product_grid": (C.c_int, [C.c_int32]),
     "spx_plan_product_grid": (C.c_int, [_VP]),
+    "spx_product_grid_for": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     "spx_rhs": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_jvp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_linearize_bytes": (C.c_size_t, [_VP]),

@@ -171,12 +171,13 @@ static int g_product_grid = 0;
 // 1.5-4 % slower than the 43*3 transform, each point and Stockham pass costing
 // shared-memory traffic and barriers the count does not see.  Mode 2 keeps it
 // at <= 0.8 with no more stages than n.  Returns m == n (and rads empty) otherwise.
-static int choose_product_grid(int n, int cut, bool max_n, std::vector<int>& rads) {
+static int choose_product_grid(int n, int cut, bool max_n, std::vector<int>& rads, int mode = -1) {
   rads.clear();
-  if (g_product_grid == 1 || cut < 1 || n < 8) return n;
+  if (mode < 0) mode = g_product_grid;
+  if (mode == 1 || cut < 1 || n < 8) return n;
   const std::vector<int> fn = factorize(n);
   const double base = line_pair_cost(n, fn, cut);
-  double best = (g_product_grid == 2 ? 0.8 : 0.5) * base;
+  double best = (mode == 2 ? 0.8 : 0.5) * base;
   int bm = n;
   for (int m = 3 * cut + 1; m <= 2 * n; ++m) {
     if (m == n || (max_n && m > n)) continue;
@@ -902,6 +903,12 @@ int spx_set_product_grid(int32_t mode) {
 }
 
 int spx_plan_product_grid(const spx_plan* pl) { return pl ? pl->host.axm.n : 0; }
+
+int spx_product_grid_for(int32_t nx, int32_t cut, int32_t mode) {
+  if (nx < 1 || mode < 0 || mode > 2) { set_error("spx_product_grid_for: bad argument"); return SPX_E_ARG; }
+  std::vector<int> rads;
+  return choose_product_grid(nx, cut, false, rads, mode);
+}
 
 size_t spx_rhs_workspace_bytes(const spx_plan* pl) { return pl ? pl->ws_bytes : 0; }
 

@@ -55,3 +55,29 @@ def test_no_cpu_fallback_in_product():
             if fn.endswith(".py"):
                 src = open(os.path.join(dp, fn)).read()
                 assert "oracle" not in re.findall(r"^\s*(?:from|import)\s+(\w+)", src, flags=re.M), fn
+
+
+@pytest.mark.parametrize("nx,cut,mode,expect", [
+    (129, 43, 0, 129),   # default: the benchmark's 43 x 3 transform stays
+    (127, 42, 0, 128),   # prime lengths take a >= 2x cheaper grid
+    (97, 32, 0, 104),
+    (251, 83, 0, 256),
+    (65, 21, 0, 65),
+    (17, 5, 0, 17),
+    (129, 43, 2, 136),   # least modeled FP64 work, no extra Stockham stage
+    (65, 21, 2, 64),
+    (33, 11, 2, 33),
+    (129, 43, 1, 129),   # always Nx
+    (97, 32, 1, 97),
+])
+def test_product_grid_choice_without_gpu(nx, cut, mode, expect):
+    # host-side choice of the 1D1V stepper's product grid (no device call)
+    from spectrax_gb300 import _lib
+    assert _lib.lib().spx_product_grid_for(nx, cut, mode) == expect
+
+
+def test_product_grid_choice_rejects_bad_arguments():
+    from spectrax_gb300 import _lib
+    L = _lib.lib()
+    assert L.spx_product_grid_for(0, 1, 0) == _lib.SPX_E_ARG
+    assert L.spx_product_grid_for(33, 11, 3) == _lib.SPX_E_ARG
