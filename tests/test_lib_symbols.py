@@ -81,3 +81,15 @@ def test_product_grid_choice_rejects_bad_arguments():
     L = _lib.lib()
     assert L.spx_product_grid_for(0, 1, 0) == _lib.SPX_E_ARG
     assert L.spx_product_grid_for(33, 11, 3) == _lib.SPX_E_ARG
+
+
+def test_product_grid_mode_setter_without_gpu():
+    from spectrax_gb300 import vector_field
+    with pytest.raises(ValueError):
+        vector_field.set_product_grid("bogus")
+    try:
+        vector_field.set_product_grid("fp64")
+        assert vector_field.get_product_grid() == "fp64"
+    finally:
+        vector_field.set_product_grid("auto")
+    assert vector_field.get_product_grid() == "auto"
