@@ -96,15 +96,19 @@ int spx_plan_info(const spx_plan* plan, int32_t* tile, int32_t* ntiles, int32_t*
  * folds onto |k| = K when Nx = 3K).  For plans created afterwards: mode 0
  * (default) uses such a grid where its transforms are modeled >= 2x cheaper
  * than Nx-point ones (prime Nx: 97 -> 104, 127 -> 128, 251 -> 256); mode 1 always Nx
- * points; mode 2 the cheapest grid of <= 0.8x the modeled FP64 work without an
- * extra Stockham stage (129 -> 136, 65 -> 64; measured slower than Nx on the
- * two-stream stage kernel).  Results agree to rounding.  spx_plan_product_grid
- * returns the grid length M of a plan.
+ * points; mode 2 the cheapest grid of <= 0.8x the modeled FP64 work, one with
+ * more Stockham stages than Nx only at <= 0.5x (129 -> 136, 65 -> 64; measured
+ * slower than Nx on the two-stream stage kernel).  Only plans with 3K <= Nx get
+ * M != Nx (with 3K > Nx the Nx-point product folds more than the one term).
+ * Results agree to rounding.  spx_plan_product_grid returns the grid length M
+ * of a plan.
  */
 int spx_set_product_grid(int32_t mode);
 int spx_plan_product_grid(const spx_plan* plan);
 /* The product grid a 1D1V plan with Nx = nx and mask cut `cut` gets under
- * `mode` (host only; no device, no plan). */
+ * `mode` (host only; no device, no plan).  It applies the selection rule only:
+ * plan creation additionally keeps Nx points when the stage kernel with the
+ * longer table would not fit in shared memory, which this query does not model. */
 int spx_product_grid_for(int32_t nx, int32_t cut, int32_t mode);
 
 /* Number of complex128 entries of the flat state (N_C + N_F). */
@@ -331,7 +335,7 @@ int spx_dopri8_copy(spx_dopri8* s, int32_t what, void* dst, size_t bytes, void* 
  * each integrated by adaptive (or constant-step) Dopri8 to t1, all in ONE
  * persistent launch: each thread-block cluster of `cluster` CTAs takes the next
  * instance from a largest-first work queue.  Replaces the serial scan loop of
- * Examples/1D_Landau_damping_dr_curve.py:149-175 (one simulation() per k).
+ * Examples/1D_Landau_damping_dr_curve.py:88-110 (one simulation() per k).
  * The launch is captured once as a CUDA graph.
  */
 typedef struct spx_batch_opts {

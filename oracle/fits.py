@@ -1,10 +1,10 @@
 """Damping / growth-rate fits of the field energy (test infrastructure only).
 
 * Landau: gamma = slope/2 of a line fit of log E at the local maxima of E[:100]
-  (Examples/1D_Landau_damping_dr_curve.py:173-175; ``scipy.signal.find_peaks``
+  (Examples/1D_Landau_damping_dr_curve.py:106-110; ``scipy.signal.find_peaks``
   with default arguments = strict local maxima, plateaus by their middle sample).
 * Two-stream: gamma = slope/2 of a line fit of log E over samples [300:]
-  (Examples/1D_two_stream_gr_curve.py:167-168).
+  (Examples/1D_two_stream_gr_curve.py:101-104).
 * Windowed least-squares slope of log E over t in [t_a, t_b] (the differentiable
   loss of the adjoint workload): slope = sum (t-tm)(l-lm) / sum (t-tm)^2.
 """

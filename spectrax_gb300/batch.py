@@ -1,6 +1,6 @@
 """Batched solves of many uneven 1D1V instances in one persistent launch.
 
-The reference's damping-rate scan (Examples/1D_Landau_damping_dr_curve.py:149-175)
+The reference's damping-rate scan (Examples/1D_Landau_damping_dr_curve.py:88-110)
 calls ``simulation`` once per wavenumber, serially.  ``BatchSolver`` packs all
 instances (different k, Nn, Nx, nu, ...) into one graph-captured persistent
 kernel (``spx_batch_*``): each thread-block cluster integrates one instance at a

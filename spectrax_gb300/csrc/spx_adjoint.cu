@@ -378,6 +378,7 @@ int spx_rk_step_store_ex(const spx_plan* pl, const void* y, double h, void* Ysta
     set_error("spx_rk_step_store_ex: packed transforms need an odd Nx with an antisymmetric wavenumber grid");
     return SPX_E_ARG;
   }
+  if (int rd = check_plan_device(pl, "spx_rk_step_store")) return rd;
   const int herm = hermitian ? 1 : 0;
   int rc = adj_setup();
   if (rc != SPX_OK) return rc;
@@ -456,6 +457,7 @@ int spx_param_dots(const spx_plan* pl, const void* y, const void* g, double* acc
     set_error("spx_param_dots: only the 1D1V layout is supported");
     return SPX_E_UNSUPPORTED;
   }
+  if (int rd = check_plan_device(pl, "spx_param_dots")) return rd;
   int rc = adj_setup();
   if (rc != SPX_OK) return rc;
   const DevPlan& P = pl->host;
@@ -479,6 +481,7 @@ int spx_vjp_param_ex(const spx_plan* pl, const void* y, const void* w, void* g, 
     set_error("spx_vjp_param: only the 1D1V layout is supported");
     return SPX_E_UNSUPPORTED;
   }
+  if (int rd = check_plan_device(pl, "spx_vjp_param")) return rd;
   if (hermitian && !pl->herm_ok) {
     set_error("spx_vjp_param_ex: packed transforms need an odd Nx with an antisymmetric wavenumber grid");
     return SPX_E_ARG;

@@ -14,7 +14,7 @@
 // tiles, which keep that symmetry exactly.
 //
 // Instances may differ in Nx, Nn, Ns, L, nu, alpha, u (spectrax's Landau scan:
-// Examples/1D_Landau_damping_dr_curve.py:149-175 loops over k serially).
+// Examples/1D_Landau_damping_dr_curve.py:88-110 loops over k serially).
 #include <cooperative_groups.h>
 
 #include <algorithm>

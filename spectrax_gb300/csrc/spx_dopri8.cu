@@ -825,6 +825,7 @@ extern "C" {
 int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8** out) {
   if (!plan || !o || !out) { set_error("spx_dopri8_create: null argument"); return SPX_E_ARG; }
   *out = nullptr;
+  if (int rd = check_plan_device(plan, "spx_dopri8_create")) return rd;
   if (!(o->t1 >= o->t0) || !(o->dt0 > 0.0) || o->nsave < 0 || (o->nsave > 0 && !o->save_ts) ||
       o->max_steps <= 0) {
     set_error("spx_dopri8_create: bad options"); return SPX_E_ARG;

@@ -81,6 +81,7 @@ int spx_maxwellian(const spx_plan* pl, const double* Us, const double* xreal, in
     set_error("spx_maxwellian: bad argument");
     return SPX_E_ARG;
   }
+  if (int rd = check_plan_device(pl, "spx_maxwellian")) return rd;
   const DevPlan& P = pl->host;
   for (int a = 0; a < 3; ++a)
     if (P.ax[a].n > 1 && 2 * P.ax[a].cut + 1 < P.ax[a].n) {

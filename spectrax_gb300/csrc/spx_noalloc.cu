@@ -123,16 +123,16 @@ extern "C" int spx_vjp_noalloc(const spx_plan* pl, const void* y, const void* w,
               std::to_string((long long)SPX_VJP_NOALLOC_MAX_ENTRIES) + "; use spx_vjp with a workspace");
     return SPX_E_UNSUPPORTED;
   }
-  int dev = 0;
-  SPX_CUDA(cudaGetDevice(&dev));
+  // the scratch address is per device: the plan's device must be current
+  if (int rd = check_plan_device(pl, "spx_vjp_noalloc")) return rd;
   double2* scratch = nullptr;
-  int rc = setup_device(dev, &scratch);
+  int rc = setup_device(pl->device, &scratch);
   if (rc != SPX_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  k_vjp1v_static<<<P.pb.Ns * P.ntiles, NTHREADS, pl->smem_1v, st>>>(
+  k_vjp1v_static<<<P.pb.Ns * P.ntiles, pl->threads, pl->smem_1v, st>>>(
       pl->d_plan, pl->d_tab, static_cast<const double2*>(y), static_cast<const double2*>(w),
       static_cast<double2*>(g), scratch);
-  k_vjp1v_fields_static<<<1, NTHREADS, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab,
+  k_vjp1v_fields_static<<<1, pl->threads, pl->smem_1v, st>>>(pl->d_plan, pl->d_tab,
                                                           static_cast<const double2*>(w),
                                                           static_cast<double2*>(g), scratch);
   SPX_CUDA(cudaGetLastError());

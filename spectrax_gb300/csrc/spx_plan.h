@@ -40,6 +40,9 @@ int build_plan_host(const spx_problem* pb, int nsm, spx_plan* pl, int tile = 0, 
 int launch_rhs(const spx_plan* pl, const double2* y, double2* dy, double2* ws, cudaStream_t st);
 // Opt-in shared memory per block of the current device (0 on failure).
 int smem_optin();
+// SPX_OK when the calling thread's current device is the one the plan was created
+// on; otherwise SPX_E_ARG (the plan's tables, and any per-device scratch, live there).
+int check_plan_device(const spx_plan* pl, const char* who);
 }  // namespace spx
 
 namespace spx {

@@ -174,7 +174,10 @@ static int g_product_grid = 0;
 static int choose_product_grid(int n, int cut, bool max_n, std::vector<int>& rads, int mode = -1) {
   rads.clear();
   if (mode < 0) mode = g_product_grid;
-  if (mode == 1 || cut < 1 || n < 8) return n;
+  // M != n is exact only where the n-point product folds at most the single
+  // pair k1 = k2 = +-cut (3 cut == n); with 3 cut > n more terms alias on the
+  // n-point grid than the stepper adds back, so such plans keep n
+  if (mode == 1 || cut < 1 || n < 8 || 3 * cut > n) return n;
   const std::vector<int> fn = factorize(n);
   const double base = line_pair_cost(n, fn, cut);
   double best = (mode == 2 ? 0.8 : 0.5) * base;
@@ -738,6 +741,18 @@ static int allow_smem(K kernel, int optin) {
   return SPX_OK;
 }
 
+int check_plan_device(const spx_plan* pl, const char* who) {
+  int dev = -1;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  if (dev != pl->device) {
+    set_error(std::string(who) + ": the current device (" + std::to_string(dev) +
+              ") is not the plan's device (" + std::to_string(pl->device) + ")");
+    return SPX_E_ARG;
+  }
+  return SPX_OK;
+}
+
 int smem_optin() {
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -929,6 +944,7 @@ int spx_rhs(const spx_plan* pl, const void* y, void* dy, void* ws, size_t ws_byt
     set_error("spx_rhs: workspace too small or misaligned");
     return SPX_E_WORKSPACE;
   }
+  if (int rd = check_plan_device(pl, "spx_rhs")) return rd;
   return launch_rhs(pl, static_cast<const double2*>(y), static_cast<double2*>(dy),
                     static_cast<double2*>(ws), static_cast<cudaStream_t>(stream));
 }
@@ -943,7 +959,7 @@ static int check_vec_args(const spx_plan* pl, const void* a, const void* b, cons
   if (pl->ws_bytes > 0 && (!ws || ws_bytes < pl->ws_bytes || ((uintptr_t)ws & 15))) {
     set_error(std::string(who) + ": workspace too small or misaligned"); return SPX_E_WORKSPACE;
   }
-  return SPX_OK;
+  return check_plan_device(pl, who);
 }
 
 int spx_jvp(const spx_plan* pl, const void* y, const void* v, void* Jv, void* ws, size_t ws_bytes,
@@ -985,6 +1001,7 @@ int spx_linearize(const spx_plan* pl, const void* y, void* lin, size_t lin_bytes
   if (((uintptr_t)y | (uintptr_t)lin) & 15) { set_error("spx_linearize: pointers must be 16-byte aligned"); return SPX_E_ARG; }
   if (lin_bytes < spx_linearize_bytes(pl)) { set_error("spx_linearize: lin too small"); return SPX_E_WORKSPACE; }
   if (int rb = refuse_big(pl, "spx_linearize")) return rb;
+  if (int rd = check_plan_device(pl, "spx_linearize")) return rd;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const DevPlan& P = pl->host;
   if (P.path == 0) {

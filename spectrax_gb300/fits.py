@@ -1,9 +1,9 @@
 """Damping / growth-rate fits of the field energy (host side).
 
 * Landau: gamma = slope/2 of a line fit of log E at the local maxima of E[:n]
-  (Examples/1D_Landau_damping_dr_curve.py:171-175: find_peaks, polyfit, /2).
+  (Examples/1D_Landau_damping_dr_curve.py:106-110: find_peaks, polyfit, /2).
 * Two-stream: gamma = slope/2 of a line fit of log E over samples [start:]
-  (Examples/1D_two_stream_gr_curve.py:165-168).
+  (Examples/1D_two_stream_gr_curve.py:101-104).
 * ``window_slope``: least-squares slope of log E over t in [ta, tb].
 """
 from __future__ import annotations

@@ -74,8 +74,9 @@ class Plan:
         self.check_state(y)
         self.check_state(dy, "dy")
         ws, nb = self.ws_ptr()
-        _lib.check(_lib.lib().spx_rhs(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(dy.data_ptr()),
-                                      ws, nb, _stream_ptr(stream)), "spx_rhs")
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().spx_rhs(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(dy.data_ptr()),
+                                          ws, nb, _stream_ptr(stream)), "spx_rhs")
         return dy
 
     def rhs(self, y: torch.Tensor, stream=None):
@@ -86,8 +87,9 @@ class Plan:
         for t, nm in ((y, "y"), (v, "v"), (out, "out")):
             self.check_state(t, nm)
         ws, nb = self.ws_ptr()
-        _lib.check(_lib.lib().spx_jvp(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(v.data_ptr()),
-                                      C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_jvp")
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().spx_jvp(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(v.data_ptr()),
+                                          C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_jvp")
         return out
 
     def linearize(self, y, lin=None, stream=None):
@@ -100,8 +102,9 @@ class Plan:
             lin = torch.empty(nb, dtype=torch.uint8, device=self.device)
         if lin.dtype != torch.uint8 or lin.numel() < nb or not lin.is_cuda or lin.device != self.device:
             raise ValueError(f"lin must be a uint8 CUDA tensor of {nb} bytes on {self.device}")
-        _lib.check(_lib.lib().spx_linearize(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(lin.data_ptr()),
-                                            C.c_size_t(lin.numel()), _stream_ptr(stream)), "spx_linearize")
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().spx_linearize(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(lin.data_ptr()),
+                                                C.c_size_t(lin.numel()), _stream_ptr(stream)), "spx_linearize")
         return lin
 
     @property
@@ -115,16 +118,19 @@ class Plan:
         if lin.numel() < self.linearize_bytes:
             raise ValueError("lin is too small for this plan")
         ws, nb = self.ws_ptr()
-        _lib.check(_lib.lib().spx_jvp_lin(self.handle, C.c_void_p(lin.data_ptr()), C.c_void_p(v.data_ptr()),
-                                          C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_jvp_lin")
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().spx_jvp_lin(self.handle, C.c_void_p(lin.data_ptr()), C.c_void_p(v.data_ptr()),
+                                              C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)),
+                       "spx_jvp_lin")
         return out
 
     def vjp_into(self, y, w, out, stream=None):
         for t, nm in ((y, "y"), (w, "w"), (out, "out")):
             self.check_state(t, nm)
         ws, nb = self.ws_ptr()
-        _lib.check(_lib.lib().spx_vjp(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
-                                      C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_vjp")
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().spx_vjp(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
+                                          C.c_void_p(out.data_ptr()), ws, nb, _stream_ptr(stream)), "spx_vjp")
         return out
 
     def vjp_noalloc_into(self, y, w, out, stream=None):
@@ -136,9 +142,10 @@ class Plan:
         calls that overlap on the GPU race."""
         for t, nm in ((y, "y"), (w, "w"), (out, "out")):
             self.check_state(t, nm)
-        _lib.check(_lib.lib().spx_vjp_noalloc(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
-                                              C.c_void_p(out.data_ptr()), _stream_ptr(stream)),
-                   "spx_vjp_noalloc")
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().spx_vjp_noalloc(self.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
+                                                  C.c_void_p(out.data_ptr()), _stream_ptr(stream)),
+                       "spx_vjp_noalloc")
         return out
 
     def __del__(self):

@@ -2,7 +2,7 @@
 
 Run once in a container that has the SPECTRAX source tree (read-only is fine):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the SPECTRAX source tree>
 
 JAX, Diffrax and orthax are not installable in that container, so this script
 installs a small NumPy stand-in for ``jax`` / ``jax.numpy`` / ``diffrax`` in
@@ -248,4 +248,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_golden.py <path to the SPECTRAX source tree>")
+    main(sys.argv[1])

@@ -2,7 +2,7 @@
 
 Run once in a container that has the SPECTRAX source tree:
 
-    python tests/golden/make_physics_golden.py /root/reference
+    python tests/golden/make_physics_golden.py <path to the SPECTRAX source tree>
 
 Reads Examples/damping_rate_1836.csv (Landau damping rate against k for
 mi/me = 1836, the physics behind the 1D1V Landau workload) and
@@ -29,4 +29,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else ".")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_physics_golden.py <path to the SPECTRAX source tree>")
+    main(sys.argv[1])

@@ -69,6 +69,9 @@ def test_no_cpu_fallback_in_product():
     (33, 11, 2, 33),
     (129, 43, 1, 129),   # always Nx
     (97, 32, 1, 97),
+    (64, 30, 0, 64),     # 3 cut > Nx: the Nx-point product folds more than one term, keep Nx
+    (64, 30, 2, 64),
+    (127, 43, 0, 127),
 ])
 def test_product_grid_choice_without_gpu(nx, cut, mode, expect):
     # host-side choice of the 1D1V stepper's product grid (no device call)
