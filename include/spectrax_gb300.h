@@ -281,8 +281,14 @@ typedef struct spx_dopri8_opts {
                            The symmetry is then kept exactly by every stage.  0: never. */
   int32_t persistent; /* 1: on the fused 1D1V path, run all attempts of a replay in one
                            cooperative launch whose CTAs chain stages through completion
-                           counters (used when every CTA fits on the GPU at once and the
-                           plan's product grid is Nx points); 0: one launch per stage. */
+                           counters (used when every CTA fits on the GPU at once, the
+                           plan's product grid is Nx points and saveat is 1); 0: one launch
+                           per stage. */
+  int32_t saveat;     /* 0: Diffrax SaveAt(ts) -- steps end only on t1 and a save time inside
+                           an accepted step gets the step's dense output (a degree-8
+                           continuous extension of the 13 stages: order 4, order 8 on linear
+                           problems); 1: every step is shortened to end on the next save
+                           time, which then gets the step's 8th-order solution. */
 } spx_dopri8_opts;
 
 typedef struct spx_dopri8 spx_dopri8;   /* opaque: stage buffers + CUDA graph */
@@ -349,6 +355,7 @@ typedef struct spx_batch_opts {
   const double* masses;  /* host, n x SPX_MAX_SPECIES species masses (NULL: ones) */
   int32_t hermitian;     /* 1: an instance with odd Nx whose initial state is exactly Hermitian
                             (C(-k) == conj C(k) on every line) uses packed real transforms */
+  int32_t saveat;        /* as spx_dopri8_opts.saveat: 0 dense output at save times, 1 land on them */
 } spx_batch_opts;
 
 typedef struct spx_batch_stats {

@@ -12,12 +12,19 @@ t0=0, t1=t_max, dt0=dt, SaveAt(ts=linspace(0, t_max, timesteps)), max_steps=1e6)
   safety=0.9, factormin=0.2, factormax=10, RMS norm, error order 8): the scaled
   error is rms(e / (atol + rtol*max(|y0|, |y1|))); a step is kept when it is < 1;
   the next step is h*clip(0.9*err**(-1/8), 1 if kept else 0.2, 10).
-* Save times: Diffrax interpolates between steps.  This stepper instead ends a
-  step exactly on each save time (and on t1); after such a shortened step the
-  next proposal is max(h*factor, the proposal before shortening).  This is a
-  deliberate difference (no dense-output interpolant is needed and the saved
-  states carry the full 8th-order accuracy); the GPU stepper uses the same rule,
-  so GPU and oracle take identical step sequences.
+* Save times, ``saveat="interpolate"`` (default, Diffrax's ``SaveAt(ts)``): steps
+  are shortened only to end on t1; a save time t0 < ts <= t0 + h inside an
+  accepted step gets y0 + h sum_j b_j(theta) K_j with theta = (ts - t0) / h
+  (y1 itself when ts is the step's end).  The weights b_j(theta) are DENSE
+  below: a continuous extension of the 13 stages derived for this project from
+  the continuous Runge-Kutta order conditions (Hairer, Norsett & Wanner, Solving
+  ODEs I, section II.6) -- order 4 for every problem, order 8 for linear
+  constant-coefficient problems, b_j(1) = b_j.  Diffrax's own interpolation
+  coefficients cannot be run here, so interpolated values are not pinned
+  against Diffrax.  ``saveat="land"``: every step is shortened to end exactly on
+  the next save time (and on t1); after such a shortened step the next proposal
+  is max(h*factor, the proposal before shortening).  The GPU steppers implement
+  both modes with the same rules, so GPU and oracle take identical step sequences.
 * A rejected step re-uses stage 1 (f at the same (t, y)).
 """
 from __future__ import annotations
@@ -80,6 +87,34 @@ B = np.array([float(b) for b in B_FR])
 BHAT = np.array([float(b) for b in BHAT_FR])
 E = B - BHAT   # error weights: double difference of the rounded weights (as on the device)
 
+# Dense-output weights: b_j(theta) = sum_k DENSE[j, k] theta^(k+1).  The same
+# table as the product's (spectrax_gb300/tableau.py); tests/test_oracle_dopri8.py
+# checks both copies against each other and against the continuous order conditions.
+DENSE = np.array([
+    (1.0225887543186571, -7.670667446945965, 27.66902547999488, -47.67183315927078, 33.46377681416232, -3.361471942445777, 0.26957683985605563, -3.6792478485278544),
+    (0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0),
+    (0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0),
+    (-0.4421091173902579, 26.406870536094136, -184.84492950380366, 374.8074642895895, -187.50765659853084, -73.24848874139202, -61.61212137671032, 106.44097051214344),
+    (-0.016770524832150593, 2.735344067839403, -15.823213818196452, 6.754222269863948, 67.35828119490084, -84.62711564401906, -3.1659125143845404, 26.785164968828003),
+    (-0.20072361599222294, -8.659354873704325, 72.41722019543212, -165.23218623775102, 90.616848420878, 61.44772288959279, -31.048069957854498, -19.39690914921209),
+    (0.47679757022986596, -18.47192139578695, 153.84604554310715, -313.37968335449574, 114.57740262576641, 108.03033023951768, 75.5465634628353, -120.38622188397257),
+    (0.35310813749263276, 11.831309677388939, -104.72989197836371, 263.54865955594886, -185.68620659496102, -33.61812083592465, 4.5915511514030305, 44.413101556419335),
+    (-0.34706253524185315, -10.277468293537797, 81.19210342937505, -171.80907405747308, 70.61744597042717, 53.04007650498896, 37.04680015843294, -60.222580790785855),
+    (0.167271748919783, 4.31464836855168, -31.385871758930698, 56.77008096780195, -5.458949831230438, -28.532677401284158, -22.06850757356576, 26.854568510659924),
+    (-0.022168741064052283, -0.32225129840321176, 2.9237861932636586, -8.095256512177215, 6.749080918411023, 0.3572991806069449, -0.4466502168100301, -0.9856520413169936),
+    (0.05916230417764668, 0.8225615831834081, -7.362035718957821, 20.157573514806085, -16.46387839878986, -1.0935974138000835, 0.9107258995550841, 2.7313786910726767),
+    (-0.05009398061804868, -0.7090709246793181, 6.0977619370794764, -15.849967276842577, 11.733855478966397, 1.6060431641593604, -0.02395587275725969, -2.5545725253080316),
+])
+
+
+def dense_weights(theta):
+    """b_j(theta), j = 0..12, by Horner's rule."""
+    b = DENSE[:, -1].copy()
+    for k in range(DENSE.shape[1] - 2, -1, -1):
+        b = b * theta + DENSE[:, k]
+    return b * theta
+
+
 SAFETY, FACTORMIN, FACTORMAX, ERROR_ORDER = 0.9, 0.2, 10.0, 8.0
 SNAP = 1e-9   # a step within SNAP*h of the next stop lands on it exactly
 
@@ -103,8 +138,8 @@ def controller_factor(errnorm, accepted):
     return min(max(f, lo), FACTORMAX)
 
 
-def dopri8_step(f, t, y, h, k1=None):
-    """One RK8(7)13M step.  Returns (y_new, err, k1)."""
+def dopri8_step(f, t, y, h, k1=None, stages=None):
+    """One RK8(7)13M step.  Returns (y_new, err, k1); ``stages`` (a list) receives the 13 K_j."""
     ks = [None] * STAGES
     ks[0] = f(t, y) if k1 is None else k1
     for i in range(1, STAGES):
@@ -119,17 +154,22 @@ def dopri8_step(f, t, y, h, k1=None):
             y_new = y_new + (h * B[j]) * ks[j]
         if E[j] != 0.0:
             err = err + (h * E[j]) * ks[j]
+    if stages is not None:
+        stages[:] = ks
     return y_new, err, ks[0]
 
 
 def solve(f, t0, t1, y0, dt0, ts=None, adaptive=True, rtol=1e-10, atol=1e-12,
-          max_steps=1_000_000, on_save=None):
-    """Integrate y' = f(t, y) from t0 to t1.
+          max_steps=1_000_000, on_save=None, saveat="interpolate"):
+    """Integrate y' = f(t, y) from t0 to t1 (``saveat``: "interpolate" or "land").
 
     Returns dict(ts, ys, accepted, rejected, rhs_evals, status).  ``on_save(i, y)``
     (optional) replaces storing every saved state.
     status: 0 ok, 1 max_steps reached, 2 step size underflow, 3 non-finite state.
     """
+    if saveat not in ("interpolate", "land"):
+        raise ValueError("saveat must be 'interpolate' or 'land'")
+    interp = saveat == "interpolate"
     ts = np.array([t1] if ts is None else ts, dtype=np.float64)
     y = np.array(y0, dtype=np.complex128)
     t = float(t0)
@@ -151,7 +191,7 @@ def solve(f, t0, t1, y0, dt0, ts=None, adaptive=True, rtol=1e-10, atol=1e-12,
         if acc + rej >= max_steps:
             status = 1
             break
-        t_stop = min(ts[isave], t1) if isave < len(ts) else t1
+        t_stop = min(ts[isave], t1) if (isave < len(ts) and not interp) else t1
         h = dt
         landed = False
         if t + h * (1.0 + SNAP) >= t_stop:
@@ -161,7 +201,8 @@ def solve(f, t0, t1, y0, dt0, ts=None, adaptive=True, rtol=1e-10, atol=1e-12,
             status = 2
             break
         evals += STAGES - (1 if k1 is not None else 0)
-        y_new, err, k1_now = dopri8_step(f, t, y, h, k1)
+        ks = []
+        y_new, err, k1_now = dopri8_step(f, t, y, h, k1, ks)
         if adaptive:
             en = rms_scaled_error(y, y_new, err, rtol, atol)
             accepted = en < 1.0
@@ -174,6 +215,7 @@ def solve(f, t0, t1, y0, dt0, ts=None, adaptive=True, rtol=1e-10, atol=1e-12,
             dt_next = dt
         if accepted:
             acc += 1
+            t_old, y_old = t, y
             y = y_new
             t = t_stop if landed else t + h
             k1 = None
@@ -181,7 +223,15 @@ def solve(f, t0, t1, y0, dt0, ts=None, adaptive=True, rtol=1e-10, atol=1e-12,
                 status = 3
                 break
             while isave < len(ts) and ts[isave] <= t:
-                save(isave, y)
+                if interp and ts[isave] != t:
+                    w = h * dense_weights((ts[isave] - t_old) / h)
+                    yi = y_old.copy()
+                    for j in range(STAGES):
+                        if DENSE[j].any():
+                            yi = yi + w[j] * ks[j]
+                    save(isave, yi)
+                else:
+                    save(isave, y)
                 isave += 1
         else:
             rej += 1

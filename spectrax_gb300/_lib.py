@@ -57,6 +57,7 @@ class spx_dopri8_opts(C.Structure):
         ("masses", C.POINTER(C.c_double)),
         ("hermitian", C.c_int32),
         ("persistent", C.c_int32),
+        ("saveat", C.c_int32),
     ]
 
 
@@ -78,6 +79,7 @@ class spx_batch_opts(C.Structure):
         ("cluster", C.c_int32), ("tile", C.c_int32),
         ("masses", C.POINTER(C.c_double)),
         ("hermitian", C.c_int32),
+        ("saveat", C.c_int32),
     ]
 
 

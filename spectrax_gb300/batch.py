@@ -64,7 +64,9 @@ def landau_scan(n=256, seed=0, amplitude=0.01, mask_mode="divide"):
 # ----------------------------------------------------------------- solver
 class BatchSolver:
     def __init__(self, problems, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, adaptive=True,
-                 max_steps=10_000_000, cluster=2, tile=8, masses=None, device=None, hermitian=True):
+                 max_steps=10_000_000, cluster=2, tile=8, masses=None, device=None, hermitian=True,
+                 saveat="interpolate"):
+        from .dopri8 import _saveat_code
         L = _lib.lib()
         self.n = len(problems)
         self.problems = list(problems)
@@ -87,6 +89,9 @@ class BatchSolver:
         o.masses = self._masses.ctypes.data_as(C.POINTER(C.c_double))
         # instances with odd Nx and an exactly Hermitian y0 use packed real transforms
         o.hermitian = 1 if hermitian else 0
+        # save times: dense output inside a step (Diffrax SaveAt(ts)) or steps landing on them
+        o.saveat = _saveat_code(saveat)
+        self.saveat = saveat
         self.cluster, self.tile = int(cluster), int(tile)
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         h = C.c_void_p()
@@ -204,7 +209,7 @@ def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses
 
 
 # ----------------------------------------------------------------- serial baseline
-def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermitian=False):
+def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermitian=False, saveat="interpolate"):
     """Solve the instances one after another with the single-instance device
     Dopri8 (plain GPU right-hand side per stage).  Returns (final states, stats,
     energies, seconds); the plans and solvers (device buffers, captured graphs)
@@ -216,7 +221,8 @@ def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermit
     for it in insts:
         plan = get_plan(it["problem"])
         solvers.append(Dopri8Solver(plan, 0.0, t1, dt0, ts=save_ts, adaptive=True, rtol=rtol, atol=atol,
-                                    save_states=False, masses=it.get("masses"), hermitian=hermitian))
+                                    save_states=False, masses=it.get("masses"), hermitian=hermitian,
+                                    saveat=saveat))
     y0s = [torch.from_numpy(it["y0"]).to(solvers[0].plan.device) for it in insts]
     finals, stats, ens = [], [], []
     torch.cuda.synchronize()

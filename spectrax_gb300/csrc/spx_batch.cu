@@ -64,6 +64,7 @@ struct BArgs {
   double t1, dt0, rtol, atol;
   long long max_steps;
   int adaptive;
+  int interp;             // 1: save times inside a step get the dense output (steps end only on t1)
   const int* order;
   unsigned int* next;
   int tab_max;
@@ -224,12 +225,13 @@ __device__ __forceinline__ double bsum(double v, double* red) {
 }
 
 // Energies of spectrax/_diagnostics.py:191-219 for state Y (whole CTA; thread 0 writes).
-__device__ void batch_energies(const DevPlan& P, const double2* Y, const double* masses, double* out,
-                               double* red) {
+// Energies of the state whose entries val(e) returns (valid in thread 0, which writes them).
+template <class V>
+__device__ void batch_energies(const DevPlan& P, V&& val, const double* masses, double* out, double* red) {
   const int N = P.ax[1].n;
   double em = 0.0;
   for (int i = threadIdx.x; i < 6 * N; i += blockDim.x) {
-    const double2 f = __ldcg(Y + P.nc + i);
+    const double2 f = val((size_t)P.nc + i);
     em = fma(f.x, f.x, fma(f.y, f.y, em));
   }
   em = bsum(em, red);
@@ -242,7 +244,7 @@ __device__ void batch_energies(const DevPlan& P, const double2* Y, const double*
     for (int s = 0; s < pb.Ns; ++s) {
       double c[7];
       for (int k = 0; k < 7; ++k)
-        c[k] = (offs[k] < Hs) ? __ldcg(Y + ((size_t)s * Hs + offs[k]) * N + kc).x : 0.0;
+        c[k] = (offs[k] < Hs) ? val(((size_t)s * Hs + offs[k]) * N + kc).x : 0.0;
       const double a0 = pb.alpha_s[3 * s], a1 = pb.alpha_s[3 * s + 1], a2 = pb.alpha_s[3 * s + 2];
       const double u0 = pb.u_s[3 * s], u1 = pb.u_s[3 * s + 1], u2 = pb.u_s[3 * s + 2];
       const double pref = 0.5 * masses[s] * a0 * a1 * a2;
@@ -276,6 +278,7 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
   __shared__ double red[NTHREADS / 32];
   __shared__ BTerms terms;
   __shared__ int s_bad;
+  __shared__ double s_w[rk::S];   // dense-output weights h b_j(theta) of one save time
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* stab = reinterpret_cast<double2*>(smem_raw);
   double2* sA = stab + (a.tab_max + 15) / 16 * 16;        // per-tile work area (work_max entries)
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
       while (hi < a.nsave && a.save_ts[hi] <= 0.0) ++hi;
       if (hi > 0) {
         if (crank == 0) {
-          batch_energies(P, Yb[0], I->masses, en, red);
+          batch_energies(P, [&](size_t e) { return __ldcg(Yb[0] + e); }, I->masses, en, red);
           __syncthreads();
           if (threadIdx.x == 0)
             for (int k = 1; k < hi; ++k)
@@ -348,7 +351,8 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
     __syncthreads();
     while (ctl.status == SPX_ST_RUNNING) {
       // attempt parameters (identical in every CTA of the cluster)
-      const double t_stop = (ctl.isave < a.nsave) ? fmin(a.save_ts[ctl.isave], a.t1) : a.t1;
+      const double t_stop = (ctl.isave < a.nsave && !a.interp) ? fmin(a.save_ts[ctl.isave], a.t1) : a.t1;
+      const double t_old = ctl.t;
       double h = ctl.dt;
       bool landed = false;
       if (ctl.t + h * (1.0 + rk::SNAP) >= t_stop) { h = t_stop - ctl.t; landed = true; }
@@ -465,14 +469,32 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
             while (hi < a.nsave && a.save_ts[hi] <= ctl.t) ++hi;
             if (hi > lo) {
               if (crank == 0) {
-                batch_energies(P, Yb[ctl.cur], I->masses, en + (size_t)lo * (2 + Ns), red);
-                __syncthreads();
-                if (threadIdx.x == 0)
-                  for (int k = lo + 1; k < hi; ++k)
-                    for (int q = 0; q < 2 + Ns; ++q) en[k * (2 + Ns) + q] = en[lo * (2 + Ns) + q];
+                // each save time: the state itself at the step's end (or in land-on-save
+                // mode), else the dense output y_old + sum_j h b_j(theta) K_j
+                const double2* Yn = Yb[ctl.cur];
+                const double2* Yo = Yb[ctl.cur ^ 1];
+                for (int k = lo; k < hi; ++k) {
+                  const double tsv = a.save_ts[k];
+                  const bool exact = !a.interp || tsv == ctl.t;
+                  if (threadIdx.x < rk::S)
+                    s_w[threadIdx.x] = exact ? 0.0 : h * rk::dense_weight(threadIdx.x, (tsv - t_old) / h);
+                  __syncthreads();
+                  auto val = [&](size_t e) -> double2 {
+                    if (exact) return __ldcg(Yn + e);
+                    double2 v = __ldcg(Yo + e);
+#pragma unroll 1
+                    for (int j = 0; j < rk::S; ++j)
+                      if (s_w[j] != 0.0) v = crfma(s_w[j], __ldcg(K + (size_t)j * len + e), v);
+                    return v;
+                  };
+                  batch_energies(P, val, I->masses, en + (size_t)k * (2 + Ns), red);
+                  __syncthreads();
+                }
               }
-              __syncthreads();
               if (threadIdx.x == 0) { ctl.isave = hi; ctl.saved = hi; }
+              // the next attempt's stage 0 (other ranks) overwrites K_0 read above
+              __threadfence();
+              cl.sync();
             }
           }
           __syncthreads();
@@ -576,7 +598,8 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   if (!pbs || !o || !out || n <= 0) { set_error("spx_batch_create: bad argument"); return SPX_E_ARG; }
   *out = nullptr;
   if (o->cluster < 1 || o->cluster > 16) { set_error("spx_batch_create: cluster must be 1..16"); return SPX_E_ARG; }
-  if (!(o->t1 >= 0.0) || !(o->dt0 > 0.0) || o->max_steps <= 0 || o->nsave < 0 || (o->nsave && !o->save_ts)) {
+  if (!(o->t1 >= 0.0) || !(o->dt0 > 0.0) || o->max_steps <= 0 || o->nsave < 0 || (o->nsave && !o->save_ts) ||
+      o->saveat < 0 || o->saveat > 1) {
     set_error("spx_batch_create: bad options"); return SPX_E_ARG;
   }
   int rc;
@@ -718,6 +741,7 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
   A.nsave = o->nsave;
   A.t1 = o->t1; A.dt0 = o->dt0; A.rtol = o->rtol; A.atol = o->atol;
   A.max_steps = o->max_steps; A.adaptive = o->adaptive ? 1 : 0;
+  A.interp = o->saveat == 0 ? 1 : 0;
   A.tab_max = tab_max;
   A.work_max = work_max;
   b->y_in = const_cast<double2*>(A.y_in);

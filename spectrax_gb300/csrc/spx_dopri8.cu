@@ -37,6 +37,9 @@ struct D8Dev {
   int herm;           // 1: the state is exactly Hermitian, stages use packed real transforms
   unsigned int att;       // attempts finished since reset (the persistent kernel's attempt barrier)
   unsigned int save_seq;  // incremented whenever an accepted step crosses save times
+  int interp;             // 1: save times inside a step are interpolated (steps end only on t1)
+  int spare;
+  double save_t0, save_h; // the accepted step a pending save interpolates ([t0, t0 + h]); h = 0: none
 };
 
 struct D8Args {
@@ -75,7 +78,7 @@ struct Attempt {
 
 __device__ __forceinline__ Attempt attempt_params(const D8Dev& s, const double* __restrict__ ts) {
   Attempt a;
-  a.t_stop = (s.isave < s.nsave) ? fmin(ts[s.isave], s.t1) : s.t1;
+  a.t_stop = (s.isave < s.nsave && !s.interp) ? fmin(ts[s.isave], s.t1) : s.t1;
   a.h = s.dt;
   a.landed = 0;
   if (s.t + a.h * (1.0 + rk::SNAP) >= a.t_stop) { a.h = a.t_stop - s.t; a.landed = 1; }
@@ -108,6 +111,7 @@ struct EpiLast {
   const double2* __restrict__ Y;
   const double2* __restrict__ K;
   double2* __restrict__ Ynew;
+  double2* __restrict__ K12;   // the last stage's K (read by the dense output)
   long long len;
   const double* hb;   // h b_j and h e_j (j <= 12), formed once per CTA
   const double* he;
@@ -131,6 +135,7 @@ struct EpiLast {
     yn = crfma(hb[12], v, yn);
     er = crfma(he[12], v, er);
     Ynew[e] = yn;
+    K12[e] = v;
     if (!(isfinite(yn.x) && isfinite(yn.y))) nonfinite = 1;
     if (adaptive) {
       const double m0 = fma(y0.x, y0.x, y0.y * y0.y), m1 = fma(yn.x, yn.x, yn.y * yn.y);
@@ -169,6 +174,8 @@ __device__ void finalize_step(const D8Args& a, const Attempt& at, double sum, in
   }
   st->evals += st->k1_valid ? (rk::S - 1) : rk::S;
   if (accept) {
+    st->save_t0 = st->t;
+    st->save_h = at.h;
     st->t = at.landed ? at.t_stop : st->t + at.h;
     st->cur ^= 1;
     st->accepted += 1;
@@ -362,45 +369,54 @@ __device__ __forceinline__ void load_state_l2(D8Dev& s, const D8Dev* st) {
   for (int i = 0; i < (int)(sizeof(D8Dev) / 8); ++i) dst[i] = __ldcg(src + i);
 }
 
-// Energies of one saved state (the formulas of k_d8_save), by one CTA through L2.
-__device__ void persist_energies(const D8Args& a, const DevPlan& P, const D8Dev& s, const double2* Y,
-                                 double* red) {
+// Energies of spectrax/_diagnostics.py:191-219 (EM, kinetic total, kinetic per
+// species) of the state whose entries val(e) returns, into e[0 .. 2 + Ns), by one
+// CTA (the result is valid in thread 0, which writes it).
+template <class V>
+__device__ void save_energies(const DevPlan& P, const double* masses, V&& val, double* out, double* red) {
   const spx_problem& pb = P.pb;
   const size_t pl = (size_t)P.plane;
   double em = 0.0;
   for (size_t i = threadIdx.x; i < 6 * pl; i += blockDim.x) {
-    const double2 f = __ldcg(Y + P.nc + i);
+    const double2 f = val((size_t)P.nc + i);
     em = fma(f.x, f.x, fma(f.y, f.y, em));
   }
   em = block_sum(em, red);
   if (threadIdx.x == 0) {
-    const int Ns = pb.Ns, Hs = P.nh;
+    const int Ns = pb.Ns;
+    const int Hs = P.nh;
     const int kc = ((P.ax[0].n / 2) * P.ax[1].n + P.ax[1].n / 2) * P.ax[2].n + P.ax[2].n / 2;
     const int offs[7] = {0, 1, pb.Nn, pb.Nn * pb.Nm, 2, 2 * pb.Nn, 2 * pb.Nn * pb.Nm};
     const double O0 = pb.Omega_cs[0];
-    const double EM = 0.5 * em * O0 * O0;
     double ke_tot = 0.0;
-    double kes[SPX_MAX_SPECIES];
     for (int sp = 0; sp < Ns; ++sp) {
       double c[7];
       for (int k = 0; k < 7; ++k)
-        c[k] = (offs[k] >= 0 && offs[k] < Hs) ? __ldcg(Y + ((size_t)sp * Hs + offs[k]) * pl + kc).x : 0.0;
+        c[k] = (offs[k] >= 0 && offs[k] < Hs) ? val(((size_t)sp * Hs + offs[k]) * pl + kc).x : 0.0;
       const double a0 = pb.alpha_s[3 * sp], a1 = pb.alpha_s[3 * sp + 1], a2 = pb.alpha_s[3 * sp + 2];
       const double u0 = pb.u_s[3 * sp], u1 = pb.u_s[3 * sp + 1], u2 = pb.u_s[3 * sp + 2];
-      const double m = a.masses[sp];
-      const double pref = 0.5 * m * a0 * a1 * a2;
+      const double pref = 0.5 * masses[sp] * a0 * a1 * a2;
       const double t0 = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) + (u0 * u0 + u1 * u1 + u2 * u2);
       const double t1 = 1.41421356237309504880 * (a0 * u0 * c[1] + a1 * u1 * c[2] + a2 * u2 * c[3]);
       const double t2 = 0.70710678118654752440 * (a0 * a0 * c[4] + a1 * a1 * c[5] + a2 * a2 * c[6]);
-      kes[sp] = pref * (t0 * c[0] + t1 + t2);
-      ke_tot += kes[sp];
+      out[2 + sp] = pref * (t0 * c[0] + t1 + t2);
+      ke_tot += out[2 + sp];
     }
-    for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
-      double* e = a.energies + (size_t)idx * (2 + Ns);
-      e[0] = EM;
-      e[1] = ke_tot;
-      for (int sp = 0; sp < Ns; ++sp) e[2 + sp] = kes[sp];
-    }
+    out[0] = 0.5 * em * O0 * O0;
+    out[1] = ke_tot;
+  }
+}
+
+// Energies of one saved state of the persistent kernel (land-on-save mode: the
+// state itself), by one CTA through L2, for every pending save index.
+__device__ void persist_energies(const D8Args& a, const DevPlan& P, const D8Dev& s, const double2* Y,
+                                 double* red) {
+  const int Ns = P.pb.Ns;
+  double* e0 = a.energies + (size_t)s.save_lo * (2 + Ns);
+  save_energies(P, a.masses, [&](size_t e) { return __ldcg(Y + e); }, e0, red);
+  if (threadIdx.x == 0) {
+    for (int idx = s.save_lo + 1; idx < s.save_hi; ++idx)
+      for (int q = 0; q < 2 + Ns; ++q) a.energies[(size_t)idx * (2 + Ns) + q] = e0[q];
     a.st->saved = s.save_hi;
   }
 }
@@ -589,7 +605,8 @@ __global__ void __launch_bounds__(GEN_THREADS, 1) k_d8_stage_gen(D8Args a, int s
       general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, epi);
     }
   } else {
-    EpiLast el{Y, a.K, pick(a.Y, s.cur ^ 1), a.len, hcs[0], hcs[1], s.rtol, s.atol, s.adaptive, 0.0, 0};
+    EpiLast el{Y, a.K, pick(a.Y, s.cur ^ 1), a.K + (size_t)(rk::S - 1) * a.len, a.len, hcs[0], hcs[1],
+               s.rtol, s.atol, s.adaptive, 0.0, 0};
     if (b == nplanes) maxwell_range(P, stab, in, 0, P.plane, el);
     else general_nl_plane(P, stab, in, a.ws, GB, b, sA, sB, el);
     last_stage_tail(a, at, el, red);
@@ -622,65 +639,46 @@ __global__ void __launch_bounds__(NTHREADS) k_d8_herm_check(const double2* __res
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicAnd(flag, 0);
 }
 
-// Save: copy the state for pending save indices and compute the energies of
-// spectrax/_diagnostics.py:191-219 (EM, kinetic total, kinetic per species).
+// Save: for every pending save index, the state at that save time -- the current
+// state when the time is the end of the accepted step (or in land-on-save mode),
+// otherwise the dense output y_old + sum_j h b_j(theta) K_j of the step just
+// accepted -- copied out if states are kept, and its energies.
 __global__ void __launch_bounds__(NTHREADS) k_d8_save(D8Args a) {
   __shared__ D8Dev s;
   __shared__ double red[NTHREADS / 32];
+  __shared__ double w[rk::S];
   pdl_wait_and_release();
   if (threadIdx.x == 0) s = *a.st;
   __syncthreads();
   if (!s.save_pending) return;
-  const double2* Y = pick(a.Y, s.cur);
-  if (a.saved) {
-    for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
-      double2* dst = a.saved + (size_t)idx * a.len;
-      for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.len;
-           i += (long long)gridDim.x * blockDim.x)
-        dst[i] = Y[i];
-    }
-  }
-  if (blockIdx.x != 0) return;
+  const double2* Yn = pick(a.Y, s.cur);
+  const double2* Yo = pick(a.Y, s.cur ^ 1);
+  const long long len = a.len;
   const DevPlan& P = *a.plan;
-  const spx_problem& pb = P.pb;
-  const size_t pl = (size_t)P.plane;
-  double em = 0.0;
-  for (size_t i = threadIdx.x; i < 6 * pl; i += blockDim.x) {
-    const double2 f = Y[P.nc + i];
-    em = fma(f.x, f.x, fma(f.y, f.y, em));
-  }
-  em = block_sum(em, red);
-  if (threadIdx.x == 0) {
-    const int Ns = pb.Ns;
-    const int Hs = P.nh;
-    const int kc = ((P.ax[0].n / 2) * P.ax[1].n + P.ax[1].n / 2) * P.ax[2].n + P.ax[2].n / 2;
-    const int offs[7] = {0, 1, pb.Nn, pb.Nn * pb.Nm, 2, 2 * pb.Nn, 2 * pb.Nn * pb.Nm};
-    const double O0 = pb.Omega_cs[0];
-    const double EM = 0.5 * em * O0 * O0;
-    double ke_tot = 0.0;
-    double kes[SPX_MAX_SPECIES];
-    for (int sp = 0; sp < Ns; ++sp) {
-      double c[7];
-      for (int k = 0; k < 7; ++k)
-        c[k] = (offs[k] >= 0 && offs[k] < Hs) ? Y[((size_t)sp * Hs + offs[k]) * pl + kc].x : 0.0;
-      const double a0 = pb.alpha_s[3 * sp], a1 = pb.alpha_s[3 * sp + 1], a2 = pb.alpha_s[3 * sp + 2];
-      const double u0 = pb.u_s[3 * sp], u1 = pb.u_s[3 * sp + 1], u2 = pb.u_s[3 * sp + 2];
-      const double m = a.masses[sp];
-      const double pref = 0.5 * m * a0 * a1 * a2;
-      const double t0 = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2) + (u0 * u0 + u1 * u1 + u2 * u2);
-      const double t1 = 1.41421356237309504880 * (a0 * u0 * c[1] + a1 * u1 * c[2] + a2 * u2 * c[3]);
-      const double t2 = 0.70710678118654752440 * (a0 * a0 * c[4] + a1 * a1 * c[5] + a2 * a2 * c[6]);
-      kes[sp] = pref * (t0 * c[0] + t1 + t2);
-      ke_tot += kes[sp];
+  for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
+    const double tsv = a.save_ts[idx];
+    const bool exact = !s.interp || s.save_h == 0.0 || tsv == s.t;
+    if (threadIdx.x < rk::S)
+      w[threadIdx.x] = exact ? 0.0 : s.save_h * rk::dense_weight(threadIdx.x, (tsv - s.save_t0) / s.save_h);
+    __syncthreads();
+    auto val = [&](size_t e) -> double2 {
+      if (exact) return Yn[e];
+      double2 v = Yo[e];
+#pragma unroll 1
+      for (int j = 0; j < rk::S; ++j)
+        if (w[j] != 0.0) v = crfma(w[j], a.K[(size_t)j * len + e], v);
+      return v;
+    };
+    if (a.saved) {
+      double2* dst = a.saved + (size_t)idx * len;
+      for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len;
+           i += (long long)gridDim.x * blockDim.x)
+        dst[i] = val((size_t)i);
     }
-    for (int idx = s.save_lo; idx < s.save_hi; ++idx) {
-      double* e = a.energies + (size_t)idx * (2 + Ns);
-      e[0] = EM;
-      e[1] = ke_tot;
-      for (int sp = 0; sp < Ns; ++sp) e[2 + sp] = kes[sp];
-    }
-    a.st->saved = s.save_hi;
+    if (blockIdx.x == 0) save_energies(P, a.masses, val, a.energies + (size_t)idx * (2 + P.pb.Ns), red);
+    __syncthreads();
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.st->saved = s.save_hi;
 }
 
 }  // namespace spx
@@ -827,7 +825,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   *out = nullptr;
   if (int rd = check_plan_device(plan, "spx_dopri8_create")) return rd;
   if (!(o->t1 >= o->t0) || !(o->dt0 > 0.0) || o->nsave < 0 || (o->nsave > 0 && !o->save_ts) ||
-      o->max_steps <= 0) {
+      o->max_steps <= 0 || o->saveat < 0 || o->saveat > 1) {
     set_error("spx_dopri8_create: bad options"); return SPX_E_ARG;
   }
   if (o->adaptive && !(o->rtol >= 0.0 && o->atol >= 0.0 && o->rtol + o->atol > 0.0)) {
@@ -861,7 +859,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
     if (ea != cudaSuccess) { delete s; return cuda_fail(ea, "cudaFuncGetAttributes"); }
     s->smem_stage = stage_smem_1v(plan, fa.sharedSizeBytes, &npf);
     if (npf < 1) { delete s; set_error("Nx / tile too large for the Dopri8 stage kernel"); return SPX_E_UNSUPPORTED; }
-    if (o->persistent && P.axm.n == P.ax[1].n) {
+    if (o->persistent && o->saveat == 1 && P.axm.n == P.ax[1].n) {
       // the persistent kernel needs every CTA resident at once (a cooperative launch);
       // it is compiled for the Nx-point product grid only (its register budget)
       int coop = 0, per_sm = 0;
@@ -925,6 +923,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   I.t = o->t0; I.t0 = o->t0; I.t1 = o->t1; I.dt = o->dt0;
   I.rtol = o->rtol; I.atol = o->atol; I.adaptive = o->adaptive ? 1 : 0;
   I.max_steps = o->max_steps; I.nsave = o->nsave; I.status = SPX_ST_RUNNING;
+  I.interp = o->saveat == 0 ? 1 : 0;
   if (o->hermitian && P.path == 0 && (P.ax[1].n & 1)) {
     // the streaming and Maxwell terms keep the symmetry only if k(N-1-c) == -k(c) exactly
     const int N = P.ax[1].n;

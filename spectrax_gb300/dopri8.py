@@ -6,6 +6,13 @@ constant step).  ``simulation`` mirrors the reference driver: it builds the
 merged parameters, integrates from 0 to t_max saving at
 ``linspace(0, t_max, timesteps)``, and returns the same output dictionary
 (Ck, Fk, time, dCk, the parameters and the energy diagnostics).
+
+Save times follow Diffrax's ``SaveAt(ts)`` by default (``saveat="interpolate"``):
+steps are shortened only to end on t_max, and a save time inside an accepted
+step gets that step's dense output (``tableau.DENSE``: a degree-8 continuous
+extension of the 13 stages, order 4 for every problem and order 8 on linear
+ones).  ``saveat="land"`` instead shortens steps to end exactly on every save
+time.
 """
 from __future__ import annotations
 
@@ -31,10 +38,19 @@ def species_masses(params):
     return np.ones(Ns)
 
 
+_SAVEAT_MODES = {"interpolate": 0, "land": 1}
+
+
+def _saveat_code(saveat: str) -> int:
+    if saveat not in _SAVEAT_MODES:
+        raise ValueError("saveat must be 'interpolate' (Diffrax SaveAt(ts)) or 'land'")
+    return _SAVEAT_MODES[saveat]
+
+
 class Dopri8Solver:
     def __init__(self, plan: Plan, t0: float, t1: float, dt0: float, ts=None, adaptive=True,
                  rtol=1e-10, atol=1e-12, max_steps=1_000_000, save_states=True, masses=None,
-                 hermitian=True, persistent=False):
+                 hermitian=True, persistent=False, saveat="interpolate"):
         L = _lib.lib()
         self.plan = plan
         self.ts = np.ascontiguousarray(np.asarray([] if ts is None else ts, np.float64))
@@ -54,8 +70,10 @@ class Dopri8Solver:
         o.hermitian = 1 if hermitian else 0
         # optional: one cooperative launch per replay, stages chained by per-CTA
         # completion counters (same results bit for bit; not faster on the
-        # two-stream workload, where the stages are FP64-issue bound)
+        # two-stream workload, where the stages are FP64-issue bound); land mode only
         o.persistent = 1 if persistent else 0
+        o.saveat = _saveat_code(saveat)
+        self.saveat = saveat
         self.save_states = bool(save_states)
         h = C.c_void_p()
         with torch.cuda.device(plan.device):
@@ -142,7 +160,7 @@ def _controller_factor(en: float, accepted: bool) -> float:
 
 
 def host_dopri8_solve(plan: Plan, y0, t1: float, dt0: float, ts=None, adaptive=True, rtol=1e-10,
-                      atol=1e-12, max_steps=1_000_000, stream=None):
+                      atol=1e-12, max_steps=1_000_000, stream=None, saveat="interpolate"):
     """Dopri8 driven from the host around the plain right-hand side ``plan.rhs_into``.
 
     This is how an external solver uses the drop-in vector field (the role
@@ -151,7 +169,8 @@ def host_dopri8_solve(plan: Plan, y0, t1: float, dt0: float, ts=None, adaptive=T
     step-size decision on the host after each attempt (one device-to-host read
     per step).  Same tableau, controller and save-time rule as the device
     solver.  Returns (final state, saved states (len(ts), n), stats dict)."""
-    from .tableau import A, B, E
+    from .tableau import A, B, DENSE, E, dense_weights
+    interp = _saveat_code(saveat) == 0
     y = torch.as_tensor(y0).to(plan.device, torch.complex128).contiguous().clone()
     plan.check_state(y, "y0")
     ts = np.asarray([] if ts is None else ts, np.float64)
@@ -169,7 +188,7 @@ def host_dopri8_solve(plan: Plan, y0, t1: float, dt0: float, ts=None, adaptive=T
     k1_valid = False
     status = "DONE" if t >= t1 else "RUNNING"
     while status == "RUNNING":
-        t_stop = min(ts[isave], t1) if isave < len(ts) else t1
+        t_stop = min(ts[isave], t1) if (isave < len(ts) and not interp) else t1
         h, landed = dt, False
         if t + h * (1.0 + _SNAP) >= t_stop:
             h, landed = t_stop - t, True
@@ -211,12 +230,21 @@ def host_dopri8_solve(plan: Plan, y0, t1: float, dt0: float, ts=None, adaptive=T
         else:
             accept, dt_next = True, dt
         if accept:
+            t_old = t
             t = t_stop if landed else t + h
             y, ynew = ynew, y
             acc += 1
             k1_valid = False
             while isave < len(ts) and ts[isave] <= t:
-                saved[isave].copy_(y)
+                if interp and ts[isave] != t:
+                    # dense output of the step just taken (ynew now holds its start)
+                    w = dense_weights((ts[isave] - t_old) / h)
+                    saved[isave].copy_(ynew)
+                    for j in range(13):
+                        if any(DENSE[j]):
+                            saved[isave].add_(K[j], alpha=h * w[j])
+                else:
+                    saved[isave].copy_(y)
                 isave += 1
             if nonfinite:
                 status = "NONFINITE"
@@ -230,7 +258,7 @@ def host_dopri8_solve(plan: Plan, y0, t1: float, dt0: float, ts=None, adaptive=T
 
 
 def solve(params, y0=None, t_max=None, dt=None, ts=None, adaptive=True, rtol=None, atol=None,
-          max_steps=1_000_000, save_states=True, mask_mode=None):
+          max_steps=1_000_000, save_states=True, mask_mode=None, saveat="interpolate"):
     """Integrate one instance; returns (solver, status)."""
     plan = plan_for_params(params, mask_mode)
     y0 = initial_state(params) if y0 is None else y0
@@ -239,15 +267,20 @@ def solve(params, y0=None, t_max=None, dt=None, ts=None, adaptive=True, rtol=Non
     tol = float(params.get("ode_tolerance", 1e-12))
     s = Dopri8Solver(plan, 0.0, t_max, dt, ts=ts, adaptive=adaptive,
                      rtol=tol if rtol is None else rtol, atol=tol if atol is None else atol,
-                     max_steps=max_steps, save_states=save_states, masses=species_masses(params))
+                     max_steps=max_steps, save_states=save_states, masses=species_masses(params),
+                     saveat=saveat)
     s.reset(torch.as_tensor(np.asarray(y0, np.complex128)))
     status = s.run()
     return s, status
 
 
 def simulation(input_parameters=None, Nx=33, Ny=1, Nz=1, Nn=20, Nm=1, Np=1, Ns=2, timesteps=200,
-               dt=0.01, solver=None, adaptive_time_step=True, mask_mode=None, max_steps=1_000_000):
-    """Mirror of spectrax/_simulation.py:113-194 running on the GPU."""
+               dt=0.01, solver=None, adaptive_time_step=True, mask_mode=None, max_steps=1_000_000,
+               saveat="interpolate"):
+    """Mirror of spectrax/_simulation.py:113-194 running on the GPU.
+
+    ``saveat``: "interpolate" (the reference's Diffrax ``SaveAt(ts)``: dense
+    output at the save times) or "land" (steps end on every save time)."""
     solver = Dopri8() if solver is None else solver
     p = initialize_simulation_parameters(input_parameters or {}, Nx, Ny, Nz, Nn, Nm, Np, Ns, timesteps, dt)
     time = np.linspace(0, p["t_max"], timesteps)
@@ -261,7 +294,8 @@ def simulation(input_parameters=None, Nx=33, Ny=1, Nz=1, Nn=20, Nm=1, Np=1, Ns=2
         from .midpoint import energies
         tol = float(p.get("ode_tolerance", 1e-12))
         _, saved, info = host_dopri8_solve(plan, initial_state(p), float(time[-1]), dt, ts=time,
-                                           adaptive=adaptive_time_step, rtol=tol, atol=tol, max_steps=max_steps)
+                                           adaptive=adaptive_time_step, rtol=tol, atol=tol, max_steps=max_steps,
+                                           saveat=saveat)
         if info["status_name"] != "DONE":
             raise RuntimeError(f"Dopri8 solve ended with status {info['status_name']}")
         masses = species_masses(p)
@@ -269,7 +303,7 @@ def simulation(input_parameters=None, Nx=33, Ny=1, Nz=1, Nn=20, Nm=1, Np=1, Ns=2
         ys = saved.cpu().numpy()
     else:
         s, status = solve(p, ts=time, adaptive=adaptive_time_step, dt=dt, max_steps=max_steps,
-                          mask_mode=mask_mode)
+                          mask_mode=mask_mode, saveat=saveat)
         if status not in (1,):
             raise RuntimeError(f"Dopri8 solve ended with status {_lib.STATUS_NAMES.get(status, status)}")
         ys = s.saved_states().cpu().numpy()

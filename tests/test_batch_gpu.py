@@ -51,6 +51,38 @@ def test_batch_matches_serial(cluster, tile):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("saveat", ["interpolate", "land"])
+def test_batch_save_modes_match_oracle(saveat):
+    # energies at 21 save times (several inside one step when interpolating)
+    # against the oracle's states in the same save mode; identical step counts
+    from oracle import diag as odiag
+    from oracle import dopri8 as od
+    from oracle import rhs as orhs
+    from oracle import tables as otab
+    from spectrax_gb300.batch import BatchSolver
+    insts = _small_insts(2)[:3]
+    ts = np.linspace(0.0, 0.6, 21)
+    b = BatchSolver([it["problem"] for it in insts], 0.6, dt0=0.02, rtol=1e-10, atol=1e-10, save_ts=ts,
+                    cluster=2, tile=4, masses=[it["masses"] for it in insts], saveat=saveat)
+    b.unpack(b.run(b.pack([it["y0"] for it in insts])))
+    stats, ens = b.results()
+    for i, it in enumerate(insts):
+        pb = it["problem"]
+        user = dict(Lx=pb.Lx, nu=pb.nu, qs=[-1.0, 1.0], alpha_s=list(pb.alpha_s)[:6], u_s=[0.0] * 6,
+                    Omega_cs=[1.0, 1 / 1836.0], mi_me=1836.0)
+        p = otab.initialize_simulation_parameters(user, *it["shape"], 5, 0.02)
+        ref = od.solve(lambda t, y: orhs.rhs(p, y), 0.0, 0.6, it["y0"], 0.02, ts=ts, adaptive=True,
+                       rtol=1e-10, atol=1e-10, saveat=saveat)
+        assert stats[i]["accepted"] == ref["accepted"] and stats[i]["rejected"] == ref["rejected"]
+        assert stats[i]["saved"] == len(ts)
+        Nx, Ny, Nz, Nn, Nm, Np, Ns = it["shape"]
+        e_ref = odiag.energies(ref["ys"], Nx, Ny, Nz, Nn, Nm, Np, Ns, p["alpha_s"], p["u_s"], p["Omega_cs"],
+                               mi_me=1836.0)
+        np.testing.assert_allclose(ens[i][:, 0], e_ref["EM_energy"], rtol=1e-9)
+        np.testing.assert_allclose(ens[i][:, 1], e_ref["kinetic_energy"].real, rtol=1e-9)
+
+
+@pytest.mark.gpu
 def test_batch_matches_oracle():
     import torch
     from oracle import dopri8 as od

@@ -34,38 +34,45 @@ def _y0(shape, seed=1, amp=0.01):
     return y
 
 
-def _run_gpu(p, y0, t1, dt, ts, adaptive, rtol=1e-10, atol=1e-12, max_steps=100000):
+def _run_gpu(p, y0, t1, dt, ts, adaptive, rtol=1e-10, atol=1e-12, max_steps=100000, saveat="interpolate"):
     import torch
     from spectrax_gb300 import dopri8, vector_field
     plan = vector_field.plan_for_params(p, "divide")
     s = dopri8.Dopri8Solver(plan, 0.0, t1, dt, ts=ts, adaptive=adaptive, rtol=rtol, atol=atol,
-                            max_steps=max_steps, masses=dopri8.species_masses(p))
+                            max_steps=max_steps, masses=dopri8.species_masses(p), saveat=saveat)
     s.reset(torch.from_numpy(y0))
     st = s.run()
     return s, st
 
 
 CASES = [
-    ("1v_fixed", (17, 1, 1, 12, 1, 1, 2), False, 0.05, 1.0),
-    ("1v_adaptive", (33, 1, 1, 16, 1, 1, 3), True, 0.01, 1.5),
-    ("gen_fixed", (6, 5, 1, 2, 2, 2, 2), False, 0.02, 0.2),
-    ("gen_adaptive", (5, 1, 4, 3, 2, 2, 1), True, 0.01, 0.3),
+    ("1v_fixed", (17, 1, 1, 12, 1, 1, 2), False, 0.05, 1.0, 6),
+    ("1v_adaptive", (33, 1, 1, 16, 1, 1, 3), True, 0.01, 1.5, 6),
+    ("1v_dense_saves", (33, 1, 1, 16, 1, 1, 3), True, 0.01, 1.5, 61),   # several saves inside one step
+    ("1v_fixed_off_grid", (17, 1, 1, 12, 1, 1, 2), False, 0.07, 1.0, 9),
+    ("gen_fixed", (6, 5, 1, 2, 2, 2, 2), False, 0.02, 0.2, 6),
+    ("gen_adaptive", (5, 1, 4, 3, 2, 2, 1), True, 0.01, 0.3, 6),
+    ("gen_dense_saves", (5, 1, 4, 3, 2, 2, 1), True, 0.01, 0.3, 31),
 ]
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name,shape,adaptive,dt,t1", CASES, ids=[c[0] for c in CASES])
-def test_dopri8_matches_oracle(name, shape, adaptive, dt, t1):
+@pytest.mark.parametrize("saveat", ["interpolate", "land"])
+@pytest.mark.parametrize("name,shape,adaptive,dt,t1,nts", CASES, ids=[c[0] for c in CASES])
+def test_dopri8_matches_oracle(name, shape, adaptive, dt, t1, nts, saveat):
+    # identical step sequences (accepted, rejected, RHS evaluations) in both save
+    # modes; saved states (interpolated or landed on) within 1e-10
     p = _params(shape)
     y0 = _y0(shape)
-    ts = np.linspace(0.0, t1, 6)
+    ts = np.linspace(0.0, t1, nts)
     f = lambda t, y: orhs.rhs(p, y, "divide")
-    ref = od.solve(f, 0.0, t1, y0, dt, ts=ts, adaptive=adaptive, rtol=1e-10, atol=1e-12)
-    s, st = _run_gpu(p, y0, t1, dt, ts, adaptive)
+    ref = od.solve(f, 0.0, t1, y0, dt, ts=ts, adaptive=adaptive, rtol=1e-10, atol=1e-12, saveat=saveat)
+    s, st = _run_gpu(p, y0, t1, dt, ts, adaptive, saveat=saveat)
     assert st == 1
     info = s.stats()
     assert info["accepted"] == ref["accepted"] and info["rejected"] == ref["rejected"], (info, ref)
     assert info["rhs_evals"] == ref["rhs_evals"]
+    assert info["saved"] == nts
     ys = s.saved_states().cpu().numpy()
     assert rel_err(ys, ref["ys"]) < 1e-10
     Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
@@ -120,18 +127,20 @@ def test_simulation_driver_defaults():
 
 
 @pytest.mark.gpu
-def test_host_driven_dopri8_matches_oracle():
+@pytest.mark.parametrize("saveat", ["interpolate", "land"])
+def test_host_driven_dopri8_matches_oracle(saveat):
     # the plain RHS driven from the host (external-solver use of the drop-in)
     import torch
     from spectrax_gb300 import dopri8, vector_field
     shape = (33, 1, 1, 16, 1, 1, 3)
     p = _params(shape)
     y0 = _y0(shape)
-    ts = np.linspace(0.0, 1.0, 5)
+    ts = np.linspace(0.0, 1.0, 23)
     ref = od.solve(lambda t, y: orhs.rhs(p, y, "divide"), 0.0, 1.0, y0, 0.01, ts=ts, adaptive=True,
-                   rtol=1e-10, atol=1e-12)
+                   rtol=1e-10, atol=1e-12, saveat=saveat)
     plan = vector_field.plan_for_params(p, "divide")
-    y, ys, st = dopri8.host_dopri8_solve(plan, torch.from_numpy(y0), 1.0, 0.01, ts=ts, rtol=1e-10, atol=1e-12)
+    y, ys, st = dopri8.host_dopri8_solve(plan, torch.from_numpy(y0), 1.0, 0.01, ts=ts, rtol=1e-10, atol=1e-12,
+                                         saveat=saveat)
     assert st["status_name"] == "DONE"
     assert st["accepted"] == ref["accepted"] and st["rejected"] == ref["rejected"], (st, ref)
     assert rel_err(ys.cpu().numpy(), ref["ys"]) < 1e-10

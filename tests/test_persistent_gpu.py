@@ -33,7 +33,8 @@ def _run(plan, p, y0, t1, dt, ts, adaptive, persistent, max_steps=100000):
     import torch
     from spectrax_gb300 import dopri8
     s = dopri8.Dopri8Solver(plan, 0.0, t1, dt, ts=ts, adaptive=adaptive, rtol=1e-10, atol=1e-12,
-                            max_steps=max_steps, masses=dopri8.species_masses(p), persistent=persistent)
+                            max_steps=max_steps, masses=dopri8.species_masses(p), persistent=persistent,
+                            saveat="land")
     s.reset(torch.from_numpy(y0))
     status = s.run()
     return s, status

@@ -86,7 +86,8 @@ def test_persistent_request_falls_back_on_a_product_grid():
         out = []
         for persistent in (True, False):
             s = dopri8.Dopri8Solver(plan, 0.0, 0.1, 0.02, ts=np.linspace(0, 0.1, 3), adaptive=False,
-                                    max_steps=20, masses=[1.0, 1.0], persistent=persistent)
+                                    max_steps=20, masses=[1.0, 1.0], persistent=persistent,
+                                    saveat="land")
             s.reset(torch.from_numpy(y0))
             assert s.run() == 1
             assert not s.stats()["persistent"]
