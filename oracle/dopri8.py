@@ -238,7 +238,7 @@ def solve(f, t0, t1, y0, dt0, ts=None, adaptive=True, rtol=1e-10, atol=1e-12,
             k1 = k1_now
         dt = dt_next
     ys = np.stack(saved) if saved else None
-    return dict(ts=ts, ys=ys, accepted=acc, rejected=rej, rhs_evals=evals, status=status, t=t)
+    return dict(ts=ts, ys=ys, accepted=acc, rejected=rej, rhs_evals=evals, status=status, t=t, y=y)
 
 
 # ----------------------------------------------------------------- order conditions

@@ -42,3 +42,101 @@ def step(f, y0, dt, rtol=1e-10, atol=1e-10, max_iters=300):
         y1 = y1 + np.linalg.solve(JF, -res)
         iters += 1
     return y1, y1 - y1_init, iters
+
+
+def jvp_quadratic(f, y, v):
+    """J(y) v of a right-hand side that is affine plus quadratic in y (this one is:
+    every term is linear in Ck or bilinear in (Fk, Ck)): the central difference
+    (f(y + v) - f(y - v)) / 2 is then exact up to rounding, for any size of v."""
+    return 0.5 * (f(y + v) - f(y - v))
+
+
+def gmres(matvec, b, restart=30, tol=1e-10, maxiter=20):
+    """Restarted GMRES(restart) for A x = b from x = 0, stopping when the residual
+    is below tol * ||b||; Gram-Schmidt with one re-orthogonalisation pass and
+    Givens rotations.  Returns (x, relative residual, matrix-vector products)."""
+    n = len(b)
+    x = np.zeros(n, np.complex128)
+    bnorm = np.linalg.norm(b)
+    if bnorm == 0.0:
+        return x, 0.0, 0
+    r = b.copy()
+    beta = bnorm
+    its = 0
+    for _ in range(maxiter):
+        V = np.empty((restart + 1, n), np.complex128)
+        V[0] = r / beta
+        H = np.zeros((restart + 1, restart), np.complex128)
+        g = np.zeros(restart + 1, np.complex128)
+        g[0] = beta
+        cs = np.zeros(restart, np.complex128)
+        sn = np.zeros(restart, np.complex128)
+        k = 0
+        for j in range(restart):
+            w = matvec(V[j])
+            its += 1
+            for _pass in range(2):
+                for i in range(j + 1):
+                    hij = np.vdot(V[i], w)
+                    H[i, j] += hij
+                    w = w - hij * V[i]
+            hn = np.linalg.norm(w)
+            H[j + 1, j] = hn
+            for i in range(j):
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = -np.conj(sn[i]) * H[i, j] + np.conj(cs[i]) * H[i + 1, j]
+                H[i, j] = t
+            a, bb = H[j, j], H[j + 1, j]
+            den = np.hypot(abs(a), abs(bb))
+            if den == 0.0:
+                cs[j], sn[j] = 1.0, 0.0
+            elif abs(a) > 0:
+                cs[j], sn[j] = abs(a) / den, (a / abs(a)) * np.conj(bb) / den
+            else:
+                cs[j], sn[j] = 0.0, np.conj(bb) / den
+            H[j, j] = cs[j] * a + sn[j] * bb
+            H[j + 1, j] = 0.0
+            g[j + 1] = -np.conj(sn[j]) * g[j]
+            g[j] = cs[j] * g[j]
+            k = j + 1
+            if hn > 0.0:
+                V[j + 1] = w / hn
+            if abs(g[j + 1]) <= tol * bnorm or hn == 0.0:
+                break
+        yk = np.linalg.solve(np.triu(H[:k, :k]), g[:k])
+        x = x + yk @ V[:k]
+        r = b - matvec(x)
+        its += 1
+        beta = np.linalg.norm(r)
+        if beta <= tol * bnorm:
+            break
+    return x, beta / bnorm, its
+
+
+def step_newton_gmres(f, y0, dt, rtol=1e-10, atol=1e-10, max_iters=300, restart=30, gmres_tol=1e-10,
+                      gmres_maxiter=20):
+    """Matrix-free implicit midpoint step for large states.
+
+    The Newton loop of spectrax/midpoint_solver.py:56-98 (residual F(y1) =
+    y1 - y0 - dt f((y0 + y1)/2); a scaled 2-norm below 1 stops; the Newton
+    system (I - dt/2 J(y_mid)) delta = -F linearised at the current iterate)
+    with each system solved by restarted GMRES(restart) to the relative
+    tolerance gmres_tol (restart 30 / tol 1e-10 by default, a deliberate
+    difference from the reference's Eisenstat-Walker tolerance); J v from
+    ``jvp_quadratic``.  Returns (y1, y_error, Newton iterations, products)."""
+    f0 = f(y0)
+    y1_init = y0 + dt * f0
+    y1 = y1_init.copy()
+    newton = mv = 0
+    for _ in range(max_iters):
+        ymid = 0.5 * (y0 + y1)
+        res = y1 - y0 - dt * f(ymid)
+        scale = atol + rtol * np.maximum(np.abs(y0), np.abs(y1))
+        if np.linalg.norm(res / scale) < 1.0:
+            break
+        delta, _rel, its = gmres(lambda v: v - 0.5 * dt * jvp_quadratic(f, ymid, v), -res, restart, gmres_tol,
+                                 gmres_maxiter)
+        y1 = y1 + delta
+        newton += 1
+        mv += its
+    return y1, y1 - y1_init, newton, mv
