@@ -76,3 +76,41 @@ def test_device_maxwellian_matches_host(Ns, Nn, Nm, Np, Ny, Nx, Nz):
     assert rel_err(got.cpu().numpy(), ref) < 1e-13
     Fref = np.fft.fftshift(np.fft.fftn(F, axes=(-3, -2, -1), norm="forward"), axes=(-3, -2, -1))
     assert rel_err(Fk.cpu().numpy(), Fref) < 1e-13
+
+
+def _builders():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "builders.npz"))
+
+
+def test_restatements_match_reference_builder_vectors():
+    # the host Maxwellian builder and the f(x, v) oracle against vectors made by
+    # running spectrax/_initialize_maxwellian.py and spectrax/_inverse_transform.py
+    from spectrax_gb300.maxwellian import compute_C_nmp
+    g = _builders()
+    for i in range(3):
+        Ns, Nn, Nm, Np, Ny, Nx, Nz = (int(v) for v in g[f"mx{i}/shape"])
+        got = compute_C_nmp(g[f"mx{i}/Us"], g[f"mx{i}/alpha"], g[f"mx{i}/u"], Nn, Nm, Np, Ns)
+        assert rel_err(got, g[f"mx{i}/Ck"]) < 1e-14
+    for i in range(3):
+        Nn, Nm, Np = (int(v) for v in g[f"inv{i}/shape"][:3])
+        got = oinv.inverse_HF_transform(g[f"inv{i}/Ck"], Nn, Nm, Np, g[f"inv{i}/xi_x"], g[f"inv{i}/xi_y"],
+                                        g[f"inv{i}/xi_z"])
+        assert rel_err(got, g[f"inv{i}/f"]) < 1e-14
+
+
+@pytest.mark.gpu
+def test_device_builders_match_reference_vectors():
+    # spx_maxwellian and the device f(x, v) reconstruction against the reference's own output
+    from spectrax_gb300.inverse_transform import inverse_HF_transform
+    from spectrax_gb300.maxwellian import compute_C_nmp_device
+    g = _builders()
+    for i in range(3):
+        Ns, Nn, Nm, Np, Ny, Nx, Nz = (int(v) for v in g[f"mx{i}/shape"])
+        got, _ = compute_C_nmp_device(g[f"mx{i}/Us"], g[f"mx{i}/alpha"], g[f"mx{i}/u"], Nn, Nm, Np, Ns)
+        assert rel_err(got.cpu().numpy(), g[f"mx{i}/Ck"]) < 1e-13
+    for i in range(3):
+        Nn, Nm, Np = (int(v) for v in g[f"inv{i}/shape"][:3])
+        got = inverse_HF_transform(g[f"inv{i}/Ck"], Nn, Nm, Np, g[f"inv{i}/xi_x"], g[f"inv{i}/xi_y"],
+                                   g[f"inv{i}/xi_z"]).cpu().numpy()
+        assert rel_err(got, g[f"inv{i}/f"]) < 1e-12
