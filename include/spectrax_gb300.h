@@ -310,6 +310,14 @@ typedef struct spx_dopri8_stats {
  */
 int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* opts, spx_dopri8** out);
 int spx_dopri8_destroy(spx_dopri8* s);
+/* Fault-handling test hook (no counterpart in the reference).  The persistent
+ * kernel's waits on other CTAs' completion counters give up after `polls` polls
+ * (0: the default, about a second) and end the solve with SPX_ST_WAIT_TIMEOUT.
+ * unreachable != 0 makes those waits ask for a count no CTA ever publishes, so
+ * the first one runs out: a way to exercise the time-out path without a fault.
+ * Each such wait sits between stages, when the CTA has no bulk copy in flight.
+ * Takes effect at the next spx_dopri8_reset; affects only persistent solvers. */
+int spx_dopri8_set_wait_test(spx_dopri8* s, int32_t polls, int32_t unreachable);
 /* Copy y0 in (device memory or page-locked host memory) and reset the
  * clock/controller; stream-ordered, the host does not wait. */
 int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream);

@@ -19,6 +19,7 @@ SPX_OK, SPX_E_ARG, SPX_E_CUDA, SPX_E_WORKSPACE, SPX_E_UNSUPPORTED = 0, -1, -2, -
 KRYLOV_MAX_ROWS = 64   # SPX_KRYLOV_MAX_ROWS
 
 STATUS_NAMES = {0: "RUNNING", 1: "DONE", 2: "MAX_STEPS", 3: "DT_UNDERFLOW", 4: "NONFINITE", 5: "WAIT_TIMEOUT"}
+SPX_ST_WAIT_TIMEOUT = 5
 
 
 class SpectraxLibraryError(RuntimeError):
@@ -120,6 +121,7 @@ _PROTOS = {
     "spx_vjp_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "spx_dopri8_create": (C.c_int, [_VP, C.POINTER(spx_dopri8_opts), C.POINTER(_VP)]),
     "spx_dopri8_destroy": (C.c_int, [_VP]),
+    "spx_dopri8_set_wait_test": (C.c_int, [_VP, C.c_int32, C.c_int32]),
     "spx_dopri8_reset": (C.c_int, [_VP, _VP, _VP]),
     "spx_dopri8_advance": (C.c_int, [_VP, C.c_int64, _VP, C.POINTER(C.c_int32)]),
     "spx_dopri8_run": (C.c_int, [_VP, _VP, C.POINTER(C.c_int32)]),

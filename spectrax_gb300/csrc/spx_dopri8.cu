@@ -38,7 +38,8 @@ struct D8Dev {
   unsigned int att;       // attempts finished since reset (the persistent kernel's attempt barrier)
   unsigned int save_seq;  // incremented whenever an accepted step crosses save times
   int interp;             // 1: save times inside a step are interpolated (steps end only on t1)
-  int spare;
+  int wait_polls;         // poll limit of the persistent kernel's counter waits; < 0: the
+                          // waits ask for a count nobody publishes (time-out test), limit -wait_polls
   double save_t0, save_h; // the accepted step a pending save interpolates ([t0, t0 + h]); h = 0: none
 };
 
@@ -453,20 +454,23 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_persist(D8Args a, int natt) 
       // the producers of this stage's inputs have finished stage - 1
       const int nblk = P.pb.Ns * P.ntiles;
       bool ok = true;
+      const int polls = s.wait_polls < 0 ? -s.wait_polls : s.wait_polls;
+      // time-out test: a target no CTA ever publishes
+      const unsigned int never = s.wait_polls < 0 ? 0x40000000u : 0u;
       if (stage > 0) {
-        const unsigned int need = s.att * rk::S + stage;
+        const unsigned int need = s.att * rk::S + stage + never;
         const int b = blockIdx.x;
         if (b < nblk) {
           const int tl = b % P.ntiles;
-          if (threadIdx.x == 0 && tl > 0) ok = wait_counter(a.done + b - 1, need);
-          if (threadIdx.x == 1 && tl + 1 < P.ntiles) ok = wait_counter(a.done + b + 1, need);
-          if (threadIdx.x == 2) ok = wait_counter(a.done + nblk, need);
+          if (threadIdx.x == 0 && tl > 0) ok = wait_counter(a.done + b - 1, need, polls);
+          if (threadIdx.x == 1 && tl + 1 < P.ntiles) ok = wait_counter(a.done + b + 1, need, polls);
+          if (threadIdx.x == 2) ok = wait_counter(a.done + nblk, need, polls);
         } else {
           // the field CTA reads the tiles holding planes 0 and 1; the others must be
           // past stage - 2 before this stage overwrites their stage - 2 input buffer
           const int t01 = 1 / P.tile;
           for (int c = threadIdx.x; c < nblk && ok; c += blockDim.x)
-            ok = wait_counter(a.done + c, (c % P.ntiles) <= t01 ? need : need - 1);
+            ok = wait_counter(a.done + c, (c % P.ntiles) <= t01 ? need : need - 1, polls);
         }
       }
       if (__syncthreads_or(!ok)) {
@@ -514,7 +518,10 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_d8_persist(D8Args a, int natt) 
     }
     // attempt barrier: the controller of this attempt has run
     bool ok = true;
-    if (threadIdx.x == 0) ok = wait_counter(&a.st->att, s.att + 1);
+    if (threadIdx.x == 0) {
+      const int polls = s.wait_polls < 0 ? -s.wait_polls : s.wait_polls;
+      ok = wait_counter(&a.st->att, s.att + 1 + (s.wait_polls < 0 ? 0x40000000u : 0u), polls);
+    }
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicExch(&a.st->status, SPX_ST_WAIT_TIMEOUT);
       return;
@@ -706,6 +713,7 @@ struct spx_dopri8 {
 };
 
 static bool g_d8_consts = false;
+constexpr int kDefaultWaitPolls = 1 << 22;   // ~0.3-1 s of polling with short sleeps
 
 static int upload_consts() {
   if (g_d8_consts) return SPX_OK;
@@ -770,6 +778,19 @@ static int d8_attrs() {
   return SPX_OK;
 }
 
+
+// The reset record (device copy of the controller state at t0): a save time at
+// (or before) t0 is taken from y0.
+static cudaError_t write_reset_record(spx_dopri8* s) {
+  D8Dev R = s->init;
+  R.cur = 0;
+  int hi = 0;
+  while (hi < s->nsave && s->ts[hi] <= R.t0) ++hi;
+  if (hi > 0) { R.save_pending = 1; R.save_lo = 0; R.save_hi = hi; R.isave = hi; }
+  if (R.t0 >= R.t1) R.status = SPX_ST_DONE;
+  R.herm = s->herm_allowed ? 1 : 0;
+  return cudaMemcpy(s->d_init, &R, sizeof(R), cudaMemcpyHostToDevice);
+}
 
 // All `natt` attempts in one cooperative launch (every CTA co-resident).
 static void enqueue_persistent(spx_dopri8* s, cudaStream_t st, int natt) {
@@ -924,6 +945,7 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
   I.rtol = o->rtol; I.atol = o->atol; I.adaptive = o->adaptive ? 1 : 0;
   I.max_steps = o->max_steps; I.nsave = o->nsave; I.status = SPX_ST_RUNNING;
   I.interp = o->saveat == 0 ? 1 : 0;
+  I.wait_polls = kDefaultWaitPolls;
   if (o->hermitian && P.path == 0 && (P.ax[1].n & 1)) {
     // the streaming and Maxwell terms keep the symmetry only if k(N-1-c) == -k(c) exactly
     const int N = P.ax[1].n;
@@ -932,18 +954,8 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
       if (!(plan->tab[P.ax[1].kofs + c].x == -plan->tab[P.ax[1].kofs + N - 1 - c].x)) anti = false;
     s->herm_allowed = anti;
   }
-  {
-    // the reset record: a save time at (or before) t0 is taken from y0
-    D8Dev R = I;
-    R.cur = 0;
-    int hi = 0;
-    while (hi < s->nsave && s->ts[hi] <= R.t0) ++hi;
-    if (hi > 0) { R.save_pending = 1; R.save_lo = 0; R.save_hi = hi; R.isave = hi; }
-    if (R.t0 >= R.t1) R.status = SPX_ST_DONE;
-    R.herm = s->herm_allowed ? 1 : 0;
-    e = cudaMemcpy(s->d_init, &R, sizeof(R), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "dopri8 reset record"); }
-  }
+  e = write_reset_record(s);
+  if (e != cudaSuccess) { d8_free(s); return cuda_fail(e, "dopri8 reset record"); }
   e = cudaMallocHost(&s->h_status, sizeof(int) * 4);
   if (e == cudaSuccess && o->nsave > 0)
     e = cudaMemcpy(b + o_ts, o->save_ts, o->nsave * sizeof(double), cudaMemcpyHostToDevice);
@@ -972,6 +984,14 @@ int spx_dopri8_create(const spx_plan* plan, const spx_dopri8_opts* o, spx_dopri8
 }
 
 int spx_dopri8_destroy(spx_dopri8* s) { return d8_free(s); }
+
+int spx_dopri8_set_wait_test(spx_dopri8* s, int32_t polls, int32_t unreachable) {
+  if (!s || polls < 0) { set_error("spx_dopri8_set_wait_test: bad argument"); return SPX_E_ARG; }
+  const int p = polls == 0 ? kDefaultWaitPolls : polls;
+  s->init.wait_polls = unreachable ? -p : p;
+  SPX_CUDA(write_reset_record(s));
+  return SPX_OK;
+}
 
 int spx_dopri8_reset(spx_dopri8* s, const void* y0, void* stream) {
   if (!s || !y0) { set_error("spx_dopri8_reset: null argument"); return SPX_E_ARG; }

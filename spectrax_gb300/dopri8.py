@@ -47,6 +47,17 @@ def _saveat_code(saveat: str) -> int:
     return _SAVEAT_MODES[saveat]
 
 
+class DeviceWaitTimeout(RuntimeError):
+    """A bounded device-side wait gave up (status SPX_ST_WAIT_TIMEOUT); the solve
+    stopped and its state is not a valid trajectory point."""
+
+
+def _check_wait(status: int) -> int:
+    if status == _lib.SPX_ST_WAIT_TIMEOUT:
+        raise DeviceWaitTimeout("Dopri8 solve stopped: a bounded device-side wait timed out")
+    return status
+
+
 class Dopri8Solver:
     def __init__(self, plan: Plan, t0: float, t1: float, dt0: float, ts=None, adaptive=True,
                  rtol=1e-10, atol=1e-12, max_steps=1_000_000, save_states=True, masses=None,
@@ -100,7 +111,7 @@ class Dopri8Solver:
         st = C.c_int32()
         _lib.check(_lib.lib().spx_dopri8_advance(self.handle, int(attempts), _stream_ptr(stream), C.byref(st)),
                    "spx_dopri8_advance")
-        return int(st.value)
+        return _check_wait(int(st.value))
 
     def enqueue(self, attempts: int, stream=None):
         """Queue exactly `attempts` step attempts without synchronising."""
@@ -110,7 +121,14 @@ class Dopri8Solver:
     def run(self, stream=None) -> int:
         st = C.c_int32()
         _lib.check(_lib.lib().spx_dopri8_run(self.handle, _stream_ptr(stream), C.byref(st)), "spx_dopri8_run")
-        return int(st.value)
+        return _check_wait(int(st.value))
+
+    def set_wait_test(self, polls: int = 0, unreachable: bool = False):
+        """Fault-handling test hook (spx_dopri8_set_wait_test): the persistent
+        kernel's counter waits give up after `polls` polls (0: default); with
+        `unreachable` they wait for a count no CTA publishes.  From the next reset."""
+        _lib.check(_lib.lib().spx_dopri8_set_wait_test(self.handle, int(polls), 1 if unreachable else 0),
+                   "spx_dopri8_set_wait_test")
 
     def stats(self, stream=None) -> dict:
         s = _lib.spx_dopri8_stats()

@@ -83,3 +83,30 @@ def test_persistent_stops_at_max_steps():
     assert sa == sb == 2                                   # SPX_ST_MAX_STEPS
     assert a.stats()["accepted"] == b.stats()["accepted"] == 13
     assert np.array_equal(a.state().cpu().numpy(), b.state().cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_bounded_counter_wait_times_out_and_the_context_stays_usable():
+    # the persistent kernel's counter waits are made to run out (a target no CTA
+    # publishes, 1000 polls): the solve must stop with SPX_ST_WAIT_TIMEOUT, the
+    # wrapper must raise, and the same solver must then run normally again
+    import torch
+    from spectrax_gb300 import _lib, dopri8, vector_field
+    p = _params(33, 16, 2)
+    plan = vector_field.get_plan(vector_field.problem_from_params(p, "divide"), None, 0, 256)
+    y0 = _state(33, 16, 2, True)
+    s = dopri8.Dopri8Solver(plan, 0.0, 1.0, 0.05, ts=np.linspace(0, 1.0, 5), adaptive=False,
+                            masses=dopri8.species_masses(p), persistent=True, saveat="land")
+    s.set_wait_test(polls=1000, unreachable=True)
+    s.reset(torch.from_numpy(y0))
+    with pytest.raises(dopri8.DeviceWaitTimeout):
+        s.run()
+    torch.cuda.synchronize()                               # the context is intact
+    st = s.stats()
+    assert st["persistent"] and st["status"] == _lib.SPX_ST_WAIT_TIMEOUT
+    s.set_wait_test()                                      # back to the default limit
+    s.reset(torch.from_numpy(y0))
+    assert s.run() == 1
+    ref, sref = _run(plan, p, y0, 1.0, 0.05, np.linspace(0, 1.0, 5), False, persistent=False)
+    assert sref == 1
+    assert np.array_equal(s.state().cpu().numpy(), ref.state().cpu().numpy())
