@@ -64,19 +64,41 @@ def gather_results(local: dict, group=None):
     return out
 
 
-def run_sharded_batch(insts, t1, save_ts=None, rtol=1e-8, atol=1e-8, cluster=4, tile=16, group=None):
-    """Each rank solves its shard of `insts` in one persistent launch; results are gathered."""
-    import torch.distributed as dist
+class RankFailure(RuntimeError):
+    """Another rank's shard failed; raised on every rank after the result exchange."""
+
+
+def solve_shard_on_gpu(shard, t1, save_ts=None, rtol=1e-8, atol=1e-8, cluster=4, tile=16):
+    """One persistent batch launch over this rank's instances; {local index: result}."""
     from .batch import BatchSolver
+    b = BatchSolver([it["problem"] for it in shard], t1, rtol=rtol, atol=atol, save_ts=save_ts,
+                    cluster=cluster, tile=tile, masses=[it.get("masses") or [1.0] * 8 for it in shard])
+    ys = b.unpack(b.run(b.pack([it["y0"] for it in shard])))
+    stats, ens = b.results()
+    return {k: dict(y=ys[k], stats=stats[k], energies=ens[k]) for k in range(len(shard))}
+
+
+def run_sharded_batch(insts, t1, save_ts=None, rtol=1e-8, atol=1e-8, cluster=4, tile=16, group=None,
+                      solve_shard=None):
+    """Each rank solves its cost-balanced shard of `insts` (one persistent launch by
+    default; `solve_shard(shard, t1, save_ts, rtol, atol, cluster, tile)` replaces
+    it) and the per-instance results are gathered on every rank.  A rank whose
+    shard raises still takes part in the exchange, so the others learn of the
+    failure at once; every rank then raises RankFailure naming it."""
+    import torch.distributed as dist
+    solve_shard = solve_shard or solve_shard_on_gpu
     world = dist.get_world_size(group) if dist.is_initialized() else 1
     rank = dist.get_rank(group) if dist.is_initialized() else 0
     mine = shard_instances([instance_cost(it["problem"]) for it in insts], world, rank)
-    local = {}
+    local, error = {}, None
     if mine:
-        b = BatchSolver([insts[i]["problem"] for i in mine], t1, rtol=rtol, atol=atol, save_ts=save_ts,
-                        cluster=cluster, tile=tile, masses=[insts[i].get("masses") or [1.0] * 8 for i in mine])
-        ys = b.unpack(b.run(b.pack([insts[i]["y0"] for i in mine])))
-        stats, ens = b.results()
-        for k, i in enumerate(mine):
-            local[i] = dict(y=ys[k], stats=stats[k], energies=ens[k])
-    return gather_results(local, group)
+        try:
+            res = solve_shard([insts[i] for i in mine], t1, save_ts, rtol, atol, cluster, tile)
+            local = {mine[k]: v for k, v in res.items()}
+        except Exception as exc:            # reported to every rank below
+            error = f"rank {rank}: {type(exc).__name__}: {exc}"
+    merged = gather_results({("error", rank): error, **local}, group)
+    errors = sorted(v for k, v in merged.items() if isinstance(k, tuple) and v is not None)
+    if errors:
+        raise RankFailure("; ".join(errors))
+    return {k: v for k, v in merged.items() if not isinstance(k, tuple)}
