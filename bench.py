@@ -221,7 +221,7 @@ def run_extras(args):
         # all 256 by the single-instance device solver's time ratio
         from spectrax_gb300.dopri8 import host_dopri8_solve
         from spectrax_gb300.vector_field import get_plan
-        sub = insts[::16]
+        sub = insts[::64]
         _, _, _, ts_dev_sub = serial_solve(sub, t1, rtol=1e-8, atol=1e-8, save_ts=ts)
         torch.cuda.synchronize()
         t0p = time.perf_counter()
@@ -243,7 +243,7 @@ def run_extras(args):
             "max_rel_err_state_vs_serial": err, "max_rel_err_field_energy_vs_serial": eerr,
             "hermitian_instances": int(sum(1 for s_ in stats if s_.get("hermitian"))),
             "serial_plain_rhs_s_estimated": tp_all, "speedup_vs_plain_rhs": tp_all / tb,
-            "serial_plain_rhs_sample": f"{len(sub)} instances (every 16th) timed: {tp_sub:.3f} s",
+            "serial_plain_rhs_sample": f"{len(sub)} instances (every 64th) timed: {tp_sub:.3f} s",
             "note": "per-instance adaptive Dopri8 (rtol=atol=1e-8). serial_s / speedup: the same instances "
                     "one by one through the graph-captured single-instance device solver (general "
                     "complex-transform stages); speedup_vs_plain_rhs: one by one through the plain RHS "
@@ -530,11 +530,16 @@ def run_ours(args):
     hbm_peak, hbm_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, _lib.lib())
     launch_ms = ms_per_step / 13.0
-    # algorithmic bytes of an average stage launch (the save launch is empty between saves)
-    bytes_launch = perf.dopri8_vectors_per_step() * n * 16 / 13.0
-    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile), plan.product_grid)
-    # FP64 work of a step: 13 RHS + the Runge-Kutta combinations (4 flops per complex FMA)
-    flops_step = 13.0 * ops.flops + 4.0 * perf.dopri8_combination_fmas_per_entry() * n
+    # algorithmic bytes of an average stage launch (the save launch is empty between
+    # saves): a 13-stage step moves s (s + 3) / 2 + s + 3 = 120 state vectors when every
+    # stage reads y and all earlier K_j; this tableau's zero entries leave 107 of them
+    vec_dense, vec_touched = perf.dopri8_vectors_per_step_dense(13), perf.dopri8_vectors_per_step()
+    bytes_launch = vec_dense * n * 16 / 13.0
+    packed = bool(st1.get("hermitian"))
+    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile), plan.product_grid, packed=packed)
+    # FP64 work the step executes: 13 RHS + the Runge-Kutta combinations (4 flops per
+    # complex FMA; half of them when only the k <= 0 half of each plane is formed)
+    flops_step = 13.0 * ops.flops + (2.0 if packed else 4.0) * perf.dopri8_combination_fmas_per_entry() * n
     achieved_gbs = bytes_launch / (launch_ms * 1e-3) / 1e9
     achieved_tf = flops_step / (ms_per_step * 1e-3) / 1e12
     traffic = profile_traffic()
@@ -553,13 +558,16 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                      "peak_source": hbm_src,
-                     "kernel": "k_d8_stage_1v (duration = step time / 13)"},
+                     "kernel": "k_d8_stage_1v (duration = step time / 13)",
+                     "bytes_per_launch": bytes_launch,
+                     "vectors_per_step": vec_dense, "vectors_touched_by_this_tableau": vec_touched},
         "fp64": {"achieved": achieved_tf, "peak": fp64_peak, "unit": "TFLOP/s",
                  "frac": achieved_tf / fp64_peak, "peak_source": "live FMA probe (spx_probe_fp64)",
-                 "note": "FP64 work of the complex-transform formulation of the step (pruned transforms on "
-                         "the plan's product grid, products, streaming, stage combinations) per unit time; the "
-                         "packed real transforms used for this exactly Hermitian state execute fewer instructions. "
-                         "FP64 issue is the binding ceiling of this path on GB300"},
+                 "packed_real_transforms": packed,
+                 "note": "FP64 work the step executes (pruned transforms on the plan's product grid, packed "
+                         "two real lines per transform for this exactly Hermitian state, products, streaming, "
+                         "stage combinations on the evaluated half of each plane) per unit time. FP64 issue "
+                         "is the binding ceiling of this path on GB300"},
         "clocks": clk.summary(),
     }
     if world == 1:
@@ -584,7 +592,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--extras", type=int, default=1, help="also time the batched scan and the adjoint")
-    ap.add_argument("--scan-t1", type=float, default=4.0, help="horizon of the batched scan extra")
+    ap.add_argument("--scan-t1", type=float, default=40.0, help="horizon of the batched scan extra")
     ap.add_argument("--tile", type=int, default=0, help="Hermite planes per CTA (0: autotune)")
     ap.add_argument("--threads", type=int, default=256, help="CTA width when --tile is given")
     ap.add_argument("--product-grid", default="auto", choices=["auto", "nx", "fp64"],

@@ -364,6 +364,9 @@ typedef struct spx_batch_opts {
   int32_t hermitian;     /* 1: an instance with odd Nx whose initial state is exactly Hermitian
                             (C(-k) == conj C(k) on every line) uses packed real transforms */
   int32_t saveat;        /* as spx_dopri8_opts.saveat: 0 dense output at save times, 1 land on them */
+  const double* costs;   /* host, n relative costs ordering the work queue (largest first), e.g.
+                            durations measured on a short horizon; NULL: an estimate from the
+                            FFT work per evaluation and the stability-limited step count */
 } spx_batch_opts;
 
 typedef struct spx_batch_stats {
@@ -372,6 +375,7 @@ typedef struct spx_batch_stats {
   int32_t status, saved;
   int32_t hermitian;     /* 1 if the instance ran with packed real transforms */
   int32_t pad;
+  double start_s, end_s; /* when its cluster took and finished it, seconds after the first start */
 } spx_batch_stats;
 
 typedef struct spx_batch spx_batch;

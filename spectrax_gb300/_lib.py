@@ -81,6 +81,7 @@ class spx_batch_opts(C.Structure):
         ("masses", C.POINTER(C.c_double)),
         ("hermitian", C.c_int32),
         ("saveat", C.c_int32),
+        ("costs", C.POINTER(C.c_double)),
     ]
 
 
@@ -90,6 +91,7 @@ class spx_batch_stats(C.Structure):
         ("accepted", C.c_int64), ("rejected", C.c_int64), ("rhs_evals", C.c_int64),
         ("status", C.c_int32), ("saved", C.c_int32),
         ("hermitian", C.c_int32), ("pad", C.c_int32),
+        ("start_s", C.c_double), ("end_s", C.c_double),
     ]
 
 

@@ -65,7 +65,7 @@ def landau_scan(n=256, seed=0, amplitude=0.01, mask_mode="divide"):
 class BatchSolver:
     def __init__(self, problems, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, adaptive=True,
                  max_steps=10_000_000, cluster=2, tile=8, masses=None, device=None, hermitian=True,
-                 saveat="interpolate"):
+                 saveat="interpolate", costs=None):
         from .dopri8 import _saveat_code
         L = _lib.lib()
         self.n = len(problems)
@@ -92,6 +92,12 @@ class BatchSolver:
         # save times: dense output inside a step (Diffrax SaveAt(ts)) or steps landing on them
         o.saveat = _saveat_code(saveat)
         self.saveat = saveat
+        # queue order: the caller's relative costs (largest first), else the built-in estimate
+        self._costs = None if costs is None else np.ascontiguousarray(np.asarray(costs, np.float64))
+        if self._costs is not None:
+            if self._costs.shape != (self.n,):
+                raise ValueError("costs must hold one value per instance")
+            o.costs = self._costs.ctypes.data_as(C.POINTER(C.c_double))
         self.cluster, self.tile = int(cluster), int(tile)
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         h = C.c_void_p()
@@ -129,7 +135,8 @@ class BatchSolver:
                                                 _stream_ptr()), "spx_batch_results")
         torch.cuda.current_stream().synchronize()
         stats = [dict(t=s.t, dt=s.dt, accepted=s.accepted, rejected=s.rejected, rhs_evals=s.rhs_evals,
-                      status=s.status, saved=s.saved, hermitian=bool(s.hermitian)) for s in st]
+                      status=s.status, saved=s.saved, hermitian=bool(s.hermitian),
+                      start_s=s.start_s, end_s=s.end_s) for s in st]
         energies = []
         for i in range(self.n):
             w = 2 + self.problems[i].Ns

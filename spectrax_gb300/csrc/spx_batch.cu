@@ -49,7 +49,14 @@ struct BInst {
   int status, saved;
   int herm_ok;           // odd Nx with an antisymmetric wavenumber table, and requested
   int herm;              // result: y0 was exactly Hermitian, packed real transforms used
+  unsigned long long t_begin, t_end;   // %globaltimer (ns) when the instance's cluster took / finished it
 };
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 struct BArgs {
   BInst* inst;
@@ -294,6 +301,7 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
     cl.sync();                      // rank 0 keeps s_inst until every rank has read it
     if (id < 0) break;
     BInst* I = a.inst + id;
+    if (crank == 0 && threadIdx.x == 0) I->t_begin = globaltimer_ns();
     load_plan(P, stab, &I->P, a.tab + I->tab_off);
     const long long len = I->len;
     double2* base = a.pool + I->pool_off;
@@ -467,6 +475,9 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
           if (s_inst == 1) {
             int lo = ctl.isave, hi = lo;
             while (hi < a.nsave && a.save_ts[hi] <= ctl.t) ++hi;
+            // every thread has its (lo, hi) before thread 0 moves ctl.isave below,
+            // so the whole cluster takes the branch (and its cluster barrier) together
+            __syncthreads();
             if (hi > lo) {
               if (crank == 0) {
                 // each save time: the state itself at the step's end (or in land-on-save
@@ -508,6 +519,7 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
     for (long long i = (long long)crank * blockDim.x + threadIdx.x; i < len; i += (long long)C * blockDim.x)
       a.y_out[I->y_off + i] = __ldcg(Yf + i);
     if (crank == 0 && threadIdx.x == 0) {
+      I->t_end = globaltimer_ns();
       I->t = ctl.t; I->dt = ctl.dt; I->accepted = ctl.acc; I->rejected = ctl.rej;
       I->evals = ctl.evals; I->status = ctl.status; I->saved = ctl.saved; I->herm = ctl.herm;
     }
@@ -667,10 +679,12 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     for (int s = 0; s < SPX_MAX_SPECIES; ++s) I.masses[s] = 1.0;
     if (o->masses)
       for (int s = 0; s < p.Ns; ++s) I.masses[s] = o->masses[(size_t)i * SPX_MAX_SPECIES + s];
-    // cost estimate: FFT work per RHS x stability-limited steps ~ k_max * alpha * sqrt(2 Nn)
+    // cost: the caller's (e.g. measured durations), else an estimate: FFT work
+    // per RHS x stability-limited steps ~ k_max * alpha * sqrt(2 Nn)
     const double kmax = (p.Nx / 2) * 2.0 * M_PI / p.Lx;
-    cost[i] = (double)p.Ns * p.Nn * p.Nx * std::log2((double)p.Nx + 1.0) *
-              (1.0 + kmax * std::fabs(p.alpha_s[0]) * std::sqrt(2.0 * p.Nn));
+    cost[i] = o->costs ? o->costs[i]
+                       : (double)p.Ns * p.Nn * p.Nx * std::log2((double)p.Nx + 1.0) *
+                             (1.0 + kmax * std::fabs(p.alpha_s[0]) * std::sqrt(2.0 * p.Nn));
   }
   b->total_len = yoff;
   b->en_total = en_off;
@@ -792,7 +806,11 @@ int spx_batch_results(spx_batch* b, spx_batch_stats* stats, double* energies, vo
     std::vector<BInst> h(b->n);
     SPX_CUDA(cudaMemcpyAsync(h.data(), b->args.inst, sizeof(BInst) * b->n, cudaMemcpyDeviceToHost, st));
     SPX_CUDA(cudaStreamSynchronize(st));
+    unsigned long long t0 = ~0ULL;
+    for (int i = 0; i < b->n; ++i) t0 = std::min(t0, h[i].t_begin);
     for (int i = 0; i < b->n; ++i) {
+      stats[i].start_s = 1e-9 * (double)(h[i].t_begin - t0);
+      stats[i].end_s = 1e-9 * (double)(h[i].t_end - t0);
       stats[i].t = h[i].t; stats[i].dt = h[i].dt;
       stats[i].accepted = h[i].accepted; stats[i].rejected = h[i].rejected; stats[i].rhs_evals = h[i].evals;
       stats[i].status = h[i].status; stats[i].saved = h[i].saved;

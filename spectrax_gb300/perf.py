@@ -10,6 +10,13 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
+def dopri8_vectors_per_step_dense(s: int = 13) -> int:
+    """Vectors per step of an s-stage method whose stage i reads y and all i - 1
+    earlier K_j and writes K_i, whose last combination reads s + 1 vectors and
+    writes y_new and the error: s (s + 3) / 2 + s + 3 (120 for s = 13)."""
+    return s * (s + 3) // 2 + s + 3
+
+
 def dopri8_vectors_per_step() -> int:
     """State-sized vectors read + written by one step attempt of the fused 1D1V stepper.
 
@@ -109,10 +116,14 @@ def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit", radices=None
     return o
 
 
-def rhs_ops(shape, tile=None, ntiles=None, product_grid=None) -> Ops:
+def rhs_ops(shape, tile=None, ntiles=None, product_grid=None, packed=False) -> Ops:
     """FP64 work of one right-hand-side evaluation (fused 1D1V or general path).
     product_grid: length of the 1D1V products' grid (the plan's; default Nx),
-    transformed with the cheapest radix order the plan builder tries."""
+    transformed with the cheapest radix order the plan builder tries.
+    packed (1D1V, exactly Hermitian state): the work the stage kernels execute
+    with packed real transforms -- two real lines per complex transform, per tile
+    of nt planes ceil((nt + 1) / 2) inverse and ceil(nt / 2) forward transforms,
+    and only the k <= 0 half of each output plane evaluated."""
     Nx, Ny, Nz, Nn, Nm, Np, Ns = shape
     o = Ops()
     plane = Nx * Ny * Nz
@@ -126,12 +137,20 @@ def rhs_ops(shape, tile=None, ntiles=None, product_grid=None) -> Ops:
                       fft_line_ops(M, cut, "dif", r).instr)
         fi, ff = fft_line_ops(M, cut, "dit", rad), fft_line_ops(M, cut, "dif", rad)
         ntiles = ntiles or 1
-        lines_inv = Ns * (Nn + ntiles)          # C_{n-1} per plane + one G per tile
-        lines_fwd = Ns * Nn
+        if packed:
+            T = tile or -(-Nn // ntiles)
+            nts = [min(T, Nn - t * T) for t in range(ntiles)]
+            lines_inv = Ns * sum((nt + 2) // 2 for nt in nts)
+            lines_fwd = Ns * sum((nt + 1) // 2 for nt in nts)
+            o.add(addmul=2, mult=lines_fwd * M)                      # packed real products
+            o.add(fma=6, addmul=6, mult=Ns * Nn * ((Nx + 1) // 2))   # half plane + the packed split
+        else:
+            lines_inv = Ns * (Nn + ntiles)          # C_{n-1} per plane + one G per tile
+            lines_fwd = Ns * Nn
+            o.add(fma=2, addmul=2, mult=Ns * Nn * M)             # G * C
+            o.add(fma=6, addmul=4, mult=Ns * Nn * Nx)            # streaming, damping, NL add
         o.instr += fi.instr * lines_inv + ff.instr * lines_fwd
         o.flops += fi.flops * lines_inv + ff.flops * lines_fwd
-        o.add(fma=2, addmul=2, mult=Ns * Nn * M)             # G * C
-        o.add(fma=6, addmul=4, mult=Ns * Nn * Nx)            # streaming, damping, NL add
         o.add(fma=4, addmul=2, mult=Ns * Nx)                 # G combination
         o.add(fma=8 * Ns + 6, addmul=24, mult=Nx)            # Maxwell + current
         return o
