@@ -188,6 +188,20 @@ size_t spx_krylov_ws_bytes(int64_t n);
 int spx_krylov_cgs2(const void* V, int64_t n, int32_t k, void* w, void* out, void* ws, size_t ws_bytes,
                     void* stream);
 int spx_krylov_axpy(const void* V, int64_t n, int32_t k, const void* c, void* x, void* stream);
+/*
+ * Implicit-midpoint Newton glue (spectrax/midpoint_solver.py:44-53), one pass each:
+ * spx_midpoint_residual: r = y1 - y0 - dt f (stored when r != NULL) and, on the
+ *   device, sums[0] = sum |r / (atol + rtol max(|y0|, |y1|))|^2, sums[1] = the
+ *   number of non-finite entries of r (fixed-order reduction; ws as for
+ *   spx_krylov_cgs2).  f = f(y_mid): the Newton residual, whose scaled 2-norm
+ *   decides convergence; f = f(y0): the error estimate y1 - y1_init of the
+ *   adaptive step controller.
+ * spx_midpoint_update: y1 += sign * delta (delta may be NULL), ymid = (y0 + y1) / 2.
+ */
+int spx_midpoint_residual(int64_t n, const void* y0, const void* y1, const void* f, double dt, double rtol,
+                          double atol, void* r, double* sums, void* ws, size_t ws_bytes, void* stream);
+int spx_midpoint_update(int64_t n, const void* y0, void* y1, const void* delta, double sign, void* ymid,
+                        void* stream);
 
 /*
  * g = J(y)^T w (plain transpose, no conjugation): the vector-Jacobian product of

@@ -140,3 +140,67 @@ def step_newton_gmres(f, y0, dt, rtol=1e-10, atol=1e-10, max_iters=300, restart=
         newton += 1
         mv += its
     return y1, y1 - y1_init, newton, mv
+
+
+def controller_factor(errnorm, accepted, order=2.0):
+    """Diffrax PIDController defaults with error order `order` (2 for this solver)."""
+    if errnorm == 0.0:
+        f = 10.0
+    elif not np.isfinite(errnorm):
+        f = 0.2
+    else:
+        f = 0.9 * errnorm ** (-1.0 / order)
+    return min(max(f, 1.0 if accepted else 0.2), 10.0)
+
+
+def solve(f, t1, y0, dt0, ts, rtol=1e-10, atol=1e-10, ctrl_rtol=1e-6, ctrl_atol=1e-6, adaptive=True,
+          step_fn=None, max_steps=100000):
+    """Implicit midpoint from 0 to t1 as spectrax/_simulation.py:164-180 runs it.
+
+    adaptive: Diffrax's PIDController (ctrl_rtol, ctrl_atol) on the RMS of
+    y_error / (ctrl_atol + ctrl_rtol max(|y0|, |y1|)) with y_error = y1 - y1_init
+    (spectrax/midpoint_solver.py:51) and error order 2; steps end only on t1 and a
+    save time inside an accepted step gets the linear interpolation of the step's
+    end points (LocalLinearInterpolation, midpoint_solver.py:24).  Otherwise steps
+    of dt0 that land on every save time.  step_fn(f, y, h) -> (y1, y_error) defaults
+    to the dense-Newton ``step``.  Returns dict(ys, accepted, rejected, t)."""
+    step_fn = step_fn or (lambda ff, y, h: step(ff, y, h, rtol, atol)[:2])
+    ts = np.asarray(ts, np.float64)
+    y = np.array(y0, np.complex128)
+    t, h_prop = 0.0, float(dt0)
+    isave, saved, acc, rej = 0, [], 0, 0
+    while isave < len(ts) and ts[isave] <= t:
+        saved.append(y.copy())
+        isave += 1
+    while t < t1 * (1 - 1e-15):
+        if acc + rej >= max_steps:
+            raise RuntimeError("max_steps reached")
+        t_stop = t1 if adaptive else (min(ts[isave], t1) if isave < len(ts) else t1)
+        h, landed = h_prop, False
+        if t + h * (1 + 1e-9) >= t_stop:
+            h, landed = t_stop - t, True
+        y1, yerr = step_fn(f, y, h)
+        if adaptive:
+            scale = ctrl_atol + ctrl_rtol * np.maximum(np.abs(y), np.abs(y1))
+            r = yerr / scale
+            en = float(np.sqrt(np.mean(r.real ** 2 + r.imag ** 2)))
+            accepted = en < 1.0
+            h_next = h * controller_factor(en, accepted)
+        else:
+            accepted, h_next = True, h_prop
+        if not accepted:
+            rej += 1
+            h_prop = h_next
+            continue
+        t_new = t_stop if landed else t + h
+        while isave < len(ts) and ts[isave] <= t_new:
+            if adaptive and ts[isave] != t_new:
+                w = (ts[isave] - t) / h
+                saved.append(y + w * (y1 - y))
+            else:
+                saved.append(y1.copy())
+            isave += 1
+        y, t = y1, t_new
+        acc += 1
+        h_prop = h_next if adaptive else h_prop
+    return dict(ys=np.stack(saved), accepted=acc, rejected=rej, t=t, y=y)

@@ -119,6 +119,9 @@ _PROTOS = {
     "spx_maxwellian": (C.c_int, [_VP, _VP, _VP, C.c_int32, _VP, _VP]),
     "spx_krylov_cgs2": (C.c_int, [_VP, C.c_int64, C.c_int32, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_krylov_axpy": (C.c_int, [_VP, C.c_int64, C.c_int32, _VP, _VP, _VP]),
+    "spx_midpoint_residual": (C.c_int, [C.c_int64, _VP, _VP, _VP, C.c_double, C.c_double, C.c_double, _VP, _VP,
+                                        _VP, C.c_size_t, _VP]),
+    "spx_midpoint_update": (C.c_int, [C.c_int64, _VP, _VP, _VP, C.c_double, _VP, _VP]),
     "spx_vjp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_vjp_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "spx_dopri8_create": (C.c_int, [_VP, C.POINTER(spx_dopri8_opts), C.POINTER(_VP)]),

@@ -201,6 +201,75 @@ __global__ void k_kry_finish(const double2* __restrict__ h, const double2* __res
   }
 }
 
+// ---------------------------------------------------------------- implicit midpoint glue
+// r[e] = y1[e] - y0[e] - dt f[e] (stored when r != nullptr); npart[b] = block b's
+// sum of |r / (atol + rtol max(|y0|, |y1|))|^2, bpart[b] its count of non-finite r.
+// With f = f(y_mid) this is the Newton residual of spectrax/midpoint_solver.py:48-50,
+// with f = f(y0) the solver's error estimate y1 - y1_init (:51).
+__global__ void __launch_bounds__(NTHREADS) k_mid_residual(long long n, const double2* __restrict__ y0,
+                                                           const double2* __restrict__ y1,
+                                                           const double2* __restrict__ f, double dt, double rtol,
+                                                           double atol, double2* __restrict__ r,
+                                                           double* __restrict__ npart, double* __restrict__ bpart) {
+  __shared__ double red[2][NTHREADS / 32];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  double sq = 0.0, bad = 0.0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += stride) {
+    const double2 a = y0[e], b = y1[e], g = f[e];
+    const double2 v = make_double2(fma(-dt, g.x, b.x - a.x), fma(-dt, g.y, b.y - a.y));
+    if (r) r[e] = v;
+    const double m0 = fma(a.x, a.x, a.y * a.y), m1 = fma(b.x, b.x, b.y * b.y);
+    const double inv = 1.0 / fma(rtol, sqrt(fmax(m0, m1)), atol);
+    const double rx = v.x * inv, ry = v.y * inv;
+    sq = fma(rx, rx, fma(ry, ry, sq));
+    if (!(isfinite(v.x) && isfinite(v.y))) bad += 1.0;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    sq += __shfl_down_sync(0xffffffffu, sq, off);
+    bad += __shfl_down_sync(0xffffffffu, bad, off);
+  }
+  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = sq; red[1][threadIdx.x >> 5] = bad; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, c = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { s += red[0][q]; c += red[1][q]; }
+    npart[blockIdx.x] = s;
+    bpart[blockIdx.x] = c;
+  }
+}
+
+// out[0] = sum of npart, out[1] = sum of bpart (lanes take blocks in order, then a
+// fixed shuffle tree: deterministic)
+__global__ void k_mid_sum2(const double* __restrict__ npart, const double* __restrict__ bpart, int nb,
+                           double* __restrict__ out) {
+  const int lane = threadIdx.x;
+  double s = 0.0, c = 0.0;
+  for (int b = lane; b < nb; b += 32) { s += npart[b]; c += bpart[b]; }
+  for (int off = 16; off > 0; off >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, off);
+    c += __shfl_down_sync(0xffffffffu, c, off);
+  }
+  if (lane == 0) { out[0] = s; out[1] = c; }
+}
+
+// y1 += sign * delta (when delta != nullptr); ymid = (y0 + y1) / 2
+__global__ void __launch_bounds__(NTHREADS) k_mid_update(long long n, const double2* __restrict__ y0,
+                                                         double2* __restrict__ y1,
+                                                         const double2* __restrict__ delta, double sign,
+                                                         double2* __restrict__ ymid) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += stride) {
+    double2 b = y1[e];
+    if (delta) {
+      const double2 d = delta[e];
+      b = make_double2(fma(sign, d.x, b.x), fma(sign, d.y, b.y));
+      y1[e] = b;
+    }
+    const double2 a = y0[e];
+    ymid[e] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+  }
+}
+
 }  // namespace spx
 
 using namespace spx;
@@ -240,6 +309,39 @@ int spx_krylov_cgs2(const void* V, int64_t n, int32_t k, void* w, void* out, voi
   k_kry_reduce<<<1, KRY_RED_THREADS, 0, st>>>(part, nb, k, h2);
   k_kry_update<<<nb, NTHREADS, 0, st>>>(Vp, n, k, h2, -1.0, wp, npart);
   k_kry_finish<<<1, SPX_KRYLOV_MAX_ROWS, 0, st>>>(h, h2, npart, nb, k, static_cast<double2*>(out));
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+int spx_midpoint_residual(int64_t n, const void* y0, const void* y1, const void* f, double dt, double rtol,
+                          double atol, void* r, double* sums, void* ws, size_t ws_bytes, void* stream) {
+  if (!y0 || !y1 || !f || !sums || !ws || n <= 0) { set_error("spx_midpoint_residual: bad argument"); return SPX_E_ARG; }
+  if (((uintptr_t)y0 | (uintptr_t)y1 | (uintptr_t)f | (uintptr_t)r | (uintptr_t)ws) & 15) {
+    set_error("spx_midpoint_residual: pointers must be 16-byte aligned"); return SPX_E_ARG;
+  }
+  if (ws_bytes < spx_krylov_ws_bytes(n)) { set_error("spx_midpoint_residual: workspace too small"); return SPX_E_WORKSPACE; }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int nb = kry_blocks(n);
+  // the first 2 nb doubles of the Krylov workspace (its block-partial area)
+  double* npart = static_cast<double*>(ws);
+  double* bpart = npart + nb;
+  k_mid_residual<<<nb, NTHREADS, 0, st>>>(n, static_cast<const double2*>(y0), static_cast<const double2*>(y1),
+                                          static_cast<const double2*>(f), dt, rtol, atol, static_cast<double2*>(r),
+                                          npart, bpart);
+  k_mid_sum2<<<1, 32, 0, st>>>(npart, bpart, nb, sums);
+  SPX_CUDA(cudaGetLastError());
+  return SPX_OK;
+}
+
+int spx_midpoint_update(int64_t n, const void* y0, void* y1, const void* delta, double sign, void* ymid,
+                        void* stream) {
+  if (!y0 || !y1 || !ymid || n <= 0) { set_error("spx_midpoint_update: bad argument"); return SPX_E_ARG; }
+  if (((uintptr_t)y0 | (uintptr_t)y1 | (uintptr_t)delta | (uintptr_t)ymid) & 15) {
+    set_error("spx_midpoint_update: pointers must be 16-byte aligned"); return SPX_E_ARG;
+  }
+  k_mid_update<<<kry_blocks(n), NTHREADS, 0, static_cast<cudaStream_t>(stream)>>>(
+      n, static_cast<const double2*>(y0), static_cast<double2*>(y1), static_cast<const double2*>(delta), sign,
+      static_cast<double2*>(ymid));
   SPX_CUDA(cudaGetLastError());
   return SPX_OK;
 }

@@ -304,7 +304,7 @@ def simulation(input_parameters=None, Nx=33, Ny=1, Nz=1, Nn=20, Nm=1, Np=1, Ns=2
     time = np.linspace(0, p["t_max"], timesteps)
     if isinstance(solver, ImplicitMidpoint):
         from .midpoint import midpoint_solve
-        ys, en, info = midpoint_solve(p, time, solver, mask_mode=mask_mode)
+        ys, en, info = midpoint_solve(p, time, solver, mask_mode=mask_mode, adaptive=adaptive_time_step)
     elif plan_for_params(p, mask_mode).path == 2:
         # planes too large for the device stepper's shared memory: the same
         # tableau, controller and save rule driven from the host around spx_rhs

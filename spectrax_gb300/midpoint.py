@@ -143,31 +143,62 @@ class NewtonGMRES:
         return x, rel, its
 
 
-def step(plan: Plan, y0, dt, rtol, atol, max_iters=300, solver: NewtonGMRES | None = None, stats=None):
-    """One implicit midpoint step; returns (y1, y_error)."""
+class _Glue:
+    """Device buffers of one step (y_mid, f(y_mid), residual, the two reduced sums)."""
+
+    def __init__(self, plan: Plan, ws):
+        self.plan, self.ws = plan, ws
+        self.ymid = torch.empty(plan.state_len, dtype=torch.complex128, device=plan.device)
+        self.fmid = torch.empty_like(self.ymid)
+        self.res = torch.empty_like(self.ymid)
+        self.sums = torch.empty(2, dtype=torch.float64, device=plan.device)
+
+    def residual(self, y0, y1, f, dt, rtol, atol, store=True):
+        """Scaled squared 2-norm of y1 - y0 - dt f (and the residual in self.res when store);
+        one 16-byte device-to-host read."""
+        _lib.check(_lib.lib().spx_midpoint_residual(
+            self.plan.state_len, C.c_void_p(y0.data_ptr()), C.c_void_p(y1.data_ptr()), C.c_void_p(f.data_ptr()),
+            float(dt), float(rtol), float(atol), C.c_void_p(self.res.data_ptr()) if store else None,
+            C.c_void_p(self.sums.data_ptr()), C.c_void_p(self.ws.data_ptr()), C.c_size_t(self.ws.numel()),
+            _stream_ptr(None)), "spx_midpoint_residual")
+        sq, bad = self.sums.tolist()
+        if bad != 0.0:
+            raise FloatingPointError("implicit midpoint: non-finite residual")
+        return sq
+
+    def update(self, y0, y1, delta=None, sign=1.0):
+        """y1 += sign delta; y_mid = (y0 + y1) / 2."""
+        _lib.check(_lib.lib().spx_midpoint_update(
+            self.plan.state_len, C.c_void_p(y0.data_ptr()), C.c_void_p(y1.data_ptr()),
+            C.c_void_p(delta.data_ptr()) if delta is not None else None, float(sign),
+            C.c_void_p(self.ymid.data_ptr()), _stream_ptr(None)), "spx_midpoint_update")
+
+
+def step(plan: Plan, y0, dt, rtol, atol, max_iters=300, solver: NewtonGMRES | None = None, stats=None,
+         glue: _Glue | None = None, f0=None, want_error=True):
+    """One implicit midpoint step; returns (y1, y_error, f0) with y_error = y1 - (y0 + dt f(y0))
+    (spectrax/midpoint_solver.py:37-53; None unless want_error).  Per Newton iteration: one right-hand side at
+    y_mid, one fused residual + scaled-norm pass with a single scalar read, the GMRES
+    solve, and one fused update of y1 and y_mid."""
     solver = solver or NewtonGMRES(plan)
-    f0 = plan.rhs(y0)
-    y1_init = y0 + dt * f0
-    y1 = y1_init.clone()
-    fmid = torch.empty_like(y0)
+    glue = glue or _Glue(plan, solver.kws)
+    f0 = plan.rhs(y0) if f0 is None else f0
+    y1 = torch.add(y0, f0, alpha=dt)               # the explicit-Euler guess y1_init
+    glue.update(y0, y1)
     newton = 0
     for _ in range(max_iters):
-        ymid = 0.5 * (y0 + y1)
-        plan.rhs_into(ymid, fmid)
-        res = y1 - y0 - dt * fmid
-        scale = atol + rtol * torch.maximum(y0.abs(), y1.abs())
-        norm = torch.linalg.vector_norm(res / scale).item()
-        if not math.isfinite(norm):
-            raise FloatingPointError("implicit midpoint: non-finite residual")
+        plan.rhs_into(glue.ymid, glue.fmid)
+        norm = math.sqrt(glue.residual(y0, y1, glue.fmid, dt, rtol, atol))
         if norm < 1.0:
             break
-        delta, _rel, _its = solver.solve(ymid, -res, 0.5 * dt, atol=0.0)
-        y1 = y1 + delta
+        # (I - dt/2 J(y_mid)) delta = -res: solve with +res and subtract
+        delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=0.0)
+        glue.update(y0, y1, delta, -1.0)
         newton += 1
     if stats is not None:
         stats["newton"] = stats.get("newton", 0) + newton
         stats["rhs"] = stats.get("rhs", 0) + newton + 2
-    return y1, y1 - y1_init
+    return y1, (y1 - y0 - dt * f0) if want_error else None, f0
 
 
 def energies(plan: Plan, y: torch.Tensor, masses):
@@ -196,15 +227,41 @@ def energies(plan: Plan, y: torch.Tensor, masses):
     return em, sum(ke), ke
 
 
-def solve(plan: Plan, y0, t_max, dt, ts, solver: ImplicitMidpoint, masses, save_states=True):
-    """Fixed steps of size dt from 0 to t_max, landing exactly on each save time."""
+# Diffrax PIDController defaults (the Dopri8 stepper's), with the error order of this
+# order-2 solver: the next step is h clip(0.9 err^(-1/2), 1 if kept else 0.2, 10)
+_SAFETY, _FACTORMIN, _FACTORMAX, _ORDER = 0.9, 0.2, 10.0, 2.0
+
+
+def controller_factor(en: float, accepted: bool) -> float:
+    if en == 0.0:
+        f = _FACTORMAX
+    elif not math.isfinite(en):
+        f = _FACTORMIN
+    else:
+        f = _SAFETY * en ** (-1.0 / _ORDER)
+    return min(max(f, 1.0 if accepted else _FACTORMIN), _FACTORMAX)
+
+
+def solve(plan: Plan, y0, t_max, dt, ts, solver: ImplicitMidpoint, masses, save_states=True, adaptive=False,
+          ctrl_rtol=None, ctrl_atol=None, max_steps=1_000_000):
+    """Implicit midpoint from 0 to t_max, saving at ts.
+
+    adaptive=False: steps of dt, landing exactly on each save time.
+    adaptive=True (the reference's default, spectrax/_simulation.py:164-180): steps
+    end only on t_max; the step size follows Diffrax's PIDController on the RMS of
+    y_error / (ctrl_atol + ctrl_rtol max(|y0|, |y1|)), error order 2; a save time
+    inside an accepted step gets the linear interpolation of its end points (the
+    solver's LocalLinearInterpolation, spectrax/midpoint_solver.py:24).
+    Returns (saved states or None, energies (len(ts), 2 + Ns), info)."""
     ts = np.asarray(ts, np.float64)
     ng = NewtonGMRES(plan, restart=solver.restart, gmres_tol=solver.gmres_tol)
-    y = torch.as_tensor(y0).to(plan.device, torch.complex128).contiguous()
+    glue = _Glue(plan, ng.kws)
+    y = torch.as_tensor(y0).to(plan.device, torch.complex128).contiguous().clone()
+    n = plan.state_len
     t = 0.0
     isave = 0
     ys, en = [], []
-    info = {"steps": 0}
+    info = {"steps": 0, "rejected": 0}
 
     def save(yy):
         if save_states:
@@ -215,29 +272,52 @@ def solve(plan: Plan, y0, t_max, dt, ts, solver: ImplicitMidpoint, masses, save_
     while isave < len(ts) and ts[isave] <= t:
         save(y)
         isave += 1
+    h_prop = float(dt)
+    f0 = None
     while t < t_max * (1 - 1e-15):
-        t_stop = min(ts[isave], t_max) if isave < len(ts) else t_max
-        h = dt
-        landed = False
+        if info["steps"] + info["rejected"] >= max_steps:
+            raise RuntimeError("implicit midpoint: max_steps reached")
+        t_stop = t_max if adaptive else (min(ts[isave], t_max) if isave < len(ts) else t_max)
+        h, landed = h_prop, False
         if t + h * (1 + 1e-9) >= t_stop:
-            h = t_stop - t
-            landed = True
-        y, _ = step(plan, y, h, solver.rtol, solver.atol, solver.max_iters, ng, info)
-        t = t_stop if landed else t + h
-        info["steps"] += 1
-        while isave < len(ts) and ts[isave] <= t:
-            save(y)
+            h, landed = t_stop - t, True
+        y1, _, f0 = step(plan, y, h, solver.rtol, solver.atol, solver.max_iters, ng, info, glue, f0,
+                         want_error=False)
+        if adaptive:
+            sq = glue.residual(y, y1, f0, h, ctrl_rtol, ctrl_atol, store=False)
+            e = math.sqrt(sq / n)
+            accept = e < 1.0
+            h_next = h * controller_factor(e, accept)
+        else:
+            accept, h_next = True, h_prop
+        if not accept:
+            info["rejected"] += 1
+            h_prop = h_next
+            continue
+        t_new = t_stop if landed else t + h
+        while isave < len(ts) and ts[isave] <= t_new:
+            if adaptive and ts[isave] != t_new:
+                w = (ts[isave] - t) / h
+                save(torch.lerp(y, y1, w))
+            else:
+                save(y1)
             isave += 1
+        y, t = y1, t_new
+        f0 = None                                    # f(y) of the new state next step
+        info["steps"] += 1
+        h_prop = h_next if adaptive else h_prop
     info["matvecs"] = ng.matvecs
+    info["t"] = t
     ys_np = torch.stack(ys).cpu().numpy() if save_states and ys else None
     return ys_np, np.array(en), info
 
 
-def midpoint_solve(p, time, solver: ImplicitMidpoint, mask_mode=None):
+def midpoint_solve(p, time, solver: ImplicitMidpoint, mask_mode=None, adaptive=False):
     """Driver used by ``simulation(..., solver=ImplicitMidpoint(...))``."""
     from .dopri8 import species_masses
     from .params import initial_state
     plan = plan_for_params(p, mask_mode)
+    tol = float(p.get("ode_tolerance", 1e-12))
     ys, en, info = solve(plan, initial_state(p), float(p["t_max"]), float(p["dt"]), time, solver,
-                         species_masses(p))
+                         species_masses(p), adaptive=adaptive, ctrl_rtol=tol, ctrl_atol=tol)
     return ys, en, info

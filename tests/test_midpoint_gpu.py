@@ -42,7 +42,7 @@ def test_midpoint_step_matches_oracle(shape):
     ref, ref_err, _ = omid.step(f, y0, 0.1, rtol=1e-10, atol=1e-10)
     plan = vector_field.plan_for_params(p, "divide")
     ng = midpoint.NewtonGMRES(plan, restart=30, gmres_tol=1e-12)
-    y1, err = midpoint.step(plan, torch.from_numpy(y0).cuda(), 0.1, 1e-10, 1e-10, solver=ng)
+    y1, err, _ = midpoint.step(plan, torch.from_numpy(y0).cuda(), 0.1, 1e-10, 1e-10, solver=ng)
     assert rel_err(y1.cpu().numpy(), ref) < 1e-9
     assert rel_err(err.cpu().numpy(), ref_err) < 1e-6
 
@@ -70,10 +70,65 @@ def test_simulation_with_implicit_midpoint():
     import spectrax_gb300 as sg
     from spectrax_gb300.dopri8 import simulation
     out = simulation({"t_max": 0.3, "ode_tolerance": 1e-10}, Nx=9, Nn=8, timesteps=4, dt=0.1,
-                     solver=sg.ImplicitMidpoint(rtol=1e-10, atol=1e-10))
+                     solver=sg.ImplicitMidpoint(rtol=1e-10, atol=1e-10), adaptive_time_step=False)
     assert out["Ck"].shape == (4, 16, 1, 9, 1)
     assert out["solver_stats"]["steps"] == 3
     assert np.all(np.isfinite(out["EM_energy"]))
+    # the reference's default: the step size follows the PID controller on y_error
+    out = simulation({"t_max": 0.3, "ode_tolerance": 1e-5}, Nx=9, Nn=8, timesteps=4, dt=0.1,
+                     solver=sg.ImplicitMidpoint(rtol=1e-10, atol=1e-10))
+    assert out["Ck"].shape == (4, 16, 1, 9, 1)
+    assert out["solver_stats"]["steps"] != 3
+    assert np.all(np.isfinite(out["EM_energy"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(4, 5, 1, 2, 2, 2, 1), (9, 1, 1, 12, 1, 1, 2)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_adaptive_midpoint_matches_oracle(shape):
+    # PID controller on y_error = y1 - y1_init (order 2), steps ending only on t1,
+    # linear interpolation at the save times (spectrax/midpoint_solver.py:24,51):
+    # the same accepted / rejected steps as the oracle and saved states within 1e-9.
+    # The Newton tolerance (1e-12) is far below the controller's (1e-6), so the
+    # controller sees the same error estimate on both sides.
+    import torch
+    import spectrax_gb300 as sg
+    from spectrax_gb300 import midpoint, vector_field
+    p = _params(shape)
+    y0 = _state(shape)
+    ts = np.linspace(0.0, 0.5, 7)
+    ref = omid.solve(lambda y: orhs.rhs(p, y), 0.5, y0, 0.05, ts, rtol=1e-12, atol=1e-12, ctrl_rtol=1e-6,
+                     ctrl_atol=1e-6)
+    plan = vector_field.plan_for_params(p, "divide")
+    solver = sg.ImplicitMidpoint(rtol=1e-12, atol=1e-12, restart=30, gmres_tol=1e-13)
+    ys, en, info = midpoint.solve(plan, torch.from_numpy(y0), 0.5, 0.05, ts, solver, [1.0, 1.0][:shape[6]],
+                                  adaptive=True, ctrl_rtol=1e-6, ctrl_atol=1e-6)
+    assert (info["steps"], info["rejected"]) == (ref["accepted"], ref["rejected"]), (info, ref)
+    assert ref["rejected"] + ref["accepted"] > 5
+    assert rel_err(ys, ref["ys"]) < 1e-9
+
+
+@pytest.mark.gpu
+def test_midpoint_residual_kernel():
+    # the fused residual / scaled norm against NumPy, with and without storing r
+    import torch
+    from spectrax_gb300 import midpoint, vector_field
+    shape = (8, 8, 1, 2, 2, 2, 1)
+    plan = vector_field.plan_for_params(_params(shape, 2), "divide")
+    n = plan.state_len
+    rng = np.random.default_rng(9)
+    y0, y1, f = (rng.standard_normal(n) + 1j * rng.standard_normal(n) for _ in range(3))
+    g = midpoint._Glue(plan, midpoint.NewtonGMRES(plan, restart=2).kws)
+    t = [torch.from_numpy(a).cuda() for a in (y0, y1, f)]
+    sq = g.residual(*t, 0.03, 1e-3, 1e-4)
+    r = y1 - y0 - 0.03 * f
+    ref = np.sum(np.abs(r / (1e-4 + 1e-3 * np.maximum(np.abs(y0), np.abs(y1)))) ** 2)
+    assert abs(sq - ref) <= 1e-12 * ref
+    assert rel_err(g.res.cpu().numpy(), r) < 1e-15
+    assert abs(g.residual(*t, 0.03, 1e-3, 1e-4, store=False) - sq) == 0.0
+    g.update(t[0], t[1], t[2], -0.5)
+    assert rel_err(t[1].cpu().numpy(), y1 - 0.5 * f) < 1e-15
+    assert rel_err(g.ymid.cpu().numpy(), 0.5 * (y0 + y1 - 0.5 * f)) < 1e-15
 
 
 @pytest.mark.gpu

@@ -111,5 +111,5 @@ def test_orszag_tang_rhs_jvp_and_implicit_step():
     _check(plan.jvp_into(y, torch.from_numpy(v).cuda(), out).cpu().numpy(), ref, "jvp", 1e-12)
     ng = midpoint.NewtonGMRES(plan, restart=30, gmres_tol=1e-10)
     stats = {}
-    y1, _ = midpoint.step(plan, y, 0.1, 1e-10, 1e-10, solver=ng, stats=stats)
+    y1, _, _ = midpoint.step(plan, y, 0.1, 1e-10, 1e-10, solver=ng, stats=stats)
     _check(y1.cpu().numpy(), ref, "step", 1e-10)
