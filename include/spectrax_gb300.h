@@ -156,6 +156,18 @@ int spx_jvp_lin(const spx_plan* plan, const void* lin, const void* v, void* Jv, 
  * recurrence of the normalised Hermite functions (finite for every n).
  */
 int spx_hermite_basis(int32_t N, const double* xi, int64_t nv, double* out, void* stream);
+/*
+ * f(x, v) of spectrax/_inverse_transform.py:97-125 for `nlead` sets of coefficient
+ * planes Ck (nlead x Nn*Nm*Np planes, centred order, complex128, device):
+ * f[(l, point), v] = exp(-|xi_v|^2) sum_{n,m,p} C_l,(n,m,p)(point) bx[n, v] by[m, v] bz[p, v]
+ * with C = Re ifftn(ifftshift(Ck)) (1/N).  The plan: one species, every Fourier mode
+ * kept (cut >= N/2 on every axis).  bx, by, bz: (Nn | Nm | Np) x nv per-axis bases
+ * (spx_hermite_basis), xi: 3 x nv (xi_x, xi_y, xi_z), f: nlead*plane x nv, all on the
+ * device; ws: spx_fxv_workspace_bytes(plan, nlead) bytes (the real-space planes).
+ */
+size_t spx_fxv_workspace_bytes(const spx_plan* plan, int64_t nlead);
+int spx_fxv(const spx_plan* plan, const void* Ck, int64_t nlead, const double* bx, const double* by, const double* bz,
+            const double* xi, int64_t nv, double* f, void* ws, size_t ws_bytes, void* stream);
 
 /*
  * Initial Hermite-Fourier coefficients of drifting Maxwellians on the device

@@ -116,6 +116,8 @@ _PROTOS = {
     "spx_jvp_lin": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_krylov_ws_bytes": (C.c_size_t, [C.c_int64]),
     "spx_hermite_basis": (C.c_int, [C.c_int32, _VP, C.c_int64, _VP, _VP]),
+    "spx_fxv_workspace_bytes": (C.c_size_t, [_VP, C.c_int64]),
+    "spx_fxv": (C.c_int, [_VP, _VP, C.c_int64, _VP, _VP, _VP, _VP, C.c_int64, _VP, _VP, C.c_size_t, _VP]),
     "spx_maxwellian": (C.c_int, [_VP, _VP, _VP, C.c_int32, _VP, _VP]),
     "spx_krylov_cgs2": (C.c_int, [_VP, C.c_int64, C.c_int32, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_krylov_axpy": (C.c_int, [_VP, C.c_int64, C.c_int32, _VP, _VP, _VP]),
