@@ -4,7 +4,7 @@ The GPU tests rebuild the same seeded inputs with the package's own builders and
 compare the device results with what this script stores:
 
 * two_stream_nx129_nn256.npz -- the two-stream workload (Nx = 129, Nn = 256,
-  3 species), adaptive Dopri8 (rtol 1e-10, atol 1e-12) from t = 0 to 100 with
+  3 species), adaptive Dopri8 (rtol 1e-10, atol 1e-12, first step 0.2) from t = 0 to 100 with
   201 save times (Diffrax SaveAt(ts): dense output): the saved energies, the
   step counts and the final field lines and Hermite-plane norms;
 * adjoint_two_stream_nx65_nn128.npz -- the adjoint workload's loss (2000 fixed
@@ -70,7 +70,9 @@ def two_stream():
         en[i, 2:] = e["kinetic_energy_species"][0].real
 
     t0 = time.time()
-    out = od.solve(lambda t, y: orhs.rhs(p, y, "divide"), 0.0, 100.0, y0, 0.01, ts=ts, adaptive=True,
+    # first step 0.2: its error norm (~0.08) is far above the rounding noise of the
+    # error estimate (~3e-6), so the device and the oracle choose the same steps
+    out = od.solve(lambda t, y: orhs.rhs(p, y, "divide"), 0.0, 100.0, y0, 0.2, ts=ts, adaptive=True,
                    rtol=1e-10, atol=1e-12, on_save=on_save, saveat="interpolate")
     print(f"two_stream: {out['accepted']} accepted, {out['rejected']} rejected, {time.time() - t0:.0f} s")
     yf = out["y"]

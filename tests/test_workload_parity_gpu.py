@@ -6,7 +6,8 @@
   every save, the final field lines within 1e-9;
 * adjoint workload (Nx = 65, Nn = 128, 2000 steps of dt = 0.05): the loss within
   1e-9 of the oracle's, and the adjoint gradient of each of (k, nu, u, amplitude)
-  against central differences of the device loss (h = 1e-6 relative);
+  within 1e-6 of central differences of the device loss (h = 1e-6 relative; 1e-4
+  for nu, see the test);
 * Orszag-Tang-like 2D3V state (64 x 64, 8^3 Hermite modes, 2 species, 4.2 M
   coefficients): one right-hand side and one Jacobian-vector product within
   1e-12 (norm, per-plane norms and 4096 sampled entries, relative to the
@@ -39,7 +40,9 @@ def test_two_stream_to_t100_matches_oracle():
     ref = _fixture("two_stream_nx129_nn256.npz")
     p, y0 = bench.two_stream_params(seed=0)
     plan = plan_for_params(p, "divide")
-    s = Dopri8Solver(plan, 0.0, 100.0, 0.01, ts=ref["ts"], adaptive=True, rtol=1e-10, atol=1e-12,
+    # first step 0.2 as in the fixture: every error norm of the run stays far above the
+    # rounding noise of the error estimate, so both sides take the same steps
+    s = Dopri8Solver(plan, 0.0, 100.0, 0.2, ts=ref["ts"], adaptive=True, rtol=1e-10, atol=1e-12,
                      masses=[1.0, 1.0, 1836.0], save_states=False, max_steps=1 << 30)
     s.reset(torch.from_numpy(y0))
     assert s.run() == 1
@@ -64,16 +67,17 @@ def test_adjoint_workload_loss_and_gradients():
     prob = TwoStreamProblem(Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0)
     L, g = prob.loss_and_grad(*theta)
     assert abs(L - float(ref["loss"])) <= 1e-9 * abs(float(ref["loss"]))
+    # central differences with h = 1e-6 relative; for nu, whose gradient is ~6e-7
+    # (|dL/dnu| ~ 4e-4 |L|), h = 1e-4 relative: the loss carries ~2e-14 relative
+    # rounding from its 2000 steps, which at h = 1e-6 would limit the quotient to
+    # ~4e-5 relative, while the O(h^2) truncation stays below 1e-8 at h = 1e-4
     for i, name in enumerate(("k", "nu", "u", "amp")):
-        h = 1e-6 * abs(theta[i])
+        h = (1e-4 if name == "nu" else 1e-6) * abs(theta[i])
         up, dn = list(theta), list(theta)
         up[i] += h
         dn[i] -= h
         fd = (prob.loss(*up) - prob.loss(*dn)) / (2 * h)
-        # rounding of the two losses (about 1e-15 |L| each) bounds what the
-        # difference quotient can resolve
-        floor = 4e-15 * abs(L) / h
-        assert abs(g[name] - fd) <= max(1e-6 * abs(fd), floor), (name, g[name], fd, floor)
+        assert abs(g[name] - fd) <= 1e-6 * abs(fd), (name, g[name], fd)
 
 
 def _reduced(v, nplanes, plane, idx):
