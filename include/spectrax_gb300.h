@@ -385,7 +385,8 @@ typedef struct spx_batch_opts {
   int32_t nsave;         /* shared save times (energies recorded at each) */
   const double* save_ts; /* host, nsave increasing times in [0, t1] */
   int32_t cluster;       /* CTAs per instance, 1..16 (above 8: non-portable cluster sizes) */
-  int32_t tile;          /* Hermite planes per tile (0: 8; at most 32) */
+  int32_t tile;          /* Hermite planes per tile (0: 8; at most 32); -1: per instance, the
+                            height whose tiles fill the fewest whole rounds of the cluster */
   const double* masses;  /* host, n x SPX_MAX_SPECIES species masses (NULL: ones) */
   int32_t hermitian;     /* 1: an instance with odd Nx whose initial state is exactly Hermitian
                             (C(-k) == conj C(k) on every line) uses packed real transforms */

@@ -168,9 +168,10 @@ def _signature(problems, t1, rtol):
 
 
 def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses=None,
-             clusters=(1, 2, 4, 8), tiles=(4, 8, 16, 32), use_cache=True, verbose=False):
+             clusters=(1, 2, 4, 8, 16), tiles=(4, 8, 16, 32, -1), use_cache=True, verbose=False):
     """Time a short horizon of the real instances for every (cluster, tile) and
-    return the fastest as dict(cluster=, tile=, ms=, table=[...])."""
+    return the fastest as dict(cluster=, tile=, ms=, table=[...]).  tile -1: each
+    instance's tile height chosen to fill whole rounds of the cluster's CTAs."""
     sig = _signature(problems, t1_probe, rtol)
     path = _cache_path()
     cache = {}

@@ -647,9 +647,22 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     BInst& I = b->hinst[i];
     std::memset(&I, 0, sizeof(I));
     I.P = tmp.host;
-    // batch tiling: `tile` planes per tile (0: 8)
-    int T = o->tile > 0 ? o->tile : 8;
-    T = std::min(std::min(T, BATCH_MAX_TILE), p.Nn);   // the per-plane coefficient scratch holds 32 planes
+    // batch tiling: `tile` planes per tile (0: 8); tile < 0: per instance, the fewest
+    // rounds r over the cluster's CTAs whose Ns * ntiles + 1 (the field tile) <= r C
+    // tiles hold at most BATCH_MAX_TILE planes each, so small instances use every CTA
+    int T;
+    if (o->tile < 0) {
+      T = BATCH_MAX_TILE;
+      for (int r = 1; r <= 64; ++r) {
+        const int per = (r * o->cluster - 1) / p.Ns;       // tiles per species in r rounds
+        if (per < 1) continue;
+        const int t = (p.Nn + per - 1) / per;
+        if (t <= BATCH_MAX_TILE) { T = t; break; }
+      }
+    } else {
+      T = o->tile > 0 ? o->tile : 8;
+    }
+    T = std::max(1, std::min(std::min(T, BATCH_MAX_TILE), p.Nn));   // the coefficient scratch holds 32 planes
     int ntiles = (p.Nn + T - 1) / T;
     T = (p.Nn + ntiles - 1) / ntiles;
     I.P.tile = T;

@@ -30,7 +30,7 @@ def _small_insts(seed=0):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cluster,tile", [(1, 8), (2, 4), (4, 8), (8, 16)])
+@pytest.mark.parametrize("cluster,tile", [(1, 8), (2, 4), (4, 8), (8, 16), (8, -1), (16, -1)])
 def test_batch_matches_serial(cluster, tile):
     import torch
     from spectrax_gb300.batch import BatchSolver, serial_solve
