@@ -75,10 +75,11 @@ def test_simulation_with_implicit_midpoint():
     assert out["solver_stats"]["steps"] == 3
     assert np.all(np.isfinite(out["EM_energy"]))
     # the reference's default: the step size follows the PID controller on y_error
-    out = simulation({"t_max": 0.3, "ode_tolerance": 1e-5}, Nx=9, Nn=8, timesteps=4, dt=0.1,
+    out = simulation({"t_max": 0.3, "ode_tolerance": 1e-7}, Nx=9, Nn=8, timesteps=4, dt=0.1,
                      solver=sg.ImplicitMidpoint(rtol=1e-10, atol=1e-10))
     assert out["Ck"].shape == (4, 16, 1, 9, 1)
-    assert out["solver_stats"]["steps"] != 3
+    st = out["solver_stats"]
+    assert st["steps"] > 10 and st["rejected"] > 0          # the oracle takes 27 + 3
     assert np.all(np.isfinite(out["EM_energy"]))
 
 

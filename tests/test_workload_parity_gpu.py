@@ -7,7 +7,7 @@
 * adjoint workload (Nx = 65, Nn = 128, 2000 steps of dt = 0.05): the loss within
   1e-9 of the oracle's, and the adjoint gradient of each of (k, nu, u, amplitude)
   within 1e-6 of central differences of the device loss (h = 1e-6 relative; 1e-4
-  for nu, see the test);
+  for nu and the amplitude, see the test);
 * Orszag-Tang-like 2D3V state (64 x 64, 8^3 Hermite modes, 2 species, 4.2 M
   coefficients): one right-hand side and one Jacobian-vector product within
   1e-12 (norm, per-plane norms and 4096 sampled entries, relative to the
@@ -67,12 +67,13 @@ def test_adjoint_workload_loss_and_gradients():
     prob = TwoStreamProblem(Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0)
     L, g = prob.loss_and_grad(*theta)
     assert abs(L - float(ref["loss"])) <= 1e-9 * abs(float(ref["loss"]))
-    # central differences with h = 1e-6 relative; for nu, whose gradient is ~6e-7
-    # (|dL/dnu| ~ 4e-4 |L|), h = 1e-4 relative: the loss carries ~2e-14 relative
-    # rounding from its 2000 steps, which at h = 1e-6 would limit the quotient to
-    # ~4e-5 relative, while the O(h^2) truncation stays below 1e-8 at h = 1e-4
+    # central differences with h = 1e-6 relative for k and u; for nu and the
+    # amplitude, whose logarithmic sensitivities theta dL/dtheta are 6e-7 and 3e-6
+    # (~1e-3 |L|), h = 1e-4 relative: the loss carries ~1e-16 of rounding from its
+    # 2000 steps, which at h = 1e-6 would limit the quotient to ~4e-5 relative,
+    # while the O(h^2) truncation stays below 1e-8 at h = 1e-4
     for i, name in enumerate(("k", "nu", "u", "amp")):
-        h = (1e-4 if name == "nu" else 1e-6) * abs(theta[i])
+        h = (1e-4 if name in ("nu", "amp") else 1e-6) * abs(theta[i])
         up, dn = list(theta), list(theta)
         up[i] += h
         dn[i] -= h
