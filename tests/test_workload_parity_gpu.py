@@ -1,9 +1,18 @@
 """GPU: the full-size workloads against oracle fixtures (tests/golden/make_workload_fixtures.py).
 
 * two-stream, Nx = 129, Nn = 256, 3 species, adaptive Dopri8 (rtol 1e-10,
-  atol 1e-12) to t = 100 with 201 dense-output saves: the same accepted and
-  rejected step counts, field and kinetic energies within 1e-9 relative at
-  every save, the final field lines within 1e-9;
+  atol 1e-12) to t = 100 with 201 dense-output saves: field and kinetic
+  energies within 1e-9 relative at every save and the final field lines within
+  1e-9, on both the packed (Hermitian) and the general stages; the step counts
+  within a few steps of the oracle's on the general stages and within 3 % on
+  the packed ones.  On this workload the error estimate is set by rounding: 99.99 %
+  of the scaled error norm comes from the ion Hermite-1 plane, whose right-hand
+  side E_x * C_0 multiplies the field by the ion density mode C_0(k=0) =
+  1/alpha_i^3 ~ 6.3e5, so its transform carries ~1e-13 of rounding noise
+  against an absolute tolerance of 1e-12.  Each FFT ordering takes its own,
+  equally valid, step sequence (the general stages end within one step of the
+  oracle; the packed stages, which pair the ion line with its neighbour in one
+  complex transform, take ~2 % more steps) while the energies agree to ~1e-10;
 * adjoint workload (Nx = 65, Nn = 128, 2000 steps of dt = 0.05): the loss within
   1e-9 of the oracle's, and the adjoint gradient of each of (k, nu, u, amplitude)
   within 1e-6 of central differences of the device loss (h = 1e-6 relative; 1e-4
@@ -31,7 +40,8 @@ def _fixture(name):
 
 
 @pytest.mark.gpu
-def test_two_stream_to_t100_matches_oracle():
+@pytest.mark.parametrize("hermitian", [True, False], ids=["packed", "general"])
+def test_two_stream_to_t100_matches_oracle(hermitian):
     import torch
 
     import bench
@@ -40,14 +50,18 @@ def test_two_stream_to_t100_matches_oracle():
     ref = _fixture("two_stream_nx129_nn256.npz")
     p, y0 = bench.two_stream_params(seed=0)
     plan = plan_for_params(p, "divide")
-    # first step 0.2 as in the fixture: every error norm of the run stays far above the
-    # rounding noise of the error estimate, so both sides take the same steps
     s = Dopri8Solver(plan, 0.0, 100.0, 0.2, ts=ref["ts"], adaptive=True, rtol=1e-10, atol=1e-12,
-                     masses=[1.0, 1.0, 1836.0], save_states=False, max_steps=1 << 30)
+                     masses=[1.0, 1.0, 1836.0], save_states=False, max_steps=1 << 30, hermitian=hermitian)
     s.reset(torch.from_numpy(y0))
     assert s.run() == 1
     st = s.stats()
-    assert (st["accepted"], st["rejected"]) == (int(ref["accepted"]), int(ref["rejected"])), st
+    assert st["hermitian"] == hermitian
+    acc, rej = int(ref["accepted"]), int(ref["rejected"])
+    # the step sequence follows the rounding noise of the ion Hermite-1 plane (module docstring)
+    if hermitian:
+        assert abs(st["accepted"] - acc) <= 0.03 * acc, (st, acc, rej)
+    else:
+        assert abs(st["accepted"] - acc) <= 5 and abs(st["rejected"] - rej) <= 5, (st, acc, rej)
     en = s.energies().cpu().numpy()
     np.testing.assert_allclose(en[:, 0], ref["energies"][:, 0], rtol=1e-9)    # field energy
     np.testing.assert_allclose(en[:, 1:], ref["energies"][:, 1:], rtol=1e-9)  # kinetic, total and per species
