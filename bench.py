@@ -245,9 +245,10 @@ def run_extras(args):
             "serial_plain_rhs_s_estimated": tp_all, "speedup_vs_plain_rhs": tp_all / tb,
             "serial_plain_rhs_sample": f"{len(sub)} instances (every 64th) timed: {tp_sub:.3f} s",
             "note": "per-instance adaptive Dopri8 (rtol=atol=1e-8). serial_s / speedup: the same instances "
-                    "one by one through the graph-captured single-instance device solver (general "
-                    "complex-transform stages); speedup_vs_plain_rhs: one by one through the plain RHS "
-                    "with a host-driven Dopri8"}
+                    "one by one through the graph-captured single-instance device solver (the batch's "
+                    "arithmetic: packed transforms for the Hermitian instances, the same product "
+                    "grids); speedup_vs_plain_rhs: one by one through the plain RHS with a "
+                    "host-driven Dopri8"}
     except Exception as e:  # keep the main line even if an extra fails
         out["batch_scan"] = {"error": repr(e)}
     try:
@@ -541,7 +542,8 @@ def run_ours(args):
     vec_dense, vec_touched = perf.dopri8_vectors_per_step_dense(13), perf.dopri8_vectors_per_step()
     bytes_launch = vec_dense * n * 16 / 13.0
     packed = bool(st1.get("hermitian"))
-    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile), plan.product_grid, packed=packed)
+    ops = perf.rhs_ops(SHAPE, plan.tile, -(-SHAPE[3] // plan.tile), plan.product_grid, packed=packed,
+                       radices=plan.product_radices)
     # FP64 work the step executes: 13 RHS + the Runge-Kutta combinations (4 flops per
     # complex FMA; half of them when only the k <= 0 half of each plane is formed)
     flops_step = 13.0 * ops.flops + (2.0 if packed else 4.0) * perf.dopri8_combination_fmas_per_entry() * n

@@ -90,21 +90,25 @@ int spx_plan_info(const spx_plan* plan, int32_t* tile, int32_t* ntiles, int32_t*
 
 /*
  * Grid of the nonlinear products in the 1D1V Dopri8 stage kernels (the device
- * stepper and the adjoint's recomputation; the batch keeps Nx points).  The masked factors hold
+ * stepper, the adjoint's recomputation and every batch instance).  The masked factors hold
  * |k| <= K, so the kept modes of their product are exact on any grid of
  * M >= 3K + 1 points (adding back the one term the reference's Nx-point grid
  * folds onto |k| = K when Nx = 3K).  For plans created afterwards: mode 0
- * (default) uses such a grid where its transforms are modeled >= 2x cheaper
- * than Nx-point ones (prime Nx: 97 -> 104, 127 -> 128, 251 -> 256); mode 1 always Nx
- * points; mode 2 the cheapest grid of <= 0.8x the modeled FP64 work, one with
- * more Stockham stages than Nx only at <= 0.5x (129 -> 136, 65 -> 64; measured
- * slower than Nx on the two-stream stage kernel).  Only plans with 3K <= Nx get
+ * (default) gives an Nx with a prime factor >= 5 the length M = 2^a 3^b of
+ * least modeled time in register butterflies of radices 4, 3 and 2 (129 -> 144
+ * = 4*4*3*3, 65 -> 64, 33 -> 36, 17 -> 16, 97 -> 108, 127 -> 128), and keeps
+ * Nx = 2^a 3^b; mode 1 always Nx points; mode 2 the cheapest grid of <= 0.8x
+ * the FP64 count of the Nx-point transforms, one with more Stockham stages than
+ * Nx only at <= 0.5x (129 -> 136, 65 -> 64).  Only plans with 3K <= Nx get
  * M != Nx (with 3K > Nx the Nx-point product folds more than the one term).
  * Results agree to rounding.  spx_plan_product_grid returns the grid length M
  * of a plan.
  */
 int spx_set_product_grid(int32_t mode);
 int spx_plan_product_grid(const spx_plan* plan);
+/* The Stockham radices of that grid in stage order (the first max of them into
+ * `radices`); returns their count (0 for a grid of one point). */
+int spx_plan_product_radices(const spx_plan* plan, int32_t* radices, int32_t max);
 /* The product grid a 1D1V plan with Nx = nx and mask cut `cut` gets under
  * `mode` (host only; no device, no plan).  It applies the selection rule only:
  * plan creation additionally keeps Nx points when the stage kernel with the

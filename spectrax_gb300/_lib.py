@@ -108,6 +108,7 @@ _PROTOS = {
     "spx_rhs_workspace_bytes": (C.c_size_t, [_VP]),
     "spx_set_product_grid": (C.c_int, [C.c_int32]),
     "spx_plan_product_grid": (C.c_int, [_VP]),
+    "spx_plan_product_radices": (C.c_int, [_VP, C.POINTER(C.c_int32), C.c_int32]),
     "spx_product_grid_for": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     "spx_rhs": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "spx_jvp": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),

@@ -217,13 +217,14 @@ def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses
 
 
 # ----------------------------------------------------------------- serial baseline
-def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermitian=False, saveat="interpolate"):
+def serial_solve(insts, t1, dt0=0.01, rtol=1e-8, atol=1e-8, save_ts=None, hermitian=True, saveat="interpolate"):
     """Solve the instances one after another with the single-instance device
-    Dopri8 (plain GPU right-hand side per stage).  Returns (final states, stats,
+    Dopri8 (graph-captured stage kernels).  Returns (final states, stats,
     energies, seconds); the plans and solvers (device buffers, captured graphs)
     are built before the clock starts, so the seconds cover only the solves.
-    hermitian=False keeps the general complex-transform stages, the same
-    arithmetic as the batched kernel."""
+    hermitian=True (as the batch) runs packed real transforms for exactly
+    Hermitian instances, on the same product grids: the batched kernel's
+    arithmetic; False forces the general complex-transform stages."""
     from .dopri8 import Dopri8Solver
     solvers = []
     for it in insts:

@@ -402,8 +402,8 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
             for (int i = threadIdx.x; i < nt * N; i += blockDim.x) epi(b0 + i, i, __ldcg(Ki + b0 + i));
             return;
           }
-          double2* tB = sA + (size_t)(P.tile + 1) * N;
-          double2* U = tB + (size_t)(P.tile + 1) * N;
+          double2* tB = sA + (size_t)(P.tile + 1) * P.axm.n;
+          double2* U = tB + (size_t)(P.tile + 1) * P.axm.n;
           double2* F3 = U + (size_t)(P.tile + 2) * N;
           for (int i = threadIdx.x; i < (nt + 2) * N; i += blockDim.x) {
             const int n = n0 - 1 + i / N;
@@ -414,8 +414,8 @@ __global__ void __launch_bounds__(NTHREADS, SPX_BATCH_MIN_BLOCKS) k_batch(BArgs 
             F3[i] = __ldcg(in + P.nc + (size_t)(q == 0 ? 0 : (q == 1 ? 5 : 4)) * N + (i % N));
           }
           __syncthreads();
-          if (herm) rhs1v_tile_u<true, false>(P, stab, sp, n0, nt, U, F3, sA, tB, scoef, epi);
-          else rhs1v_tile_u<false, false>(P, stab, sp, n0, nt, U, F3, sA, tB, scoef, epi);
+          if (herm) rhs1v_tile_u<true, true>(P, stab, sp, n0, nt, U, F3, sA, tB, scoef, epi);
+          else rhs1v_tile_u<false, true>(P, stab, sp, n0, nt, U, F3, sA, tB, scoef, epi);
         };
         if (stage < rk::S - 1) {
           EpiNextB epi{Ki, Sb[(stage + 1) & 1], Y, K, len, &terms};
@@ -640,9 +640,9 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
       return SPX_E_UNSUPPORTED;
     }
     spx_plan tmp;
-    // products on the Nx-point grid: one tile variant keeps the batch kernel's
-    // register allocation (both variants in it spilled 60 % more)
-    rc = build_plan_host(&p, nsm, &tmp, 0, 0);
+    // products on the plan's product grid (M points, M = Nx where Nx is already
+    // 2^a 3^b): the kernel holds that one tile variant, which also runs M = Nx
+    rc = build_plan_host(&p, nsm, &tmp, 0, 1);
     if (rc != SPX_OK) { batch_free(b); return rc; }
     BInst& I = b->hinst[i];
     std::memset(&I, 0, sizeof(I));
@@ -672,9 +672,9 @@ int spx_batch_create(int32_t n, const spx_problem* pbs, const spx_batch_opts* o,
     coef_off[i] = coefs.size();
     coefs.insert(coefs.end(), tmp.coef.begin(), tmp.coef.end());
     tab_max = std::max(tab_max, I.P.tab_len);
-    // work area: two line buffers (T+1 lines), staged planes (T+2), field lines (3);
-    // the field tile reuses it for its (2 Ns + 12)-line gather + output area
-    work_max = std::max(work_max, std::max(2 * (T + 1) + (T + 2) + 3, 2 * p.Ns + 12) * p.Nx);
+    // work area: two line buffers (T+1 lines of M), staged planes (T+2 of Nx), field
+    // lines (3); the field tile reuses it for its (2 Ns + 12)-line gather + output area
+    work_max = std::max(work_max, std::max(2 * (T + 1) * I.P.axm.n + (T + 5) * p.Nx, (2 * p.Ns + 12) * p.Nx));
     if (o->hermitian && (p.Nx & 1)) {
       bool anti = true;
       for (int c = 0; c < p.Nx; ++c)

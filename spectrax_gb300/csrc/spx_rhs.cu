@@ -159,18 +159,52 @@ static std::vector<std::vector<int>> radix_orders(int m) {
   return out;
 }
 
-// 0: a product grid only where it is modeled >= 2x cheaper; 1: always Nx;
-// 2: the cheapest modeled grid at <= 0.8x without an extra stage
+// 0: a register-radix grid where Nx needs odd two-phase stages; 1: always Nx;
+// 2: the cheapest grid by FP64 count at <= 0.8x without an extra stage
 static int g_product_grid = 0;
 
+// Modeled cost of one transform of m points through register butterflies of
+// radices 4, 3, 2 in the order `rads`: FP64 instructions per point of each stage
+// (radix 4: 16 per butterfly + 12 for twiddles, radix 3: 12 + 8, radix 2: 4 + 4;
+// the first stage has no twiddles) plus kStageCost per Stockham stage (a barrier
+// and a pass through shared memory).  Fitted to the two-stream stage kernel
+// (Nx = 129 planes, tiles of 6 planes): 144 = 4*4*3*3 ran 0.311 ms per Dopri8
+// attempt, 192 = 4*4*4*3 0.337, 162 = 3^4*2 0.344, 256 = 4^4 0.375, against
+// 0.382 for 43*3 (two-phase radix 43); per-stage cost about 480 FP64
+// instructions, chains with radix 8 or a leading 2 slower than the count.
+static double register_chain_cost(int m, const std::vector<int>& rads) {
+  constexpr double kStageCost = 480.0;
+  double c = 0.0;
+  for (size_t i = 0; i < rads.size(); ++i) {
+    const int R = rads[i];
+    const double bf = (R == 4 ? 16.0 : R == 3 ? 12.0 : 4.0) + (i > 0 ? (R == 4 ? 12.0 : R == 3 ? 8.0 : 4.0) : 0.0);
+    c += (double)m / R * bf + kStageCost;
+  }
+  return c;
+}
+
+// Radices 4 (as many as fit), then 3, then a lone 2 for m = 2^a 3^b; empty if m
+// has another prime factor.
+static std::vector<int> register_chain(int m) {
+  std::vector<int> r;
+  int a = 0, b = 0;
+  while (m % 2 == 0) { m /= 2; ++a; }
+  while (m % 3 == 0) { m /= 3; ++b; }
+  if (m != 1) return r;
+  for (int i = 0; i < a / 2; ++i) r.push_back(4);
+  for (int i = 0; i < b; ++i) r.push_back(3);
+  if (a & 1) r.push_back(2);
+  return r;
+}
+
 // Product grid of the fused 1D1V stepper for an axis of n points and mask cut
-// K: the cheapest length m >= 3K+1 (m <= n when max_n) with radices 2, 4, 8 or
-// odd up to 31, by line_pair_cost.  Mode 0 keeps it only at <= 0.5 of the
-// n-point cost (prime n and the like): measured on the two-stream stage kernel
-// (Nx = 129), grids of 0.67x the FP64 work (144 = 9*8*2, 136 = 17*8) ran
-// 1.5-4 % slower than the 43*3 transform, each point and Stockham pass costing
-// shared-memory traffic and barriers the count does not see.  Mode 2 keeps it
-// at <= 0.8 with no more stages than n.  Returns m == n (and rads empty) otherwise.
+// K (both factors of the product are masked to |k| <= K, so any m >= 3K+1 gives
+// the kept modes exactly; m <= n when max_n).  Mode 0: an n with a prime factor
+// >= 5 (whose transform needs the two-phase odd-radix stages, measured slower than
+// their FP64 count) takes the 2^a 3^b length of least register_chain_cost;
+// n = 2^a 3^b keeps n.  Mode 2: the cheapest length by line_pair_cost (radices 2,
+// 4, 8 or odd up to 31) at <= 0.8x of n's, with no more stages than n.  Returns
+// m == n (and rads empty) otherwise.
 static int choose_product_grid(int n, int cut, bool max_n, std::vector<int>& rads, int mode = -1) {
   rads.clear();
   if (mode < 0) mode = g_product_grid;
@@ -178,9 +212,22 @@ static int choose_product_grid(int n, int cut, bool max_n, std::vector<int>& rad
   // pair k1 = k2 = +-cut (3 cut == n); with 3 cut > n more terms alias on the
   // n-point grid than the stepper adds back, so such plans keep n
   if (mode == 1 || cut < 1 || n < 8 || 3 * cut > n) return n;
+  if (mode == 0) {
+    if (!register_chain(n).empty()) return n;
+    double best = 0.0;
+    int bm = n;
+    for (int m = 3 * cut + 1; m <= 2 * n; ++m) {
+      if (max_n && m > n) break;
+      const std::vector<int> r = register_chain(m);
+      if (r.empty() || (int)r.size() > MAXST) continue;
+      const double c = register_chain_cost(m, r);
+      if (bm == n || c < best) { best = c; bm = m; rads = r; }
+    }
+    return bm;
+  }
   const std::vector<int> fn = factorize(n);
   const double base = line_pair_cost(n, fn, cut);
-  double best = (mode == 2 ? 0.8 : 0.5) * base;
+  double best = 0.8 * base;
   int bm = n;
   for (int m = 3 * cut + 1; m <= 2 * n; ++m) {
     if (m == n || (max_n && m > n)) continue;
@@ -918,6 +965,13 @@ int spx_set_product_grid(int32_t mode) {
 }
 
 int spx_plan_product_grid(const spx_plan* pl) { return pl ? pl->host.axm.n : 0; }
+
+int spx_plan_product_radices(const spx_plan* pl, int32_t* radices, int32_t max) {
+  if (!pl || (!radices && max > 0) || max < 0) { set_error("spx_plan_product_radices: bad argument"); return SPX_E_ARG; }
+  const AxisPlan& am = pl->host.axm;
+  for (int i = 0; i < am.nst && i < max; ++i) radices[i] = am.radix[i];
+  return am.nst;
+}
 
 int spx_product_grid_for(int32_t nx, int32_t cut, int32_t mode) {
   if (nx < 1 || mode < 0 || mode > 2) { set_error("spx_product_grid_for: bad argument"); return SPX_E_ARG; }

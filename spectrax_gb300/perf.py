@@ -116,10 +116,11 @@ def fft_line_ops(n: int, cut: int | None = None, mode: str = "dit", radices=None
     return o
 
 
-def rhs_ops(shape, tile=None, ntiles=None, product_grid=None, packed=False) -> Ops:
+def rhs_ops(shape, tile=None, ntiles=None, product_grid=None, packed=False, radices=None) -> Ops:
     """FP64 work of one right-hand-side evaluation (fused 1D1V or general path).
     product_grid: length of the 1D1V products' grid (the plan's; default Nx),
-    transformed with the cheapest radix order the plan builder tries.
+    transformed with `radices` (the plan's Stockham radices, Plan.product_radices;
+    default: the cheapest of the orders the FP64-count rule tries).
     packed (1D1V, exactly Hermitian state): the work the stage kernels execute
     with packed real transforms -- two real lines per complex transform, per tile
     of nt planes ceil((nt + 1) / 2) inverse and ceil(nt / 2) forward transforms,
@@ -130,7 +131,9 @@ def rhs_ops(shape, tile=None, ntiles=None, product_grid=None, packed=False) -> O
     if Ny == 1 and Nz == 1 and Nm == 1 and Np == 1:
         cut = Nx // 3
         M = product_grid or Nx
-        if M == Nx:
+        if radices:
+            rad = list(radices)
+        elif M == Nx:
             rad = factorize(Nx)
         else:
             rad = min(radix_orders(M), key=lambda r: fft_line_ops(M, cut, "dit", r).instr +

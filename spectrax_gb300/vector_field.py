@@ -45,6 +45,9 @@ class Plan:
         _lib.check(L.spx_plan_info(h, C.byref(t), C.byref(nt), C.byref(th), C.byref(path)), "spx_plan_info")
         self.tile, self.ntiles, self.threads, self.path = t.value, nt.value, th.value, path.value
         self.product_grid = int(L.spx_plan_product_grid(h))
+        rads = (C.c_int32 * 16)()
+        nr = int(L.spx_plan_product_radices(h, rads, 16))
+        self.product_radices = tuple(int(rads[i]) for i in range(min(max(nr, 0), 16)))
 
     @property
     def shape(self):
@@ -166,9 +169,10 @@ _GRID_MODES = {"auto": 0, "nx": 1, "fp64": 2}
 
 def set_product_grid(mode: str) -> None:
     """Grid of the nonlinear products in the 1D1V stepper kernels for plans made
-    from now on (spx_set_product_grid): "auto" (a grid of M >= 3K + 1 points
-    where its transforms are modeled >= 2x cheaper, e.g. prime Nx), "nx" (always
-    Nx points) or "fp64" (the least modeled FP64 work).  Results agree to rounding."""
+    from now on (spx_set_product_grid): "auto" (an Nx with a prime factor >= 5
+    takes the 2^a 3^b length M >= 3K + 1 of least modeled time in radix-4/3/2
+    stages, e.g. 129 -> 144), "nx" (always Nx points) or "fp64" (the least FP64
+    count).  Results agree to rounding."""
     global _product_grid
     if mode not in _GRID_MODES:
         raise ValueError("mode must be one of " + ", ".join(_GRID_MODES))

@@ -58,13 +58,16 @@ def test_no_cpu_fallback_in_product():
 
 
 @pytest.mark.parametrize("nx,cut,mode,expect", [
-    (129, 43, 0, 129),   # default: the benchmark's 43 x 3 transform stays
-    (127, 42, 0, 128),   # prime lengths take a >= 2x cheaper grid
-    (97, 32, 0, 104),
+    (129, 43, 0, 144),   # default: an Nx with a prime factor >= 5 takes a 2^a 3^b grid (4*4*3*3)
+    (127, 42, 0, 128),
+    (97, 32, 0, 108),
     (251, 83, 0, 256),
-    (65, 21, 0, 65),
-    (17, 5, 0, 17),
-    (129, 43, 2, 136),   # least modeled FP64 work, no extra Stockham stage
+    (65, 21, 0, 64),
+    (33, 11, 0, 36),
+    (17, 5, 0, 16),
+    (151, 50, 0, 192),
+    (96, 32, 0, 96),     # Nx = 2^a 3^b keeps its own grid
+    (129, 43, 2, 136),   # least FP64 count, no extra Stockham stage
     (65, 21, 2, 64),
     (33, 11, 2, 33),
     (129, 43, 1, 129),   # always Nx

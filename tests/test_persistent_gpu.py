@@ -40,6 +40,16 @@ def _run(plan, p, y0, t1, dt, ts, adaptive, persistent, max_steps=100000):
     return s, status
 
 
+def _nx_plan(p, tile):
+    # the persistent kernel is compiled for Nx-point products: plans on the Nx grid
+    from spectrax_gb300 import vector_field
+    vector_field.set_product_grid("nx")
+    try:
+        return vector_field.get_plan(vector_field.problem_from_params(p, "divide"), None, tile, 256)
+    finally:
+        vector_field.set_product_grid("auto")
+
+
 CASES = [
     # name, Nx, Nn, Ns, hermitian, adaptive, dt0, t1, tile
     ("herm_adaptive_65", 65, 40, 3, True, True, 0.2, 2.0, 0),
@@ -52,9 +62,8 @@ CASES = [
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,Nx,Nn,Ns,herm,adaptive,dt,t1,tile", CASES, ids=[c[0] for c in CASES])
 def test_persistent_matches_stage_launches(name, Nx, Nn, Ns, herm, adaptive, dt, t1, tile):
-    from spectrax_gb300 import vector_field
     p = _params(Nx, Nn, Ns)
-    plan = vector_field.get_plan(vector_field.problem_from_params(p, "divide"), None, tile, 256)
+    plan = _nx_plan(p, tile)
     y0 = _state(Nx, Nn, Ns, herm)
     ts = np.linspace(0.0, t1, 7)
     a, sa = _run(plan, p, y0, t1, dt, ts, adaptive, persistent=True)
@@ -74,9 +83,8 @@ def test_persistent_matches_stage_launches(name, Nx, Nn, Ns, herm, adaptive, dt,
 
 @pytest.mark.gpu
 def test_persistent_stops_at_max_steps():
-    from spectrax_gb300 import vector_field
     p = _params(33, 8, 2)
-    plan = vector_field.get_plan(vector_field.problem_from_params(p, "divide"), None, 0, 256)
+    plan = _nx_plan(p, 0)
     y0 = _state(33, 8, 2, True)
     a, sa = _run(plan, p, y0, 10.0, 0.05, None, False, persistent=True, max_steps=13)
     b, sb = _run(plan, p, y0, 10.0, 0.05, None, False, persistent=False, max_steps=13)
@@ -91,9 +99,9 @@ def test_bounded_counter_wait_times_out_and_the_context_stays_usable():
     # publishes, 1000 polls): the solve must stop with SPX_ST_WAIT_TIMEOUT, the
     # wrapper must raise, and the same solver must then run normally again
     import torch
-    from spectrax_gb300 import _lib, dopri8, vector_field
+    from spectrax_gb300 import _lib, dopri8
     p = _params(33, 16, 2)
-    plan = vector_field.get_plan(vector_field.problem_from_params(p, "divide"), None, 0, 256)
+    plan = _nx_plan(p, 0)
     y0 = _state(33, 16, 2, True)
     s = dopri8.Dopri8Solver(plan, 0.0, 1.0, 0.05, ts=np.linspace(0, 1.0, 5), adaptive=False,
                             masses=dopri8.species_masses(p), persistent=True, saveat="land")

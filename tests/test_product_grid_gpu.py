@@ -48,9 +48,12 @@ CASES = [  # Nx, mask, grid mode, expected product grid, Nn, Ns, Hermitian state
     (129, "divide", "fp64", 136, 10, 2, False),   # Nx = 3K: the folded term is added back
     (129, "divide", "fp64", 136, 10, 2, True),    # same, packed real transforms
     (65, "divide", "fp64", 64, 12, 2, True),
-    (97, "divide", "auto", 104, 6, 2, False),     # prime Nx: the default mode takes it
-    (129, "divide", "auto", 129, 6, 2, True),     # the default keeps the benchmark's grid
-    (33, "divide", "fp64", 33, 9, 2, True),       # no cheaper grid: unchanged
+    (97, "divide", "auto", 108, 6, 2, False),     # prime Nx
+    (129, "divide", "auto", 144, 6, 2, True),     # the benchmark's grid: 4*4*3*3, Nx = 3K
+    (129, "divide", "auto", 144, 7, 3, False),
+    (33, "divide", "auto", 36, 9, 2, True),       # Nx = 3K, Ns * tiles > 1
+    (17, "divide", "auto", 16, 7, 3, False),
+    (33, "divide", "fp64", 33, 9, 2, True),       # no cheaper grid by the FP64 count: unchanged
     (17, "divide", "fp64", 17, 7, 3, False),
 ]
 
@@ -82,7 +85,7 @@ def test_persistent_request_falls_back_on_a_product_grid():
     try:
         vector_field.set_product_grid("auto")
         plan = vector_field.plan_for_params(p, "divide")
-        assert plan.product_grid == 104
+        assert plan.product_grid == 108
         out = []
         for persistent in (True, False):
             s = dopri8.Dopri8Solver(plan, 0.0, 0.1, 0.02, ts=np.linspace(0, 0.1, 3), adaptive=False,
