@@ -6,10 +6,10 @@ is solved matrix-free by restarted GMRES whose matrix-vector product is the
 hand-written linearised right-hand side (``spx_linearize`` once per Newton
 system, then ``spx_jvp_lin`` per product).  The Newton stopping rule is
 the reference's (scaled 2-norm < 1, at most 300 iterations,
-spectrax/midpoint_solver.py:56-98); the inner solve uses restart 30 and a
-relative tolerance of 1e-10 by default, a deliberate difference from the
-reference's Eisenstat-Walker tolerance with maxiter 20, so parity is on the
-converged root rather than on the iterates.
+spectrax/midpoint_solver.py:56-98); the inner solve uses restart 30 and, by
+default, a fixed relative tolerance of 1e-10 (parity on the converged root), or
+with gmres_tol=None the reference's Eisenstat-Walker tolerance min(0.1, norm/2)
+with absolute tolerance atol, at most 20 restarts.
 
 Krylov vectors live in one (restart+1, n) complex128 block on the device; the
 orthogonalisation is classical Gram-Schmidt with one re-orthogonalisation pass
@@ -37,7 +37,8 @@ class NewtonGMRES:
         self.m = int(restart)
         if not 1 <= self.m < _lib.KRYLOV_MAX_ROWS:
             raise ValueError(f"restart must be in [1, {_lib.KRYLOV_MAX_ROWS - 1}]")
-        self.tol = float(gmres_tol)
+        # None: the reference's Eisenstat-Walker rule, set per Newton system by step()
+        self.tol = None if gmres_tol is None else float(gmres_tol)
         self.maxiter = int(gmres_maxiter)
         n = plan.state_len
         dev = plan.device
@@ -74,15 +75,18 @@ class NewtonGMRES:
                                               C.c_void_p(coef.data_ptr()), C.c_void_p(x.data_ptr()),
                                               _stream_ptr(None)), "spx_krylov_axpy")
 
-    def solve(self, ymid, b, c, atol=0.0):
-        """Solve (I - c J(ymid)) x = b; returns (x, relative residual, iterations)."""
+    def solve(self, ymid, b, c, atol=0.0, tol=None):
+        """Solve (I - c J(ymid)) x = b to ||r|| <= max(tol ||b||, atol) (tol: this
+        call's relative tolerance, default the solver's); returns (x, relative
+        residual, iterations)."""
         V, w, m = self.V, self.w, self.m
+        tol = self.tol if tol is None else tol
         self.plan.linearize(ymid, self.lin)
         x = torch.zeros_like(b)
         bnorm = torch.linalg.vector_norm(b).item()
         if bnorm == 0.0:
             return x, 0.0, 0
-        target = max(self.tol * bnorm, atol)
+        target = max(tol * bnorm, atol)
         r = b.clone()
         beta = bnorm
         its = 0
@@ -191,8 +195,13 @@ def step(plan: Plan, y0, dt, rtol, atol, max_iters=300, solver: NewtonGMRES | No
         norm = math.sqrt(glue.residual(y0, y1, glue.fmid, dt, rtol, atol))
         if norm < 1.0:
             break
-        # (I - dt/2 J(y_mid)) delta = -res: solve with +res and subtract
-        delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=0.0)
+        # (I - dt/2 J(y_mid)) delta = -res: solve with +res and subtract.  A solver
+        # without its own tolerance takes the reference's Eisenstat-Walker rule:
+        # relative min(0.1, norm / 2), absolute atol (spectrax/midpoint_solver.py:80-89)
+        if solver.tol is None:
+            delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=atol, tol=min(0.1, 0.5 * norm))
+        else:
+            delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=0.0)
         glue.update(y0, y1, delta, -1.0)
         newton += 1
     if stats is not None:
@@ -308,6 +317,7 @@ def solve(plan: Plan, y0, t_max, dt, ts, solver: ImplicitMidpoint, masses, save_
         h_prop = h_next if adaptive else h_prop
     info["matvecs"] = ng.matvecs
     info["t"] = t
+    info["y"] = y                                    # the final state (device)
     ys_np = torch.stack(ys).cpu().numpy() if save_states and ys else None
     return ys_np, np.array(en), info
 

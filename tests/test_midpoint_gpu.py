@@ -48,6 +48,24 @@ def test_midpoint_step_matches_oracle(shape):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(4, 5, 1, 2, 2, 2, 1), (9, 1, 1, 12, 1, 1, 2)], ids=lambda s: "x".join(map(str, s)))
+def test_midpoint_step_eisenstat_walker(shape):
+    # the reference's inner tolerance min(0.1, norm / 2) (gmres_tol=None): Newton stops
+    # on the same scaled-norm rule, so the step agrees with the tight solve to ~rtol
+    import torch
+    from spectrax_gb300 import midpoint, vector_field
+    p = _params(shape)
+    y0 = _state(shape)
+    ref, _, _ = omid.step(lambda y: orhs.rhs(p, y), y0, 0.1, rtol=1e-10, atol=1e-10)
+    plan = vector_field.plan_for_params(p, "divide")
+    ng = midpoint.NewtonGMRES(plan, restart=30, gmres_tol=None)
+    st = {}
+    y1, _, _ = midpoint.step(plan, torch.from_numpy(y0).cuda(), 0.1, 1e-10, 1e-10, solver=ng, stats=st)
+    assert st["newton"] >= 1
+    assert rel_err(y1.cpu().numpy(), ref) < 1e-8
+
+
+@pytest.mark.gpu
 def test_gmres_solves_linear_system():
     import torch
     from spectrax_gb300 import midpoint, vector_field
