@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(NTHREADS) k_param_dots_1v(const DevPlan* __res
 // ws: part (Ns * ntiles * N double2) | pp (grid x (2 + SPX_MAX_SPECIES) doubles) |
 // gpart (Ns * groups * N double2); the tickets live in the plan (calls on one
 // plan are serialised, as its workspace is).
-template <bool HERM>
+template <bool HERM, bool MG>
 __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __restrict__ gP,
                                                               const double2* __restrict__ gtab,
                                                               const double2* __restrict__ y,
@@ -204,10 +204,12 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
   const int nblk = P.pb.Ns * P.ntiles;
   const int N = P.ax[1].n, Nn = P.pb.Nn, T = P.tile;
   const int nk = 2 + P.pb.Ns;
-  // work area: sA, sB (2T+2 lines each) | Uy, Uw (T+2 lines each) | yF3, wE (3 lines each) | coefficients
+  // work area: sA, sB (2T+2 lines of Lw = max(Nx, product grid) each) | Uy, Uw (T+2
+  // lines of Nx each) | yF3, wE (3 lines each) | coefficients
+  const int Lw = MG ? max(N, P.axm.n) : N;
   double2* sA = stab + (P.tab_len + 15) / 16 * 16;
-  double2* sB = sA + (size_t)(2 * T + 2) * N;
-  double2* Uy = sB + (size_t)(2 * T + 2) * N;
+  double2* sB = sA + (size_t)(2 * T + 2) * Lw;
+  double2* Uy = sB + (size_t)(2 * T + 2) * Lw;
   double2* Uw = Uy + (size_t)(T + 2) * N;
   double2* yF3 = Uw + (size_t)(T + 2) * N;
   double2* wE = yF3 + 3 * (size_t)N;
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_vjp_param_1v(const DevPlan* __r
         timed_out = true;
       } else {
         double pacc[3] = {0.0, 0.0, 0.0};
-        vjp1v_tile_u<HERM>(P, stab, Uy, Uw, yF3, wE, g, part, s, tile, m0, nt, sA, sB, scoef, pacc);
+        vjp1v_tile_u<HERM, MG>(P, stab, Uy, Uw, yF3, wE, g, part, s, tile, m0, nt, sA, sB, scoef, pacc);
 #pragma unroll
         for (int k = 0; k < 2 + SPX_MAX_SPECIES; ++k)
           loc[k] = (k == 0) ? pacc[0] : (k == 1) ? pacc[1] : (k == 2 + s) ? pacc[2] : 0.0;
@@ -346,10 +348,15 @@ static int adj_setup() {
   SPX_RK_ATTR(false, true)
   SPX_RK_ATTR(true, true)
 #undef SPX_RK_ATTR
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v<false>));
-  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v<true>));
-  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+#define SPX_VJP_ATTR(H, G)                                                                             \
+  SPX_CUDA(cudaFuncGetAttributes(&fa, k_vjp_param_1v<H, G>));                                          \
+  SPX_CUDA(cudaFuncSetAttribute(k_vjp_param_1v<H, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                optin - (int)fa.sharedSizeBytes));
+  SPX_VJP_ATTR(false, false)
+  SPX_VJP_ATTR(true, false)
+  SPX_VJP_ATTR(false, true)
+  SPX_VJP_ATTR(true, true)
+#undef SPX_VJP_ATTR
   SPX_CUDA(cudaFuncGetAttributes(&fa, k_param_dots_1v));
   SPX_CUDA(cudaFuncSetAttribute(k_param_dots_1v, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
   done = true;
@@ -502,12 +509,22 @@ int spx_vjp_param_ex(const spx_plan* pl, const void* y, const void* w, void* g, 
   unsigned int* ticket = pl->d_ticket;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int T = P.tile, N = P.ax[1].n;
-  const size_t smem = pl->smem_tab + (size_t)(6 * T + 14) * N * sizeof(double2) + 64 * sizeof(double);
+  // the transposed products on the plan's product grid where it has one without
+  // the folded |k| = K term (that term's transpose is only on the Nx-point grid)
+  const bool mg = P.axm.n != N && P.alias == 0;
+  const int Lw = mg ? std::max(N, P.axm.n) : N;
+  const size_t smem = pl->smem_tab + ((size_t)(4 * T + 4) * Lw + (size_t)(2 * T + 10) * N) * sizeof(double2) +
+                      64 * sizeof(double);
+  if (smem > (size_t)smem_optin()) {
+    set_error("spx_vjp_param: the tile does not fit in shared memory");
+    return SPX_E_UNSUPPORTED;
+  }
   const DevPlan* dp = pl->d_plan;
   const double2* dt = pl->d_tab;
   // a plain launch: with a programmatic early start the CTAs of this small grid
   // (one per SM) were placed less evenly and the kernel ran longer
-  auto kern = hermitian ? k_vjp_param_1v<true> : k_vjp_param_1v<false>;
+  auto kern = hermitian ? (mg ? k_vjp_param_1v<true, true> : k_vjp_param_1v<true, false>)
+                        : (mg ? k_vjp_param_1v<false, true> : k_vjp_param_1v<false, false>);
   kern<<<grid, pl->threads, smem, st>>>(dp, dt, static_cast<const double2*>(y), static_cast<const double2*>(w),
                                         static_cast<double2*>(g), reinterpret_cast<double2*>(wsb), pp, gpart,
                                         ticket, acc);

@@ -1081,13 +1081,22 @@ __device__ inline void vjp1v_tile(const DevPlan& P, const double2* __restrict__ 
 // ((nt+2)*N each, zero outside [0, Nn)); yF3: y's E_x, B_z, B_y lines; wE: w's
 // E_x, E_y, E_z lines (3*N each).  pacc (3 doubles) accumulates the parameter
 // terms of the own planes: Re w . (-col C), Re w . f_K, Re w . (-i K C).
-template <bool HERM>
+// MG: the transposed products on the plan's product grid axm (Lm points, mode k
+// at position k mod Lm; sA / sB hold lines of Lm): every factor is masked, so the
+// kept modes are the Nx-grid ones times Lm / Nx, undone by rnm = Nx / Lm.  Only
+// for plans without the folded term (alias == 0).
+template <bool HERM, bool MG = false>
 __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict__ tab,
                                     const double2* Uy, const double2* Uw, const double2* yF3,
                                     const double2* wE, double2* __restrict__ g,
                                     double2* __restrict__ part, int s, int tile, int m0, int nt,
                                     double2* sA, double2* sB, double* scoef, double* pacc) {
   const int N = P.ax[1].n, cut = P.ax[1].cut, Nn = P.pb.Nn;
+  const AxisPlan& am = MG ? P.axm : P.ax[1];
+  const int Lm = MG ? am.n : N, half = N / 2;
+  const double rn = MG ? P.rnm : 1.0;
+  // grid position of the mode at centred index c (std_index(c, N) when Lm == N)
+  auto pos = [&](int c) { const int k = c - half; return k < 0 ? k + Lm : k; };
   const double a0 = P.pb.alpha_s[3 * s], a1 = P.pb.alpha_s[3 * s + 1], a2 = P.pb.alpha_s[3 * s + 2];
   const double u0 = P.pb.u_s[3 * s], u1 = P.pb.u_s[3 * s + 1], u2 = P.pb.u_s[3 * s + 2];
   if (threadIdx.x < nt) {
@@ -1095,7 +1104,7 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
     double* c = scoef + 4 * threadIdx.x;
     const double* t = P.coef + ((size_t)s * Nn + m) * COEF_1V;
     c[0] = t[0]; c[1] = t[1];
-    c[2] = (m + 1 < Nn) ? t[COEF_1V + 2] : 0.0;   // k_{m+1}
+    c[2] = (m + 1 < Nn) ? t[COEF_1V + 2] * rn : 0.0;   // k_{m+1} (x rn on the product grid)
     c[3] = t[4];
   }
   // spectrum (masked, centred index c) of line q of [G_y | c_m (nt) | conj W_{m+1} (nt)]
@@ -1115,60 +1124,64 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
   double2* Rp = part + ((size_t)s * P.ntiles + tile) * N;
   if constexpr (!HERM) {
     const int nl = 2 * nt + 1;
-    for (int i = threadIdx.x; i < nl * N; i += blockDim.x) {
-      const int l = i / N, c = i - l * N;
-      sA[l * N + std_index(c, N)] = kept(c, N, cut) ? spec(l, c) : make_double2(0.0, 0.0);
+    // masked spectra at their grid positions (every position of the Lm-point lines)
+    for (int i = threadIdx.x; i < nl * Lm; i += blockDim.x) {
+      const int l = i / Lm, x = i - l * Lm;
+      const int k = x < (Lm + 1) / 2 ? x : x - Lm;
+      sA[i] = (k >= -cut && k <= cut) ? spec(l, k + half) : make_double2(0.0, 0.0);
     }
     __syncthreads();
-    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nl, 1, 1, N, 0}, cut);
+    double2* r = fft_axis_t<true, false>(sA, sB, am, tab, Lines{nl, 1, 1, Lm, 0}, cut);
     double2* o = (r == sA) ? sB : sA;
     // this tile's share of the field sum R_s(x) = sum_n k_n c_{n-1}(x) W_n(x), as an
     // extra line after the nt product lines: its inverse transform (masked) goes
     // through the same pass, and the tile stores the kept modes as its partial
-    for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    for (int x = threadIdx.x; x < Lm; x += blockDim.x) {
       double2 acc = make_double2(0.0, 0.0);
       for (int l = 0; l < nt; ++l) {
         const double k = scoef[4 * l + 2];
-        const double2 wt = r[(1 + nt + l) * N + x];
-        acc = cfma(cscale(k, r[(1 + l) * N + x]), make_double2(wt.x, -wt.y), acc);
+        const double2 wt = r[(1 + nt + l) * Lm + x];
+        acc = cfma(cscale(k, r[(1 + l) * Lm + x]), make_double2(wt.x, -wt.y), acc);
       }
-      r[(1 + 2 * nt) * N + x] = acc;
+      r[(1 + 2 * nt) * Lm + x] = acc;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nt * N; i += blockDim.x) {
-      const int x = i % N;
-      const double2 wt = r[(1 + nt) * N + i];
-      r[(1 + nt) * N + i] = cmul(r[x], make_double2(wt.x, -wt.y));
+    for (int i = threadIdx.x; i < nt * Lm; i += blockDim.x) {
+      const int x = i % Lm;
+      const double2 wt = r[(1 + nt) * Lm + i];
+      r[(1 + nt) * Lm + i] = cmul(r[x], make_double2(wt.x, -wt.y));
     }
     __syncthreads();
-    q = fft_axis_t<true, true>(r + (1 + nt) * N, o + (1 + nt) * N, P.ax[1], tab, Lines{nt + 1, 1, 1, N, 0}, cut);
+    q = fft_axis_t<true, true>(r + (1 + nt) * Lm, o + (1 + nt) * Lm, am, tab, Lines{nt + 1, 1, 1, Lm, 0}, cut);
     for (int c = threadIdx.x; c < N; c += blockDim.x)
-      Rp[c] = kept(c, N, cut) ? q[nt * N + std_index(c, N)] : make_double2(0.0, 0.0);
+      Rp[c] = kept(c, N, cut) ? q[nt * Lm + pos(c)] : make_double2(0.0, 0.0);
   } else {
     // Exactly Hermitian y and w: every real-space line is real, so two lines share
     // one complex transform (inverse of X_a + i X_b is x_a + i x_b).
     const int nreal = 2 * nt + 1, nin = nt + 1;
-    for (int i = threadIdx.x; i < nin * N; i += blockDim.x) {
-      const int j = i / N, c = i - j * N;
+    for (int i = threadIdx.x; i < nin * Lm; i += blockDim.x) {
+      const int j = i / Lm, x = i - j * Lm;
+      const int k = x < (Lm + 1) / 2 ? x : x - Lm;
       double2 z = make_double2(0.0, 0.0);
-      if (kept(c, N, cut)) {
+      if (k >= -cut && k <= cut) {
+        const int c = k + half;
         const double2 xa = spec(2 * j, c);
         const double2 xb = (2 * j + 1 < nreal) ? spec(2 * j + 1, c) : make_double2(0.0, 0.0);
         z = make_double2(xa.x - xb.y, xa.y + xb.x);
       }
-      sA[j * N + std_index(c, N)] = z;
+      sA[i] = z;
     }
     __syncthreads();
-    double2* r = fft_axis_t<true, false>(sA, sB, P.ax[1], tab, Lines{nin, 1, 1, N, 0}, cut);
+    double2* r = fft_axis_t<true, false>(sA, sB, am, tab, Lines{nin, 1, 1, Lm, 0}, cut);
     double2* o = (r == sA) ? sB : sA;
     auto rl = [&](int ql, int x) -> double {
-      const double2 z = r[(ql >> 1) * N + x];
+      const double2 z = r[(ql >> 1) * Lm + x];
       return (ql & 1) ? z.y : z.x;
     };
     // real lines p_l = G W_l (l < nt) and R = sum_l k_{m0+l+1} c_l W_l, in pairs
     const int nprod = nt + 1, nout = (nprod + 1) / 2;
-    for (int i = threadIdx.x; i < nout * N; i += blockDim.x) {
-      const int j = i / N, x = i - j * N;
+    for (int i = threadIdx.x; i < nout * Lm; i += blockDim.x) {
+      const int j = i / Lm, x = i - j * Lm;
       double pv[2];
 #pragma unroll
       for (int h2 = 0; h2 < 2; ++h2) {
@@ -1181,17 +1194,17 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
         }
         pv[h2] = v;
       }
-      o[j * N + x] = make_double2(pv[0], pv[1]);
+      o[j * Lm + x] = make_double2(pv[0], pv[1]);
     }
     __syncthreads();
-    double2* qq = fft_axis_t<true, true>(o, r, P.ax[1], tab, Lines{nout, 1, 1, N, 0}, cut);
+    double2* qq = fft_axis_t<true, true>(o, r, am, tab, Lines{nout, 1, 1, Lm, 0}, cut);
     q = qq;
     // R's spectrum: P_b of a pair (nt odd) or P_a (nt even), at every kept mode
     for (int c = threadIdx.x; c < N; c += blockDim.x) {
       double2 v = make_double2(0.0, 0.0);
       if (kept(c, N, cut)) {
-        const double2* fl = qq + (nt >> 1) * N;
-        const double2 W = fl[std_index(c, N)], Wm = fl[std_index(N - 1 - c, N)];
+        const double2* fl = qq + (nt >> 1) * Lm;
+        const double2 W = fl[pos(c)], Wm = fl[pos(N - 1 - c)];
         v = (nt & 1) ? make_double2(0.5 * (W.y + Wm.y), 0.5 * (Wm.x - W.x))
                      : make_double2(0.5 * (W.x + Wm.x), 0.5 * (W.y - Wm.y));
       }
@@ -1232,10 +1245,10 @@ __device__ inline void vjp1v_tile_u(const DevPlan& P, const double2* __restrict_
     if (m + 1 < Nn && kept(c, N, cut)) {
       double2 v;
       if constexpr (!HERM) {
-        v = q[l * N + std_index(c, N)];
+        v = q[l * Lm + pos(c)];
       } else {
-        const double2* fl = q + (l >> 1) * N;
-        const double2 W = fl[std_index(c, N)], Wn = fl[std_index(c2, N)];
+        const double2* fl = q + (l >> 1) * Lm;
+        const double2 W = fl[pos(c)], Wn = fl[pos(c2)];
         v = (l & 1) ? make_double2(0.5 * (W.y + Wn.y), 0.5 * (Wn.x - W.x))
                     : make_double2(0.5 * (W.x + Wn.x), 0.5 * (W.y - Wn.y));
       }

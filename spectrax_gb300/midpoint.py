@@ -20,6 +20,7 @@ least-squares problem is solved on the host with Givens rotations.
 from __future__ import annotations
 
 import math
+import time
 
 import numpy as np
 import torch
@@ -75,10 +76,11 @@ class NewtonGMRES:
                                               C.c_void_p(coef.data_ptr()), C.c_void_p(x.data_ptr()),
                                               _stream_ptr(None)), "spx_krylov_axpy")
 
-    def solve(self, ymid, b, c, atol=0.0, tol=None):
+    def solve(self, ymid, b, c, atol=0.0, tol=None, deadline=None):
         """Solve (I - c J(ymid)) x = b to ||r|| <= max(tol ||b||, atol) (tol: this
         call's relative tolerance, default the solver's); returns (x, relative
-        residual, iterations)."""
+        residual, iterations).  deadline (time.perf_counter() value): stop the
+        Arnoldi process there and return the current iterate."""
         V, w, m = self.V, self.w, self.m
         tol = self.tol if tol is None else tol
         self.plan.linearize(ymid, self.lin)
@@ -130,6 +132,8 @@ class NewtonGMRES:
                     torch.div(w, hn, out=V[j + 1])
                 if res <= target or hn == 0.0:
                     break
+                if deadline is not None and time.perf_counter() > deadline:
+                    break
             # back substitution and update
             k = k_done
             yk = np.zeros(k, np.complex128)
@@ -142,7 +146,7 @@ class NewtonGMRES:
             r = b - w
             beta = torch.linalg.vector_norm(r).item()
             rel = beta / bnorm
-            if beta <= target:
+            if beta <= target or (deadline is not None and time.perf_counter() > deadline):
                 break
         return x, rel, its
 
@@ -179,7 +183,7 @@ class _Glue:
 
 
 def step(plan: Plan, y0, dt, rtol, atol, max_iters=300, solver: NewtonGMRES | None = None, stats=None,
-         glue: _Glue | None = None, f0=None, want_error=True):
+         glue: _Glue | None = None, f0=None, want_error=True, deadline=None):
     """One implicit midpoint step; returns (y1, y_error, f0) with y_error = y1 - (y0 + dt f(y0))
     (spectrax/midpoint_solver.py:37-53; None unless want_error).  Per Newton iteration: one right-hand side at
     y_mid, one fused residual + scaled-norm pass with a single scalar read, the GMRES
@@ -199,11 +203,17 @@ def step(plan: Plan, y0, dt, rtol, atol, max_iters=300, solver: NewtonGMRES | No
         # without its own tolerance takes the reference's Eisenstat-Walker rule:
         # relative min(0.1, norm / 2), absolute atol (spectrax/midpoint_solver.py:80-89)
         if solver.tol is None:
-            delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=atol, tol=min(0.1, 0.5 * norm))
+            delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=atol, tol=min(0.1, 0.5 * norm),
+                                             deadline=deadline)
         else:
-            delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=0.0)
+            delta, _rel, _its = solver.solve(glue.ymid, glue.res, 0.5 * dt, atol=0.0, deadline=deadline)
         glue.update(y0, y1, delta, -1.0)
         newton += 1
+        if deadline is not None and time.perf_counter() > deadline:
+            # a caller's wall-clock limit (benchmarks): the step is left unconverged
+            if stats is not None:
+                stats["deadline"] = True
+            break
     if stats is not None:
         stats["newton"] = stats.get("newton", 0) + newton
         stats["rhs"] = stats.get("rhs", 0) + newton + 2

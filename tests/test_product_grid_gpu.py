@@ -125,3 +125,39 @@ def test_adjoint_recomputation_on_a_product_grid():
     assert res["fp64"][0] == 64 and res["nx"][0] == 65
     for i in (1, 2, 3):
         assert rel_err(res["fp64"][i], res["nx"][i]) <= 1e-10, i
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("Nx,herm", [(65, True), (65, False), (17, True), (97, False)])
+def test_vjp_param_on_the_product_grid(Nx, herm):
+    # the adjoint sweep's kernel on a plan with its own product grid (no folded
+    # |k| = K term): the same g and parameter sums as on the Nx-point grid
+    import ctypes as C
+
+    import torch
+    from spectrax_gb300 import _lib, vector_field
+    from spectrax_gb300.vector_field import _stream_ptr
+    Nn, Ns = 12, 2
+    p = _params(Nx, Nn, Ns, Nx)
+    y = torch.from_numpy(_state(Nx, Nn, Ns, herm, 11)).cuda()
+    w = torch.from_numpy(_state(Nx, Nn, Ns, herm, 12)).cuda()
+    out = {}
+    for mode in ("auto", "nx"):
+        vector_field.set_product_grid(mode)
+        try:
+            plan = vector_field.plan_for_params(p, "divide")
+        finally:
+            vector_field.set_product_grid("auto")
+        g = torch.empty_like(y)
+        acc = torch.zeros(2 + _lib.MAX_SPECIES, dtype=torch.float64, device=y.device)
+        ws, wsb = plan.ws_ptr()
+        _lib.check(_lib.lib().spx_vjp_param_ex(plan.handle, C.c_void_p(y.data_ptr()), C.c_void_p(w.data_ptr()),
+                                                C.c_void_p(g.data_ptr()),
+                                                C.cast(C.c_void_p(acc.data_ptr()), C.POINTER(C.c_double)),
+                                                ws, wsb, int(herm), _stream_ptr()), "spx_vjp_param_ex")
+        torch.cuda.synchronize()
+        out[mode] = (plan.product_grid, g.cpu().numpy(), acc.cpu().numpy())
+    assert out["auto"][0] != Nx and out["nx"][0] == Nx
+    assert rel_err(out["auto"][1], out["nx"][1]) <= 1e-12
+    a, b = out["auto"][2][:2 + Ns], out["nx"][2][:2 + Ns]
+    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
