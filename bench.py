@@ -267,6 +267,7 @@ def run_extras(args):
         prob = TwoStreamProblem(Nx=65, Nn=128, dt=0.05, nsteps=2000, seed=0)
         th = dict(k=0.2, nu=1.0, u=0.5, amp=1e-3)
         prob.loss(**th)
+        prob.loss_and_grad(**th)              # first call captures the sweep's CUDA graphs
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         prob.loss(**th)
