@@ -251,6 +251,7 @@ def run_extras(args):
             "speedup": ts_serial / tb, "rhs_evals": int(sum(s["rhs_evals"] for s in stats)),
             "rhs_evals_per_s": sum(s["rhs_evals"] for s in stats) / tb,
             "cluster": best["cluster"], "tile": best["tile"],
+            "autotune_refined_ms_t2": [(r["cluster"], r["tile"], round(r["ms"], 2)) for r in best.get("refined", [])],
             "max_rel_err_state_vs_serial": err, "max_rel_err_field_energy_vs_serial": eerr,
             "hermitian_instances": int(sum(1 for s_ in stats if s_.get("hermitian"))),
             "serial_plain_rhs_s_estimated": tp_all, "speedup_vs_plain_rhs": tp_all / tb,

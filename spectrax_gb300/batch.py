@@ -168,11 +168,14 @@ def _signature(problems, t1, rtol):
 
 
 def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses=None,
-             clusters=(1, 2, 4, 8, 16), tiles=(4, 8, 16, 32, -1), use_cache=True, verbose=False):
-    """Time a short horizon of the real instances for every (cluster, tile) and
-    return the fastest as dict(cluster=, tile=, ms=, table=[...]).  tile -1: each
-    instance's tile height chosen to fill whole rounds of the cluster's CTAs."""
-    sig = _signature(problems, t1_probe, rtol)
+             clusters=(1, 2, 4, 8, 16), tiles=(4, 8, 16, 32, -1), use_cache=True, verbose=False,
+             refine=3, t1_refine=2.0):
+    """Time a short horizon of the real instances for every (cluster, tile), then
+    the `refine` fastest again over t1_refine (the short probe ranks close
+    candidates by the start-up transient of the step sizes), and return the
+    fastest as dict(cluster=, tile=, ms=, table=[...], refined=[...]).  tile -1:
+    each instance's tile height chosen to fill whole rounds of the cluster's CTAs."""
+    sig = _signature(problems, t1_probe, rtol) + f"|refine{refine}@{t1_refine:g}"
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -182,32 +185,44 @@ def autotune(problems, y0s, t1_probe=0.5, rtol=1e-8, atol=1e-8, dt0=0.01, masses
             cache = {}
         if sig in cache:
             return cache[sig]
-    ts = np.array([t1_probe])
+    def timed(c, t, t1):
+        try:
+            s = BatchSolver(problems, t1, dt0=dt0, rtol=rtol, atol=atol, save_ts=np.array([t1]), cluster=c,
+                            tile=t, masses=masses)
+        except _lib.SpectraxError:
+            return None
+        y0 = s.pack(y0s)
+        s.run(y0)                         # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        s.run(y0)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
     table = []
-    best = None
     for c in clusters:
         for t in tiles:
-            try:
-                s = BatchSolver(problems, t1_probe, dt0=dt0, rtol=rtol, atol=atol, save_ts=ts, cluster=c,
-                                tile=t, masses=masses)
-            except _lib.SpectraxError:
+            ms = timed(c, t, t1_probe)
+            if ms is None:
                 continue
-            y0 = s.pack(y0s)
-            s.run(y0)                     # warm-up
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            s.run(y0)
-            e1.record()
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1)
             table.append(dict(cluster=c, tile=t, ms=ms))
             if verbose:
                 print(f"autotune cluster={c} tile={t}: {ms:.2f} ms", flush=True)
-            if best is None or ms < best["ms"]:
-                best = dict(cluster=c, tile=t, ms=ms)
-            del s
-    best = dict(best, table=table)
+    if not table:
+        raise _lib.SpectraxError("batch autotune: no (cluster, tile) candidate could be created")
+    ranked = sorted(table, key=lambda r: r["ms"])
+    refined = []
+    if refine and refine > 1 and t1_refine > t1_probe:
+        for r in ranked[:refine]:
+            ms = timed(r["cluster"], r["tile"], t1_refine)
+            if ms is not None:
+                refined.append(dict(cluster=r["cluster"], tile=r["tile"], ms=ms))
+                if verbose:
+                    print(f"autotune refine cluster={r['cluster']} tile={r['tile']}: {ms:.2f} ms", flush=True)
+    best = min(refined, key=lambda r: r["ms"]) if refined else ranked[0]
+    best = dict(best, table=table, refined=refined)
     cache[sig] = best
     try:
         json.dump(cache, open(path, "w"))

@@ -151,3 +151,18 @@ def test_batch_hermitian_instances():
             L = ys[i].reshape(-1, it["shape"][0])
             if herm:
                 assert np.all(L == np.conj(L[:, ::-1]))          # symmetry kept exactly
+
+
+@pytest.mark.gpu
+def test_autotune_refines_the_fastest_candidates():
+    # the sweep over (cluster, tile) at a short horizon, then the fastest two again
+    # over a longer one; the choice is one of the refined candidates
+    from spectrax_gb300.batch import autotune, landau_scan
+    insts = landau_scan(12, seed=3)
+    best = autotune([it["problem"] for it in insts], [it["y0"] for it in insts], t1_probe=0.05,
+                    masses=[it["masses"] for it in insts], clusters=(1, 2), tiles=(4, 8), use_cache=False,
+                    refine=2, t1_refine=0.1)
+    assert len(best["table"]) == 4 and len(best["refined"]) == 2
+    assert (best["cluster"], best["tile"]) in {(r["cluster"], r["tile"]) for r in best["refined"]}
+    fastest_two = sorted(best["table"], key=lambda r: r["ms"])[:2]
+    assert {(r["cluster"], r["tile"]) for r in fastest_two} == {(r["cluster"], r["tile"]) for r in best["refined"]}
