@@ -98,3 +98,42 @@ def test_physics_curve_fixture():
     g = float(np.interp(0.5, d["damping_k"], d["damping_rate"]))
     assert -0.16 < g < -0.15
     assert np.max(d["growth_rate"]) > 0
+
+
+def test_oracle_two_stream_growth_rate_on_reference_curve(tmp_path):
+    # the oracle stepping the reference's growth-rate example (input file, initial
+    # state and box length of Examples/1D_two_stream_gr_curve.py:55-104 at
+    # k v_th / omega_pe = 0.5, adaptive Dopri8 to t = 80, fit over t[300:]):
+    # within 1 % of the tabulated curve (Examples/growth_rate.csv)
+    import os
+    from example_configs import configs, write_toml
+    from oracle import diag as odiag
+    from oracle import dopri8 as od
+    from oracle import rhs as orhs
+    from oracle import tables as otab
+    from spectrax_gb300.params import load_parameters
+    path = tmp_path / "gr.toml"
+    write_toml(configs()["input_1D_two_stream_gr_curve.toml"], path)
+    inp, sol = load_parameters(str(path))
+    kx = 0.5
+    a0, a3, dn1, dn2, nx = inp["alpha_s"][0], inp["alpha_s"][3], inp["dn1"], inp["dn2"], inp["nx"]
+    Nx, Nn, Ns = sol["Nx"], sol["Nn"], sol["Ns"]
+    idx = [int((Nx - 1) / 2 - nx), int((Nx - 1) / 2), int((Nx - 1) / 2 + nx)]
+    Ck0 = np.zeros((2 * Nn, 1, Nx, 1), np.complex128)
+    Ck0[0, 0, idx, 0] = [1j * dn1 / (2 * a0 ** 3), 1 / a0 ** 3, -1j * dn1 / (2 * a0 ** 3)]
+    Ck0[Nn, 0, idx, 0] = [1j * dn2 / (2 * a3 ** 3), 1 / a3 ** 3, -1j * dn2 / (2 * a3 ** 3)]
+    Lx = np.sqrt(2) * np.pi * a0 / kx
+    Fk0 = np.zeros((6, 1, Nx, 1), np.complex128)
+    Fk0[0, 0, [idx[0], idx[2]], 0] = (dn1 + dn2) * Lx / (4 * np.pi * nx * inp["Omega_cs"][0])
+    user = dict(inp)
+    user.update(Ck_0=Ck0, Fk_0=Fk0, Lx=Lx)
+    p = otab.initialize_simulation_parameters(user, Nx, 1, 1, Nn, 1, 1, Ns, sol["timesteps"], sol["dt"])
+    ts = np.linspace(0.0, p["t_max"], sol["timesteps"])
+    tol = inp["ode_tolerance"]
+    out = od.solve(lambda t, y: orhs.rhs(p, y, "divide"), 0.0, ts[-1], np.concatenate([Ck0.ravel(), Fk0.ravel()]),
+                   sol["dt"], ts=ts, adaptive=True, rtol=tol, atol=tol)
+    E = odiag.energies(out["ys"], Nx, 1, 1, Nn, 1, 1, Ns, p["alpha_s"], p["u_s"], p["Omega_cs"], mi_me=1.0)["EM_energy"]
+    gamma = np.polyfit(ts[300:], np.log(E[300:]), 1)[0] / 2
+    curve = np.load(os.path.join(os.path.dirname(__file__), "golden", "physics_curves.npz"))
+    g_ref = float(np.interp(kx, curve["growth_k"], curve["growth_rate"]))
+    assert abs(gamma - g_ref) <= 0.01 * g_ref, (gamma, g_ref)

@@ -57,3 +57,35 @@ def test_landau_run_matches_oracle():
     curve = np.load(os.path.join(os.path.dirname(__file__), "golden", "physics_curves.npz"))
     g_ref = float(np.interp(0.5, curve["damping_k"], curve["damping_rate"]))
     assert abs(gg - g_ref) <= 0.03 * abs(g_ref), (gg, g_ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kx", [0.3, 0.5])
+def test_two_stream_growth_rate_matches_reference_curve(kx, tmp_path):
+    # the reference's growth-rate scan (Examples/1D_two_stream_gr_curve.py:55-104)
+    # through the drop-in simulation(): its input file, its initial state and box
+    # length for the target k v_th / omega_pe, adaptive Dopri8 to t = 80 and the fit
+    # log E ~ 2 gamma t over t[300:]; against the reference's tabulated curve
+    # (Examples/growth_rate.csv, copied by tests/golden/make_physics_golden.py)
+    from example_configs import configs, write_toml
+    from spectrax_gb300.dopri8 import simulation
+    from spectrax_gb300.params import load_parameters
+    path = tmp_path / "gr.toml"
+    write_toml(configs()["input_1D_two_stream_gr_curve.toml"], path)
+    inp, sol = load_parameters(str(path))
+    a0, a3, dn1, dn2, nx = inp["alpha_s"][0], inp["alpha_s"][3], inp["dn1"], inp["dn2"], inp["nx"]
+    Nx, Nn = sol["Nx"], sol["Nn"]
+    idx = [int((Nx - 1) / 2 - nx), int((Nx - 1) / 2), int((Nx - 1) / 2 + nx)]
+    Ck0 = np.zeros((2 * Nn, 1, Nx, 1), np.complex128)
+    Ck0[0, 0, idx, 0] = [1j * dn1 / (2 * a0 ** 3), 1 / a0 ** 3, -1j * dn1 / (2 * a0 ** 3)]
+    Ck0[Nn, 0, idx, 0] = [1j * dn2 / (2 * a3 ** 3), 1 / a3 ** 3, -1j * dn2 / (2 * a3 ** 3)]
+    Lx = np.sqrt(2) * np.pi * a0 / kx
+    Fk0 = np.zeros((6, 1, Nx, 1), np.complex128)
+    Fk0[0, 0, [idx[0], idx[2]], 0] = (dn1 + dn2) * Lx / (4 * np.pi * nx * inp["Omega_cs"][0])
+    inp.update(Ck_0=Ck0, Fk_0=Fk0, Lx=Lx)
+    out = simulation(inp, **sol)
+    t, E = out["time"], out["EM_energy"]
+    gamma = np.polyfit(t[300:], np.log(E[300:]), 1)[0] / 2
+    curve = np.load(os.path.join(os.path.dirname(__file__), "golden", "physics_curves.npz"))
+    g_ref = float(np.interp(kx, curve["growth_k"], curve["growth_rate"]))
+    assert gamma > 0 and abs(gamma - g_ref) <= 0.03 * g_ref, (gamma, g_ref)
