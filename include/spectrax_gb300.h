@@ -283,8 +283,10 @@ int spx_param_dots(const spx_plan* plan, const void* y, const void* g, double* a
 /* g = J(y)^T w together with acc[k] += Re sum_e w_e (df/dtheta_k)_e for
  * theta = (nu, k (as k d/dk), u_x of each species): spx_vjp and spx_param_dots
  * in one launch, the parameter sums added in a fixed order.  ws as for spx_rhs
- * (spx_rhs_workspace_bytes); 1D1V layout only.  Calls on one plan must not run
- * concurrently (the plan holds the kernel's completion ticket). */
+ * (spx_rhs_workspace_bytes); 1D1V layout only.  On a plan with its own product
+ * grid (spx_plan_product_grid != Nx) and 3K != Nx the transposed products run on
+ * that grid, agreeing with the Nx-point grid to rounding.  Calls on one plan must
+ * not run concurrently (the plan holds the kernel's completion ticket). */
 int spx_vjp_param(const spx_plan* plan, const void* y, const void* w, void* g, double* acc, void* ws,
                   size_t ws_bytes, void* stream);
 /* The same with `hermitian` = 1 for exactly Hermitian y and w: every real-space
