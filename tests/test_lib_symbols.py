@@ -99,3 +99,26 @@ def test_product_grid_mode_setter_without_gpu():
     finally:
         vector_field.set_product_grid("auto")
     assert vector_field.get_product_grid() == "auto"
+
+
+def test_product_grid_rule_properties_without_gpu():
+    # for every Nx up to 300 and the 2/3 cut: the default grid is Nx itself (Nx of
+    # the form 2^a 3^b, or a cut whose Nx-point product folds more than one term)
+    # or a length M = 2^a 3^b with 3 cut + 1 <= M <= 2 Nx
+    from spectrax_gb300 import _lib
+    L = _lib.lib()
+
+    def smooth(m):
+        for p in (2, 3):
+            while m % p == 0:
+                m //= p
+        return m == 1
+
+    for nx in range(1, 301):
+        cut = nx // 3
+        m = L.spx_product_grid_for(nx, cut, 0)
+        if m == nx:
+            assert smooth(nx) or nx < 8 or cut < 1 or 3 * cut > nx or not any(
+                smooth(k) for k in range(3 * cut + 1, 2 * nx + 1)), (nx, m)
+        else:
+            assert not smooth(nx) and smooth(m) and 3 * cut + 1 <= m <= 2 * nx, (nx, cut, m)
